@@ -1,0 +1,450 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 BVE path: RK4 steps/s on one solve at icosahedral level 7.
+
+Workload (the single-solve configuration the headline metric is quoted on): icosahedral
+level 7 (163,842 vertices; 436,900 faces of which 327,680 leaves are the sources), RH54
+relative vorticity plus 3 seeded Gaussian vortices (amplitude U(-2,2), width 0.1 rad),
+Omega = 2 pi, eps = 0, dt = 0.01.  A step is one RK4 step (four direct-sum evaluations
+over every vertex and face target).  Synthetic data generated on the host; nothing is
+downloaded.
+
+Printed JSON line (rank 0):
+  value      RK4 steps/s, whole job, device-resident inputs, graph-replayed steps
+  e2e        the same through lpm_bve_rk4_step with the state copied host->device before
+             and device->host after every step (pinned buffers)
+  roofline   pair kernel: algorithmic pairs per launch / CUDA-event launch time, against
+             the FP32 FMA-pipe peak (13 FMA-pipe lane-ops per pair)
+  cpu_baseline  the CPU oracle (OpenMP restatement of the reference path) on the host cores
+  fp64_gpu   the plain FP64 GPU path on a sample of targets, and FP32C-vs-FP64 error there
+
+--impl reference times the reference's CPU path (the oracle port; the reference itself
+cannot be built here) on the same workload, each step a bounded sample of targets.
+Under torchrun (N > 1) every rank advances its own replica of the solve ("scaling": "weak").
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+SEED_BASE = 20261203
+WORKLOAD = dict(seed_kind=0, level=7, ngauss=3, width=0.1, dt=0.01, omega=2 * math.pi, eps=0.0,
+                ic_seed=SEED_BASE + 1)
+OPS_PER_PAIR = 13  # FP32 FMA-pipe lane operations per velocity pair in the FP32C kernel
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--level", type=int, default=WORKLOAD["level"])
+    ap.add_argument("--prec", choices=["fp32c", "fp64"], default="fp32c")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
+    return ap.parse_args()
+
+
+def max_over_ranks(x: float, world: int, device=None) -> float:
+    """Maximum of a per-rank scalar (timings: the job is as slow as its slowest replica)."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return t.item()
+
+
+def whole_job_rate(world: int, units_per_rank: int, max_elapsed_ms: float) -> float:
+    """Units per second of the whole job: every replica processed units_per_rank units."""
+    return world * units_per_rank / (max_elapsed_ms * 1e-3)
+
+
+def workload_desc(level):
+    w = dict(WORKLOAD, level=level)
+    return (f"icosahedral level {level}, RH54 + {w['ngauss']} Gaussian vortices (seed {w['ic_seed']}, "
+            f"amp U(-2,2), width {w['width']}), eps {w['eps']}, dt {w['dt']}, Omega 2pi")
+
+
+def mesh_sizes(level):
+    nv = 2 + 10 * 4 ** level
+    nl = 20 * 4 ** level
+    nall = 20 * (4 ** (level + 1) - 1) // 3
+    return nv, nall, nl
+
+
+# ------------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+            if gpu_id:
+                cmd += ["-i", gpu_id]
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(cmd, stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1])); smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------------------------------
+# our arm
+# ------------------------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    import lpmkokkos_gb300 as P
+    from lpmkokkos_gb300 import bve
+
+    P.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = bve.Context(local_rank)
+    prec = P.FP32C if args.prec == "fp32c" else P.FP64
+    w = dict(WORKLOAD, level=args.level)
+    nv, nall, nl = mesh_sizes(args.level)
+
+    t0 = time.time()
+    sphere = bve.BVESphere(w["seed_kind"], args.level, omega=w["omega"], layout="left", device=dev)
+    ic = bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"])
+    sphere.init_vorticity(ic, ctx, flags=prec, eps=w["eps"])
+    torch.cuda.synchronize()
+    t_init = time.time() - t0
+    st = sphere.state()
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    def rank_max(x):
+        return max_over_ranks(x, world, dev)
+
+    # FP32 FMA-pipe peak at the current clock (roofline denominator)
+    import ctypes
+    r, ms = ctypes.c_double(), ctypes.c_double()
+    P._lib.check(P.lib().lpm_probe_fp32_fma(local_rank, 200000, ctypes.byref(r), ctypes.byref(ms)))
+    fma_peak_lane_ops = r.value
+
+    # warm-up: builds the plan and captures the step graph
+    t0 = time.time()
+    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=prec, eps=w["eps"])
+    torch.cuda.synchronize()
+    t_warm = time.time() - t0
+
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+    stream = torch.cuda.current_stream()
+
+    def timed(nsteps, instrumented):
+        if instrumented:
+            ctx.set_timing(True)
+            ctx.timing(reset=True)
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(nsteps):
+            flush.zero_()
+            ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=w["eps"])
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        el = e0.elapsed_time(e1)
+        pair = None
+        if instrumented:
+            pair = ctx.timing(reset=True)
+            ctx.set_timing(False)
+        return el, pair
+
+    gpu_uuid = None
+    try:
+        props = torch.cuda.get_device_properties(local_rank)
+        u = str(getattr(props, "uuid", ""))
+        gpu_uuid = ("GPU-" + u) if u and not u.startswith("GPU-") else (u or None)
+    except Exception:
+        gpu_uuid = None
+    sampler = ClockSampler(gpu_uuid)
+    # 1) instrumented pass: per-launch CUDA events around the pair kernel (direct launches)
+    el_instr, (pair_ms, pair_n) = timed(args.steps, True)
+    # 2) headline pass: graph-replayed steps (the product's default path)
+    el_graph, _ = timed(args.steps, False)
+    clocks = sampler.stop()
+    el_graph_max = rank_max(el_graph)
+    el_instr_max = rank_max(el_instr)
+
+    ms_per_step = el_graph_max / args.steps
+    value = whole_job_rate(world, args.steps, el_graph_max)
+    pairs_alg = (nv + nl) * nl                 # algorithmic pairs per evaluation
+    pairs_done = (nv + nall) * nl              # computed (masked parents are targets too)
+    pair_avg_ms = pair_ms / max(1, pair_n)
+    achieved = pairs_alg / (pair_avg_ms * 1e-3) / 1e9
+    peak_at_probe = fma_peak_lane_ops / OPS_PER_PAIR / 1e9
+    sms = torch.cuda.get_device_properties(local_rank).multi_processor_count
+    peak_nominal = sms * 128 * 2070e6 / OPS_PER_PAIR / 1e9
+
+    # 3) end to end through the public API with host buffers
+    names = ("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")
+    host = {n: torch.empty(getattr(st, n).shape, dtype=torch.float64, pin_memory=True) for n in names}
+    for n in names:
+        host[n].copy_(getattr(st, n))
+    torch.cuda.synchronize()
+    bytes_step = sum(host[n].numel() * 8 for n in names)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.e2e_steps):
+        for n in names:
+            getattr(st, n).copy_(host[n], non_blocking=True)
+        ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=w["eps"])
+        for n in names:
+            host[n].copy_(getattr(st, n), non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    el_e2e = rank_max(e0.elapsed_time(e1))
+    e2e_value = whole_job_rate(world, args.e2e_steps, el_e2e)
+
+    out = {
+        "metric": "RK4 steps/s",
+        "value": value,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_per_step,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32c" if prec == P.FP32C else "f64",
+        "data": "synthetic (seeded RH54 + Gaussian vortices on a generated icosahedral mesh)",
+        "config": {
+            "workload": workload_desc(args.level),
+            "targets": nv + nall, "sources": nl, "vertices": nv, "faces": nall,
+            "pairs_per_eval_algorithmic": pairs_alg, "pairs_per_eval_computed": pairs_done,
+            "evals_per_step": 4,
+            "l2": "256 MiB buffer written between steps (inside the timed region)",
+            "parallelism": f"replicas x{world}",
+        },
+        "pair_interactions_per_s": world * 4 * pairs_alg / (ms_per_step * 1e-3),
+        "instrumented_ms_per_step": el_instr_max / args.steps,
+        "roofline": {
+            "bound": "fp32_fma_pipe",
+            "kernel": "pairFP32C" if prec == P.FP32C else "pairFP64",
+            "achieved": achieved,
+            "peak": peak_at_probe,
+            "unit": "Gpair/s",
+            "frac": achieved / peak_at_probe,
+            "peak_source": "FP32 FMA-pipe probe (independent FFMA chains, this run) / 13 lane-ops per pair",
+            "peak_nominal_2070MHz": peak_nominal,
+            "frac_of_nominal": achieved / peak_nominal,
+            "pair_launch_ms_avg": pair_avg_ms,
+            "pair_launches": pair_n,
+            "traffic": None,
+        },
+        "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": bytes_step,
+                "d2h_bytes_per_step": bytes_step, "steps": args.e2e_steps},
+        "gpu_launches": 13 * args.steps,
+        "init_s": t_init,
+        "warmup_s": t_warm,
+    }
+    if clocks:
+        out["clocks"] = clocks
+
+    # 4) plain FP64 GPU path and FP32C accuracy on a target sample (same state)
+    if not args.no_fp64 and rank == 0:
+        out["fp64_gpu"] = fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step)
+
+    # 5) CPU baseline (rank 0, single GPU only)
+    if not args.no_cpu_baseline and rank == 0 and world == 1:
+        out["cpu_baseline"] = cpu_baseline(sphere.state(), sphere, w, args, pairs_done)
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
+
+
+def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step):
+    """Plain FP64 GPU path on 8192 sampled vertex targets; FP32C error on the same targets.
+    (Vertices: a face centre given as a distinct target would coincide with its own source.)"""
+    rng = np.random.default_rng(5)
+    leaf = np.flatnonzero(sphere.mesh["fmask"] == 0)
+    pts = sphere.physVerts
+    idx = torch.from_numpy(rng.choice(pts.shape[0], 8192, replace=False)).to(pts.device)
+    tgt = pts[idx].contiguous()
+    src = (sphere.physFaces, sphere.relVortFaces, sphere.faces_area, sphere.faces_mask)
+    res = {}
+    for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C)):
+        ctx.velocity(tgt, *src, flags=flags)  # plan
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        u, _ = ctx.velocity(tgt, *src, flags=flags)
+        e1.record()
+        torch.cuda.synchronize()
+        res[name] = (u.cpu().numpy(), e0.elapsed_time(e1))
+    ns = int(leaf.size)
+    rate64 = 8192 * ns / (res["fp64"][1] * 1e-3)
+    steps64 = rate64 / (4 * pairs_done)
+    u64, u32 = res["fp64"][0], res["fp32c"][0]
+    err = float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
+    return {"pairs_per_s": rate64, "steps_per_s_extrapolated": steps64,
+            "speedup_fp32c_vs_fp64": (1000.0 / ms_per_step) / steps64,
+            "sample": "velocity at 8192 random vertex targets from all leaf sources, one evaluation",
+            "fp32c_vs_fp64_velocity_rel_l2": err}
+
+
+def cpu_baseline(st, sphere, w, args, pairs_done):
+    """CPU oracle on the host cores, bounded sample of the same evaluation."""
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    vx = sphere.physVerts.cpu().numpy(); fx = sphere.physFaces.cpu().numpy()
+    z = sphere.relVortFaces.cpu().numpy(); a = sphere.faces_area.cpu().numpy(); m = sphere.mesh["fmask"]
+    ns = int((m == 0).sum())
+    tg = np.concatenate([vx, fx])
+    rng = np.random.default_rng(11)
+    n = 256
+    t = 0.0
+    while True:
+        sel = tg[rng.choice(tg.shape[0], n, replace=False)]
+        t0 = time.time()
+        O.velocity_distinct(sel, fx, z, a, m)
+        t = time.time() - t0
+        if t > args.cpu_seconds / 4 or n >= tg.shape[0] // 2:
+            break
+        n = min(tg.shape[0] // 2, int(n * max(2.0, min(8.0, args.cpu_seconds / 4 / max(t, 1e-3)))))
+    # final measured sample of ~cpu_seconds
+    n = min(tg.shape[0], max(n, int(n * args.cpu_seconds / max(t, 1e-3))))
+    sel = tg[rng.choice(tg.shape[0], n, replace=False)]
+    t0 = time.time()
+    O.velocity_distinct(sel, fx, z, a, m)
+    t = time.time() - t0
+    rate = n * ns / t
+    return {"value": rate / (4 * pairs_done), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+            "pairs_per_s": rate,
+            "sample": f"FP64 velocity at {n} random targets from all {ns} leaf sources, {t:.1f} s, "
+                      f"extrapolated to one RK4 step (4 evaluations of {pairs_done} pairs)"}
+
+
+# ------------------------------------------------------------------------------------------
+# reference arm: the reference path's CPU implementation (oracle port) on the host cores
+# ------------------------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import numpy as np
+    from oracle import oracle as O
+    O.build()
+    w = dict(WORKLOAD, level=args.level)
+    m = O.mesh(w["seed_kind"], args.level)
+    z = O.rh54_gaussians(m["fx"], w["ic_seed"], w["ngauss"], w["width"])
+    nv, nall, nl = mesh_sizes(args.level)
+    pairs_done = (nv + nall) * nl
+    tg = np.concatenate([m["vx"], m["fx"]])
+    rng = np.random.default_rng(3)
+    # size one sample to ~3 s of CPU work
+    n = 256
+    sel = tg[rng.choice(tg.shape[0], n, replace=False)]
+    t0 = time.time(); O.velocity_distinct(sel, m["fx"], z, m["farea"], m["fmask"]); t = time.time() - t0
+    n = max(256, min(tg.shape[0], int(n * 3.0 / max(t, 1e-3))))
+    rates = []
+    for k in range(args.warmup + args.steps):
+        sel = tg[rng.choice(tg.shape[0], n, replace=False)]
+        t0 = time.time()
+        O.velocity_distinct(sel, m["fx"], z, m["farea"], m["fmask"])
+        t = time.time() - t0
+        if k >= args.warmup:
+            rates.append(n * nl / t)
+    rate = statistics.median(rates)
+    steps = rate / (4 * pairs_done)
+    sample = (f"each step: FP64 velocity at {n} random vertex/face targets from all {nl} leaf sources, "
+              f"extrapolated to one RK4 step (4 evaluations of {pairs_done} pairs)")
+    out = {
+        "impl": "reference",
+        "metric": "RK4 steps/s", "value": steps, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1000.0 / steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded workload)",
+        "config": {"workload": workload_desc(args.level), "targets": nv + nall, "sources": nl,
+                   "implementation": "CPU oracle: OpenMP restatement of the reference BVE path "
+                                     "(Kokkos reference not buildable: no Kokkos/Trilinos/MPI/VTK)"},
+        "pair_interactions_per_s": rate,
+        "cpu_baseline": {"value": steps, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": steps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local_rank)
+        dist.init_process_group(backend=backend)
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

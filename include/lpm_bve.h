@@ -1,0 +1,160 @@
+/* lpm_bve.h -- C ABI of the GB300-native barotropic-vorticity (BVE) path.
+ *
+ * Drop-in replacement for the BVE hot path of pbosler/lpmKokkos: the spherical
+ * Biot-Savart velocity and stream-function direct sums (src/LpmBVEKernels.hpp) and
+ * the RK4 stepper that evaluates them four times per step (src/LpmBVERK4_Impl.hpp).
+ * Everything below is plain C: device pointers, sizes, strides and a CUDA stream.
+ *
+ * Conventions
+ *  - All particle arrays are DEVICE pointers owned by the caller.  A vector array is
+ *    addressed as x[i*stride_i + c*stride_c] (c = 0,1,2), so both Kokkos layouts are
+ *    accepted: LayoutLeft (stride_i = 1, stride_c = n, the CUDA default of
+ *    View<double*[3]>) and LayoutRight (stride_i = 3, stride_c = 1).
+ *  - mask arrays hold one byte per face, nonzero = masked (a divided parent panel),
+ *    as Kokkos View<bool*> does.
+ *  - Work is queued on `stream` and returns without synchronising, except the first
+ *    call for a new problem geometry (new pointers, sizes, strides or mask), which
+ *    builds a plan: it copies positions and the mask to the host, synchronising the
+ *    stream once.  The plan is reused by later calls with the same geometry.
+ *  - Every function returns LPM_OK (0) or a negative status; lpm_bve_last_error()
+ *    gives the message.  One context per host thread / stream.
+ */
+#ifndef LPM_BVE_H
+#define LPM_BVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = legacy default stream */
+
+/* ---- status codes ---------------------------------------------------------- */
+#define LPM_OK                    0
+#define LPM_ERR_INVALID_ARGUMENT (-1)
+#define LPM_ERR_CUDA             (-2)
+#define LPM_ERR_OUT_OF_MEMORY    (-3)
+#define LPM_ERR_NOT_SUPPORTED    (-4)
+#define LPM_ERR_ADMISSION        (-5) /* server: request does not fit the HBM budget */
+#define LPM_ERR_STATE            (-6) /* object used in the wrong state (e.g. unknown request id) */
+#define LPM_ERR_TIMEOUT          (-7) /* a bounded wait gave up */
+
+/* ---- flags ------------------------------------------------------------------ */
+#define LPM_BVE_FP64                0u        /* plain FP64 pair arithmetic (the GPU oracle) */
+#define LPM_BVE_FP32C               (1u << 0) /* FP32 pair arithmetic, compensated sums, FP64 epilogue */
+#define LPM_BVE_COLLOCATED          (1u << 1) /* velocity(): targets are the sources, i == j excluded */
+#define LPM_BVE_PSI                 (1u << 2) /* also compute the stream function */
+#define LPM_BVE_NO_VELOCITY         (1u << 3) /* velocity(): stream function only (u may be NULL) */
+#define LPM_BVE_RK4_FIX_QUIRK       (1u << 4) /* rk4: RK4-correct face vorticity update; default
+                                                 reproduces src/LpmBVERK4_Impl.hpp:121 */
+#define LPM_BVE_RENORM              (1u << 5) /* rk4: project positions to |x| = 1 after each step */
+#define LPM_BVE_SKIP_MASKED_TARGETS (1u << 6) /* rk4: no velocity at masked faces (their x, zeta stay fixed) */
+#define LPM_BVE_NO_GRAPH            (1u << 7) /* rk4: launch kernels directly, no captured CUDA graph */
+#define LPM_BVE_NO_SORT             (1u << 8) /* keep the caller's target order (no spatial sort) */
+
+/* ---- context ---------------------------------------------------------------- */
+typedef struct lpm_bve_ctx lpm_bve_ctx;
+
+typedef struct {
+  int device;   /* CUDA device ordinal; -1 = the current device */
+  int autotune; /* nonzero: time candidate launch shapes the first time a problem size is seen */
+  int verbose;  /* nonzero: print plan / autotune decisions to stderr */
+} lpm_bve_opts;
+
+/* Replaces: BVERK4 construction (src/LpmBVERK4.hpp:29) and Kokkos::initialize for this path. */
+int lpm_bve_ctx_create(lpm_bve_ctx** ctx, const lpm_bve_opts* opts);
+int lpm_bve_ctx_destroy(lpm_bve_ctx* ctx);
+const char* lpm_bve_last_error(const lpm_bve_ctx* ctx);
+/* Drop cached plans (use after rewriting a mask or positions in place between unrelated problems). */
+int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx);
+
+/* Timing of the O(N^2) pair kernel (the reference's Kokkos::Profiling regions around
+ * advance_timestep, src/LpmBVERK4_Impl.hpp:45,129, have no per-kernel timer).  While enabled,
+ * every pair-kernel launch is bracketed by CUDA events on its stream and RK4 steps are
+ * launched directly instead of through the captured graph.  lpm_bve_ctx_timing synchronises
+ * on the recorded events and returns the summed pair-kernel milliseconds and launch count. */
+int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable);
+int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches, int reset);
+
+/* ---- particle sets -------------------------------------------------------------- */
+typedef struct {
+  const double* x;   /* element (i, c) at x[i*stride_i + c*stride_c] */
+  int64_t n;
+  int64_t stride_i, stride_c;
+} lpm_points;
+
+typedef struct {
+  lpm_points pts;      /* face-centre (source) positions, all faces including masked parents */
+  const double* zeta;  /* relative vorticity, n */
+  const double* area;  /* panel area, n */
+  const uint8_t* mask; /* n bytes, nonzero = skip as a source; NULL = no face masked */
+} lpm_sources;
+
+/* Velocity (and stream function) at targets from all unmasked sources.
+ *   u(x_i)   = sum_j (x_i x x_j) * (-zeta_j A_j) / (4 pi (1 - x_i.x_j + eps^2))
+ *   psi(x_i) = sum_j log(1 - x_i.x_j + eps^2) * (-zeta_j A_j) / (4 pi)
+ * Without LPM_BVE_COLLOCATED the targets `tgt` are a distinct set (vertices):
+ *   replaces BVEVertexVelocity / BVEVertexStreamFn / BVEVertexSolve
+ *   (src/LpmBVEKernels.hpp:163-186, :140-161, :110-138).
+ * With LPM_BVE_COLLOCATED the targets are the sources themselves (tgt is ignored and
+ * may be NULL) and the term i == j is excluded: replaces BVEFaceVelocity /
+ * BVEFaceStreamFn / BVEFaceSolve (:285-305, :263-283, :236-261).
+ * eps = 0 gives the reference expressions exactly.  u: (n_targets x 3) with strides;
+ * psi: n_targets or NULL.  Precision: LPM_BVE_FP64 or LPM_BVE_FP32C. */
+int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources* src,
+                     double* u, int64_t u_stride_i, int64_t u_stride_c, double* psi,
+                     unsigned flags, double eps, lpm_stream_t stream);
+
+/* ---- RK4 stepper ------------------------------------------------------------------ */
+typedef struct {
+  int64_t nverts, nfaces;                                          /* BVERK4::nverts / nfaces */
+  double* vx;    int64_t vx_stride_i, vx_stride_c;                 /* vertex positions (in/out) */
+  double* vzeta;                                                   /* vertex relative vorticity (in/out) */
+  double* vvel;  int64_t vvel_stride_i, vvel_stride_c;             /* vertex velocity (in: u(x), out) */
+  double* fx;    int64_t fx_stride_i, fx_stride_c;                 /* face positions (in/out) */
+  double* fzeta;                                                   /* face relative vorticity (in/out) */
+  double* fvel;  int64_t fvel_stride_i, fvel_stride_c;             /* face velocity (in: u(x), out) */
+  const double* farea;                                             /* face areas (in) */
+  const uint8_t* fmask;                                            /* face mask (in), NULL = none */
+} lpm_bve_state;
+
+/* Advance `nsteps` RK4 steps of the barotropic vorticity equation in place.
+ * Replaces BVERK4::advance_timestep (src/LpmBVERK4.hpp:33-34, src/LpmBVERK4_Impl.hpp:42-130):
+ * stage 1 uses the velocity already stored in vvel/fvel; stages 2-4 and the closing
+ * re-evaluation are four velocity evaluations per step; dzeta = -2 Omega u_z dt.
+ * On return vvel/fvel hold u at the new positions.  The stage workspace belongs to the
+ * context (BVERK4::init, src/LpmBVERK4.cpp:5-37). */
+int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, double Omega, int nsteps,
+                     unsigned flags, double eps, lpm_stream_t stream);
+
+/* ---- host-side mesh and initial conditions ------------------------------------------ */
+#define LPM_SEED_ICOS_TRI 0 /* IcosTriSphereSeed  (src/LpmMeshSeed.hpp:134-152) */
+#define LPM_SEED_CUBED    1 /* CubedSphereSeed    (src/LpmMeshSeed.hpp:113-128) */
+
+/* Sizes of a uniformly refined tree mesh (MeshSeed::setMaxAllocations, src/LpmMeshSeed.cpp:297-305). */
+int lpm_mesh_counts(int seed, int level, int64_t* nverts, int64_t* nfaces, int64_t* nleaves);
+/* Build the mesh on the host (PolyMesh2d::treeInit, src/LpmPolyMesh2d.cpp:31-44) with the
+ * reference's index order.  Host buffers: vx (nverts x 3, row-major), fx (nfaces x 3),
+ * farea (nfaces), fmask (nfaces).  Any pointer may be NULL. */
+int lpm_mesh_build(int seed, int level, double* vx, double* fx, double* farea, uint8_t* fmask);
+
+/* Host initial conditions on row-major (n x 3) positions.
+ * RH54: zeta = 30 cos(4 lambda) P_5^4(z) (src/LpmRossbyWaves.hpp:28-32).
+ * Solid body: zeta = 2*(2 pi) z (src/LpmVorticityGallery.hpp:25-40).
+ * Gaussians (no reference counterpart): zeta += a_g exp(-(d(x, c_g)/width)^2). */
+int lpm_ic_rh54(const double* x, int64_t n, double* zeta);
+int lpm_ic_rh54_velocity(const double* x, int64_t n, double* u);
+int lpm_ic_solid_body(const double* x, int64_t n, double* zeta);
+int lpm_ic_gaussians_add(const double* x, int64_t n, const double* centers, const double* amps, int ng,
+                         double width, double* zeta);
+/* Seeded Gaussian-vortex parameters: centres uniform on the sphere (normalised normal
+ * vectors), amplitudes U(amp_lo, amp_hi); std::mt19937_64 with a portable 53-bit uniform. */
+int lpm_ic_gaussian_params(uint64_t seed, int ng, double amp_lo, double amp_hi, double* centers, double* amps);
+
+#ifdef __cplusplus
+} /* extern "C" */
+#endif
+
+#endif /* LPM_BVE_H */

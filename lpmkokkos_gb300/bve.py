@@ -1,0 +1,344 @@
+"""Host-side mirror of the reference's BVE interface over the C ABI.
+
+pbosler/lpmKokkos keeps the BVE problem in ``BVESphere<Seed>`` (src/LpmBVESphere.hpp:18-80)
+and steps it with ``BVERK4`` (src/LpmBVERK4.hpp:13-65).  The classes below keep those names,
+members and argument meanings for Python callers; device arrays are torch tensors used as
+plain device buffers, and every computation goes through liblpm_bve.so.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+from dataclasses import dataclass
+from typing import Callable, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _lib as L
+
+PI = math.pi
+
+
+def _vp(t: Optional[torch.Tensor]):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None and t.numel() > 0 else None
+
+
+def _np_ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _stream(stream) -> ctypes.c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return ctypes.c_void_p(stream.cuda_stream)
+
+
+def _points(x: torch.Tensor) -> L.Points:
+    assert x.dtype == torch.float64 and x.dim() == 2 and x.shape[1] == 3, "positions must be float64 (n, 3)"
+    return L.Points(x.data_ptr() if x.numel() else None, x.shape[0], x.stride(0), x.stride(1))
+
+
+def _mask_ptr(m: Optional[torch.Tensor]):
+    if m is None:
+        return None
+    assert m.dtype in (torch.uint8, torch.bool), "mask must be uint8 or bool"
+    return m.data_ptr() if m.numel() else None
+
+
+# ----------------------------------------------------------------------------------------
+# host mesh and initial conditions
+# ----------------------------------------------------------------------------------------
+def mesh_counts(seed: int, level: int):
+    nv, nf, nl = L.c_i64(), L.c_i64(), L.c_i64()
+    L.check(L.lib().lpm_mesh_counts(seed, level, ctypes.byref(nv), ctypes.byref(nf), ctypes.byref(nl)))
+    return nv.value, nf.value, nl.value
+
+
+def build_mesh(seed: int, level: int) -> dict:
+    """Uniformly refined icosahedral (seed 0) or cubed-sphere (seed 1) mesh, host numpy arrays."""
+    nv, nf, nl = mesh_counts(seed, level)
+    vx = np.zeros((nv, 3)); fx = np.zeros((nf, 3)); fa = np.zeros(nf); fm = np.zeros(nf, dtype=np.uint8)
+    L.check(L.lib().lpm_mesh_build(seed, level, _np_ptr(vx), _np_ptr(fx), _np_ptr(fa), _np_ptr(fm)))
+    return dict(seed=seed, level=level, nverts=nv, nfaces=nf, nleaves=nl, vx=vx, fx=fx, farea=fa, fmask=fm)
+
+
+def _map(fn, x: np.ndarray, width: int):
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    out = np.zeros((x.shape[0], width) if width > 1 else x.shape[0])
+    L.check(fn(_np_ptr(x), x.shape[0], _np_ptr(out)))
+    return out
+
+
+def ic_rh54(x: np.ndarray) -> np.ndarray:
+    return _map(L.lib().lpm_ic_rh54, x, 1)
+
+
+def rh54_velocity(x: np.ndarray) -> np.ndarray:
+    return _map(L.lib().lpm_ic_rh54_velocity, x, 3)
+
+
+def ic_solid_body(x: np.ndarray) -> np.ndarray:
+    return _map(L.lib().lpm_ic_solid_body, x, 1)
+
+
+def gaussian_params(seed: int, ng: int, amp_lo: float = -2.0, amp_hi: float = 2.0):
+    c = np.zeros((ng, 3)); a = np.zeros(ng)
+    L.check(L.lib().lpm_ic_gaussian_params(seed, ng, amp_lo, amp_hi, _np_ptr(c), _np_ptr(a)))
+    return c, a
+
+
+def ic_gaussians_add(x: np.ndarray, zeta: np.ndarray, centers, amps, width: float = 0.1) -> np.ndarray:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    z = np.array(zeta, dtype=np.float64, copy=True)
+    c = np.ascontiguousarray(centers, dtype=np.float64)
+    a = np.ascontiguousarray(amps, dtype=np.float64)
+    L.check(L.lib().lpm_ic_gaussians_add(_np_ptr(x), x.shape[0], _np_ptr(c), _np_ptr(a), a.shape[0], width,
+                                         _np_ptr(z)))
+    return z
+
+
+def rh54_gaussians(seed: int, ng: int, width: float = 0.1) -> Callable[[np.ndarray], np.ndarray]:
+    """Relative-vorticity initial condition: RH54 plus ng seeded Gaussian vortices."""
+    c, a = gaussian_params(seed, ng)
+
+    def ic(x):
+        return ic_gaussians_add(x, ic_rh54(x), c, a, width) if ng > 0 else ic_rh54(x)
+    ic.centers, ic.amps, ic.width = c, a, width
+    return ic
+
+
+# ----------------------------------------------------------------------------------------
+# context
+# ----------------------------------------------------------------------------------------
+@dataclass
+class BVEState:
+    """Device arrays of one solve (the arguments of BVERK4::advance_timestep)."""
+    vx: torch.Tensor
+    vzeta: torch.Tensor
+    vvel: torch.Tensor
+    fx: torch.Tensor
+    fzeta: torch.Tensor
+    fvel: torch.Tensor
+    farea: torch.Tensor
+    fmask: Optional[torch.Tensor]
+
+    def c_struct(self) -> L.State:
+        for name in ("vx", "vvel", "fx", "fvel"):
+            t = getattr(self, name)
+            assert t.dtype == torch.float64 and t.dim() == 2 and t.shape[1] == 3, name
+        return L.State(self.vx.shape[0], self.fx.shape[0],
+                       self.vx.data_ptr(), self.vx.stride(0), self.vx.stride(1),
+                       self.vzeta.data_ptr(),
+                       self.vvel.data_ptr(), self.vvel.stride(0), self.vvel.stride(1),
+                       self.fx.data_ptr(), self.fx.stride(0), self.fx.stride(1),
+                       self.fzeta.data_ptr(),
+                       self.fvel.data_ptr(), self.fvel.stride(0), self.fvel.stride(1),
+                       self.farea.data_ptr(), _mask_ptr(self.fmask))
+
+
+class Context:
+    """Owns an lpm_bve_ctx (plans, stage workspace, captured graphs) on one GPU."""
+
+    def __init__(self, device: Optional[int] = None, autotune: bool = False, verbose: bool = False):
+        self._lib = L.lib()
+        if device is None:
+            device = torch.cuda.current_device()
+        self.device = device
+        h = ctypes.c_void_p()
+        opts = L.Opts(device, int(autotune), int(verbose))
+        L.check(self._lib.lpm_bve_ctx_create(ctypes.byref(h), ctypes.byref(opts)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            self._lib.lpm_bve_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def invalidate(self):
+        L.check(self._lib.lpm_bve_plan_invalidate(self.handle), self.handle)
+
+    def set_timing(self, enable: bool):
+        """Bracket every pair-kernel launch with CUDA events (RK4 steps then launch directly)."""
+        L.check(self._lib.lpm_bve_ctx_set_timing(self.handle, int(enable)), self.handle)
+
+    def timing(self, reset: bool = True):
+        """(summed pair-kernel milliseconds, launches) since the last reset."""
+        ms, n = ctypes.c_double(), L.c_i64()
+        L.check(self._lib.lpm_bve_ctx_timing(self.handle, ctypes.byref(ms), ctypes.byref(n), int(reset)),
+                self.handle)
+        return ms.value, n.value
+
+    def velocity(self, tgt: Optional[torch.Tensor], src_x: torch.Tensor, src_zeta: torch.Tensor,
+                 src_area: torch.Tensor, src_mask: Optional[torch.Tensor], u: Optional[torch.Tensor] = None,
+                 psi: Optional[torch.Tensor] = None, flags: int = 0, eps: float = 0.0, stream=None):
+        """u (and psi) at `tgt` (or at the sources themselves with flags & COLLOCATED)."""
+        colloc = bool(flags & L.COLLOCATED)
+        n = src_x.shape[0] if colloc else tgt.shape[0]
+        if u is None and not (flags & L.NO_VELOCITY):
+            u = torch.empty((n, 3), dtype=torch.float64, device=src_x.device)
+        if psi is None and (flags & L.PSI):
+            psi = torch.empty(n, dtype=torch.float64, device=src_x.device)
+        src = L.Sources(_points(src_x), _vp(src_zeta), _vp(src_area), _mask_ptr(src_mask))
+        tp = None if colloc else ctypes.byref(_points(tgt))
+        us = (u.stride(0), u.stride(1)) if u is not None else (3, 1)
+        rc = self._lib.lpm_bve_velocity(self.handle, tp, ctypes.byref(src), _vp(u), us[0], us[1], _vp(psi),
+                                        flags, eps, _stream(stream))
+        L.check(rc, self.handle)
+        return u, psi
+
+    def rk4_step(self, state: BVEState, dt: float, omega: float, nsteps: int = 1, flags: int = 0,
+                 eps: float = 0.0, stream=None):
+        st = state.c_struct()
+        rc = self._lib.lpm_bve_rk4_step(self.handle, ctypes.byref(st), dt, omega, nsteps, flags, eps,
+                                        _stream(stream))
+        L.check(rc, self.handle)
+
+    def ensemble(self, states: Sequence[BVEState], flags: int = 0, eps: float = 0.0, stream=None) -> "Ensemble":
+        return Ensemble(self, states, flags, eps, stream)
+
+
+class Ensemble:
+    """Many independent solves advanced together (include/lpm_bve_ensemble.h)."""
+
+    def __init__(self, ctx: Context, states: Sequence[BVEState], flags: int, eps: float, stream=None):
+        self.ctx = ctx
+        self.states = list(states)
+        arr = (L.State * len(self.states))(*[s.c_struct() for s in self.states])
+        h = ctypes.c_void_p()
+        L.check(ctx._lib.lpm_bve_ensemble_create(ctx.handle, arr, len(self.states), flags, eps, _stream(stream),
+                                                 ctypes.byref(h)), ctx.handle)
+        self.handle = h
+
+    def step(self, dt, omega, nsteps: int = 1, stream=None):
+        m = len(self.states)
+        dts = np.broadcast_to(np.asarray(dt, dtype=np.float64), (m,)).copy()
+        oms = np.broadcast_to(np.asarray(omega, dtype=np.float64), (m,)).copy()
+        rc = self.ctx._lib.lpm_bve_ensemble_step(self.handle, dts.ctypes.data_as(L.c_dp),
+                                                 oms.ctypes.data_as(L.c_dp), nsteps, _stream(stream))
+        L.check(rc, self.ctx.handle)
+
+    def info(self):
+        ns, ni, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        pairs, nbytes = L.c_i64(), ctypes.c_size_t()
+        L.check(self.ctx._lib.lpm_bve_ensemble_info(self.handle, ctypes.byref(ns), ctypes.byref(ni), ctypes.byref(g),
+                                                    ctypes.byref(pairs), ctypes.byref(nbytes)))
+        return dict(nsolves=ns.value, nitems=ni.value, grid=g.value, pairs_per_eval=pairs.value,
+                    device_bytes=nbytes.value)
+
+    def close(self):
+        if self.handle:
+            self.ctx._lib.lpm_bve_ensemble_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ----------------------------------------------------------------------------------------
+# reference-shaped containers
+# ----------------------------------------------------------------------------------------
+def _dev_vec(host: np.ndarray, device, layout: str) -> torch.Tensor:
+    """(n, 3) float64 device tensor; layout 'left' = SoA strides (1, n) like Kokkos CUDA views."""
+    t = torch.from_numpy(np.ascontiguousarray(host, dtype=np.float64))
+    if layout == "left":
+        return t.t().contiguous().to(device).t()
+    return t.to(device)
+
+
+class BVESphere:
+    """The BVE problem on a uniformly refined sphere mesh (BVESphere<Seed>, src/LpmBVESphere.hpp:18-80).
+
+    Field names follow the reference: physVerts/physFaces coordinates, relVort*, absVort*,
+    streamFn*, velocity*, faces area and mask, and the Lagrangian copies of the coordinates.
+    """
+
+    def __init__(self, seed: int, level: int, omega: float = 2 * PI, layout: str = "left", device="cuda"):
+        m = build_mesh(seed, level)
+        self.seed, self.level, self.layout, self.device = seed, level, layout, torch.device(device)
+        self.mesh = m
+        self.Omega = omega
+        self.t = 0.0
+        self.physVerts = _dev_vec(m["vx"], self.device, layout)
+        self.physFaces = _dev_vec(m["fx"], self.device, layout)
+        self.lagVerts = self.physVerts.clone()
+        self.lagFaces = self.physFaces.clone()
+        self.faces_area = torch.from_numpy(m["farea"]).to(self.device)
+        self.faces_mask = torch.from_numpy(m["fmask"]).to(self.device)
+        nv, nf = m["nverts"], m["nfaces"]
+        z = lambda n: torch.zeros(n, dtype=torch.float64, device=self.device)  # noqa: E731
+        self.relVortVerts, self.absVortVerts, self.streamFnVerts = z(nv), z(nv), z(nv)
+        self.relVortFaces, self.absVortFaces, self.streamFnFaces = z(nf), z(nf), z(nf)
+        self.velocityVerts = _dev_vec(np.zeros((nv, 3)), self.device, layout)
+        self.velocityFaces = _dev_vec(np.zeros((nf, 3)), self.device, layout)
+
+    def nvertsHost(self):
+        return self.mesh["nverts"]
+
+    def nfacesHost(self):
+        return self.mesh["nfaces"]
+
+    def nleaves(self):
+        return self.mesh["nleaves"]
+
+    def avg_mesh_size_radians(self):
+        return math.sqrt(4 * PI / self.nfacesHost())
+
+    def init_vorticity(self, ic: Callable[[np.ndarray], np.ndarray], ctx: Context, flags: int = L.FP64,
+                       eps: float = 0.0):
+        """Host IC evaluation, then psi and u at vertices and faces (src/LpmBVESphere.cpp:127-169)."""
+        vx, fx = self.mesh["vx"], self.mesh["fx"]
+        zv = ic(vx); zf = ic(fx)
+        self.relVortVerts.copy_(torch.from_numpy(zv))
+        self.absVortVerts.copy_(torch.from_numpy(zv + 2 * self.Omega * vx[:, 2]))
+        self.relVortFaces.copy_(torch.from_numpy(zf))
+        self.absVortFaces.copy_(torch.from_numpy(zf + 2 * self.Omega * fx[:, 2]))
+        self.solve(ctx, flags, eps, psi=True)
+
+    def solve(self, ctx: Context, flags: int = L.FP64, eps: float = 0.0, psi: bool = True):
+        """Velocity (and stream function) at all vertices and faces from the face vorticity."""
+        prec = flags & L.FP32C
+        f = prec | (L.PSI if psi else 0)
+        ctx.velocity(self.physVerts, self.physFaces, self.relVortFaces, self.faces_area, self.faces_mask,
+                     u=self.velocityVerts, psi=self.streamFnVerts if psi else None, flags=f, eps=eps)
+        ctx.velocity(None, self.physFaces, self.relVortFaces, self.faces_area, self.faces_mask,
+                     u=self.velocityFaces, psi=self.streamFnFaces if psi else None, flags=f | L.COLLOCATED, eps=eps)
+
+    def state(self) -> BVEState:
+        return BVEState(self.physVerts, self.relVortVerts, self.velocityVerts, self.physFaces, self.relVortFaces,
+                        self.velocityFaces, self.faces_area, self.faces_mask)
+
+
+class BVERK4:
+    """RK4 stepper with the reference's interface (src/LpmBVERK4.hpp:13-65)."""
+
+    def __init__(self, dt: float, Omega: float, ctx: Optional[Context] = None, flags: int = L.FP64,
+                 eps: float = 0.0):
+        self.dt, self.Omega = dt, Omega
+        self.nverts = self.nfaces = 0
+        self.ctx = ctx or Context()
+        self.flags, self.eps = flags, eps
+
+    def init(self, nv: int, nf: int):
+        self.nverts, self.nfaces = nv, nf
+
+    def advance_timestep(self, vx, vzeta, vvel, fx, fzeta, fvel, fa, fm, nsteps: int = 1):
+        if vx.shape[0] != self.nverts or fx.shape[0] != self.nfaces:
+            raise ValueError("advance_timestep: array sizes differ from init(nv, nf)")
+        self.ctx.rk4_step(BVEState(vx, vzeta, vvel, fx, fzeta, fvel, fa, fm), self.dt, self.Omega, nsteps,
+                          self.flags, self.eps)

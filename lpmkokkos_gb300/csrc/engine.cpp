@@ -1,0 +1,912 @@
+// engine.cpp -- host engine of the BVE path: contexts, plans, RK4 driver, CUDA graphs,
+// and the C ABI of include/lpm_bve.h.
+//
+// A plan fixes everything about a problem that does not change from step to step: the
+// spatially sorted target slots, the compacted (unmasked) source list, the per-tile
+// self-exclusion ranges and the work items of the pair kernel.  Building it copies the
+// positions and the mask to the host once; later calls with the same geometry only queue
+// kernels.  One RK4 step is 13 launches (prep, pair, epilogue per evaluation plus the
+// combine); it is captured once into a CUDA graph and replayed.
+
+#include "lpm_bve.h"
+#include "lpm_bve_ensemble.h"
+#include "engine.hpp"
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace lpm {
+
+// ---------------------------------------------------------------------------------------
+// small utilities
+// ---------------------------------------------------------------------------------------
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define LPM_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw Error{LPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+  } while (0)
+
+[[noreturn]] void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw Error{code, buf};
+}
+
+class DeviceArena {  // owns a set of cudaMalloc'd buffers
+ public:
+  ~DeviceArena() { release(); }
+  template <typename T>
+  T* alloc(size_t count) {
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "cudaMalloc(%zu bytes): %s",
+           count * sizeof(T), cudaGetErrorString(e));
+    }
+    ptrs_.push_back(p);
+    bytes_ += count * sizeof(T);
+    return static_cast<T*>(p);
+  }
+  void release() {
+    for (void* p : ptrs_) cudaFree(p);
+    ptrs_.clear();
+    bytes_ = 0;
+  }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  std::vector<void*> ptrs_;
+  size_t bytes_ = 0;
+};
+
+template <typename T>
+void upload(T* dst, const std::vector<T>& src, cudaStream_t s) {
+  if (!src.empty()) LPM_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// Copy n strided 3-vectors from the device to a host row-major array (synchronises s).
+std::vector<double> fetchPoints(const double* p, int64_t n, int64_t si, int64_t sc, cudaStream_t s) {
+  std::vector<double> out(3 * (size_t)n);
+  if (n == 0) return out;
+  const int64_t span = (n - 1) * si + 2 * sc + 1;
+  std::vector<double> raw((size_t)span);
+  LPM_CUDA(cudaMemcpyAsync(raw.data(), p, sizeof(double) * span, cudaMemcpyDeviceToHost, s));
+  LPM_CUDA(cudaStreamSynchronize(s));
+  for (int64_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) out[3 * i + c] = raw[(size_t)(i * si + c * sc)];
+  return out;
+}
+
+inline uint32_t spread3(uint32_t x) {  // 10-bit value -> every third bit
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000ffu;
+  x = (x | (x << 8)) & 0x0300f00fu;
+  x = (x | (x << 4)) & 0x030c30c3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+inline uint32_t mortonKey(const double* x) {
+  uint32_t q[3];
+  for (int c = 0; c < 3; ++c) {
+    double t = (x[c] + 1.05) * (1024.0 / 2.1);
+    if (!(t >= 0.0)) t = 0.0;  // also catches NaN
+    if (t > 1023.0) t = 1023.0;
+    q[c] = (uint32_t)t;
+  }
+  return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+}
+
+void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc) {
+  if (n < 0) fail(LPM_ERR_INVALID_ARGUMENT, "%s: negative count", name);
+  if (n > 0 && !p) fail(LPM_ERR_INVALID_ARGUMENT, "%s: null pointer with n = %lld", name, (long long)n);
+  if (n > 0 && (si < 0 || sc < 0 || (si == 0 && n > 1)))
+    fail(LPM_ERR_INVALID_ARGUMENT, "%s: invalid strides (%lld, %lld)", name, (long long)si, (long long)sc);
+  if (n > (int64_t)INT_MAX / 4) fail(LPM_ERR_NOT_SUPPORTED, "%s: %lld points exceed the supported size", name, (long long)n);
+}
+
+// ---------------------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------------------
+enum class Mode { Distinct = 0, Collocated = 1, RK4 = 2 };
+
+// Launch shape used when the autotuner is off (measured best on GB300 among the
+// instantiated shapes; the autotuner may choose another one per problem size).
+constexpr PairShape kDefaultFP32C{128, 4, 256};
+constexpr PairShape kFP64Shape{128, 1, 128};
+
+struct SolvePlan {
+  Mode mode = Mode::Distinct;
+  Precision prec = Precision::FP64;
+  ParticleIO io;
+  const uint8_t* mask = nullptr;
+  bool skipMasked = false, sorted = true;
+  int nslots = 0, ns = 0, ntiles = 0, nchunks = 1, tileSize = 1, chunkLen = 0;
+  double eps2 = 0.0;
+  std::vector<int2> tileSelfHost;
+  DeviceArena mem;
+  SolveStage stage{};
+  SolveDev dev{};
+};
+
+// CUDA-event timing of the pair-kernel launches (enabled by lpm_bve_ctx_set_timing).
+struct PairTimer {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  std::vector<cudaEvent_t> pool;
+  double totalMs = 0.0;
+  int64_t launches = 0;
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    LPM_CUDA(cudaEventCreate(&e));
+    return e;
+  }
+  void collect() {
+    for (auto& pr : pending) {
+      LPM_CUDA(cudaEventSynchronize(pr.second));
+      float ms = 0.f;
+      LPM_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+      totalMs += ms;
+      launches += 1;
+      pool.push_back(pr.first);
+      pool.push_back(pr.second);
+    }
+    pending.clear();
+  }
+  ~PairTimer() {
+    for (auto& pr : pending) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+struct Batch {
+  PairTimer* timer = nullptr;  // non-null: bracket each pair launch with events (direct launches only)
+  std::vector<std::unique_ptr<SolvePlan>> solves;
+  Precision prec = Precision::FP64;
+  PairShape shape = kFP64Shape;
+  bool rk4 = false;
+  int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
+  DeviceArena mem;
+  WorkItem* items = nullptr;
+  SolveDev* solveDev = nullptr;
+  SolveStage* stageDev = nullptr;
+  int4* prepMap = nullptr;
+  int4* slotMap = nullptr;
+  int* counter = nullptr;
+  // captured RK4 step
+  cudaGraphExec_t graph = nullptr;
+  bool graphQuirk = false, graphRenorm = false;
+  ~Batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+struct DeviceInfo {
+  int device = 0, sms = 0;
+};
+
+// Builds the per-solve index structures (host) and its device buffers.
+void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
+                bool sort, double eps, int tileSize, cudaStream_t s) {
+  P.mode = mode;
+  P.prec = prec;
+  P.io = io;
+  P.mask = mask;
+  P.skipMasked = skipMasked;
+  P.sorted = sort;
+  P.eps2 = eps * eps;
+  P.tileSize = tileSize;
+  const int64_t na = io.na, nb = io.nb;
+
+  std::vector<uint8_t> hmask((size_t)nb, 0);
+  if (mask && nb > 0) {
+    LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)nb, cudaMemcpyDeviceToHost, s));
+    LPM_CUDA(cudaStreamSynchronize(s));
+  }
+  std::vector<double> ha, hb;
+  if (sort) {
+    if (mode != Mode::Collocated) ha = fetchPoints(io.ax.p, na, io.ax.si, io.ax.sc, s);
+    hb = fetchPoints(io.bx.p, nb, io.bx.si, io.bx.sc, s);
+  }
+
+  // Target slots: particle ids (a: id = i; face f: id = na + f).
+  std::vector<int> ids;
+  if (mode != Mode::Collocated)
+    for (int64_t i = 0; i < na; ++i) ids.push_back((int)i);
+  if (mode != Mode::Distinct)
+    for (int64_t f = 0; f < nb; ++f)
+      if (!(skipMasked && hmask[f])) ids.push_back((int)(na + f));
+  std::vector<int> srcFace;
+  for (int64_t f = 0; f < nb; ++f)
+    if (!hmask[f]) srcFace.push_back((int)f);
+
+  if (sort) {
+    auto keyOf = [&](int id) { return id < na ? mortonKey(&ha[3 * (size_t)id]) : mortonKey(&hb[3 * (size_t)(id - na)]); };
+    std::vector<std::pair<uint32_t, int>> kv(ids.size());
+    for (size_t i = 0; i < ids.size(); ++i) kv[i] = {keyOf(ids[i]), ids[i]};
+    std::sort(kv.begin(), kv.end());
+    for (size_t i = 0; i < ids.size(); ++i) ids[i] = kv[i].second;
+    std::vector<std::pair<uint32_t, int>> ks(srcFace.size());
+    for (size_t i = 0; i < srcFace.size(); ++i) ks[i] = {mortonKey(&hb[3 * (size_t)srcFace[i]]), srcFace[i]};
+    std::sort(ks.begin(), ks.end());
+    for (size_t i = 0; i < srcFace.size(); ++i) srcFace[i] = ks[i].second;
+  }
+  const int nslots = (int)ids.size(), ns = (int)srcFace.size();
+  std::vector<int> srcOf((size_t)nb, -1), slotOf((size_t)nb, -1);
+  for (int i = 0; i < ns; ++i) srcOf[srcFace[i]] = i;
+  std::vector<int> self((size_t)nslots, -1);
+  for (int t = 0; t < nslots; ++t)
+    if (ids[t] >= na) {
+      const int f = (int)(ids[t] - na);
+      slotOf[f] = t;
+      self[t] = srcOf[f];
+    }
+  std::vector<int> srcSlot((size_t)ns, -1);
+  for (int i = 0; i < ns; ++i) srcSlot[i] = slotOf[srcFace[i]];
+
+  P.nslots = nslots;
+  P.ns = ns;
+  P.ntiles = (nslots + tileSize - 1) / tileSize;
+  P.tileSelfHost.assign((size_t)P.ntiles, make_int2(INT_MAX, -1));
+  for (int t = 0; t < nslots; ++t)
+    if (self[t] >= 0) {
+      int2& r = P.tileSelfHost[t / tileSize];
+      r.x = std::min(r.x, self[t]);
+      r.y = std::max(r.y, self[t]);
+    }
+
+  DeviceArena& M = P.mem;
+  M.release();
+  int* dPerm = M.alloc<int>(nslots);
+  int* dSelf = M.alloc<int>(nslots);
+  int2* dTileSelf = M.alloc<int2>(P.ntiles);
+  int* dSrcFace = M.alloc<int>(ns);
+  int* dSrcSlot = M.alloc<int>(ns);
+  double* dTx = M.alloc<double>(3 * (size_t)nslots);
+  upload(dPerm, ids, s);
+  upload(dSelf, self, s);
+  upload(dTileSelf, P.tileSelfHost, s);
+  upload(dSrcFace, srcFace, s);
+  upload(dSrcSlot, srcSlot, s);
+
+  SolveStage& S = P.stage;
+  S = SolveStage{};
+  S.io = io;
+  S.perm = dPerm;
+  S.srcFace = dSrcFace;
+  S.srcSlot = dSrcSlot;
+  S.tx = dTx;
+  if (prec == Precision::FP32C) {
+    S.sp0 = M.alloc<float4>(ns);
+    S.sp1 = M.alloc<float4>(ns);
+  } else {
+    S.sd = M.alloc<double4_32a>(ns);
+  }
+  if (mode == Mode::RK4) {
+    for (int k = 0; k < 4; ++k) {
+      S.kx[k] = M.alloc<double>(3 * (size_t)nslots);
+      S.kz[k] = M.alloc<double>(nslots);
+    }
+  }
+  S.nslots = nslots;
+  S.ns = ns;
+
+  SolveDev& D = P.dev;
+  D = SolveDev{};
+  D.tx = dTx;
+  D.sp0 = S.sp0;
+  D.sp1 = S.sp1;
+  D.sd = S.sd;
+  D.self = dSelf;
+  D.tileSelf = dTileSelf;
+  D.nslots = nslots;
+  D.ns = ns;
+  D.tileSize = tileSize;
+  D.eps2 = P.eps2;
+}
+
+// Source chunking of one solve.  The rule depends on the solve alone (never on the other
+// solves of a batch), so a target's summation order -- and therefore its result, bit for
+// bit -- is the same whether the solve runs alone, in an ensemble or inside the server.
+// Up to kChunksPerTile chunks of at least kMinChunkTiles source tiles each.
+constexpr int kChunksPerTile = 8;
+constexpr int kMinChunkTiles = 4;
+
+int chunkLength(int ns, int srcTile) {
+  if (ns <= 0) return srcTile;
+  const int minLen = kMinChunkTiles * srcTile;
+  int nch = std::max(1, std::min(kChunksPerTile, (ns + minLen - 1) / minLen));
+  int len = (ns + nch - 1) / nch;
+  return (len + srcTile - 1) / srcTile * srcTile;
+}
+
+// Allocates partial buffers; builds items, block maps and device tables for the batch.
+void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
+  const bool anyPsi = true;  // partial buffers sized for the stream function as well
+  const int ncomp = pairNumComponents(B.prec, anyPsi);
+  const int perSM = std::max(1, pairBlocksPerSM(B.prec, B.shape, false));
+  const int slots = std::max(1, dev.sms * perSM);
+  const int srcTile = B.shape.srcTile;
+  std::vector<WorkItem> items;
+  for (size_t m = 0; m < B.solves.size(); ++m) {
+    SolvePlan& P = *B.solves[m];
+    const int chunkLen = chunkLength(P.ns, srcTile);
+    P.chunkLen = chunkLen;
+    P.nchunks = P.ns > 0 ? (P.ns + chunkLen - 1) / chunkLen : 1;
+    double* partial = P.mem.alloc<double>((size_t)P.nchunks * ncomp * std::max(1, P.nslots));
+    P.stage.partial = partial;
+    P.stage.nchunks = P.nchunks;
+    P.dev.partial = partial;
+    P.dev.nchunks = P.nchunks;
+    for (int t = 0; t < P.ntiles; ++t)
+      for (int c = 0; c < P.nchunks; ++c) {
+        WorkItem w{};
+        w.solve = (int)m;
+        w.tile = t;
+        w.s0 = std::min(P.ns, c * chunkLen);
+        w.s1 = std::min(P.ns, (c + 1) * chunkLen);
+        w.chunk = c;
+        items.push_back(w);
+      }
+  }
+  if (B.solves.size() > 1) {  // longest items first: the tail of the schedule is short items
+    std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
+      const int64_t ca = (int64_t)(a.s1 - a.s0) * std::min(B.shape.tileSize(), B.solves[a.solve]->nslots);
+      const int64_t cb = (int64_t)(b.s1 - b.s0) * std::min(B.shape.tileSize(), B.solves[b.solve]->nslots);
+      return ca > cb;
+    });
+  }
+  B.nitems = (int)items.size();
+  B.grid = std::min(B.nitems, slots);
+
+  const int bs = stageBlockSize();
+  std::vector<int4> prepMap, slotMap;
+  for (size_t m = 0; m < B.solves.size(); ++m) {
+    const SolvePlan& P = *B.solves[m];
+    for (int i = 0; i < P.nslots; i += bs) {
+      prepMap.push_back(make_int4((int)m, i, 0, 0));
+      slotMap.push_back(make_int4((int)m, i, 0, 0));
+    }
+  }
+  for (size_t m = 0; m < B.solves.size(); ++m) {
+    const SolvePlan& P = *B.solves[m];
+    for (int i = 0; i < P.ns; i += bs) prepMap.push_back(make_int4((int)m, i, 1, 0));
+  }
+  B.nPrepBlocks = (int)prepMap.size();
+  B.nSlotBlocks = (int)slotMap.size();
+
+  B.mem.release();
+  B.items = B.mem.alloc<WorkItem>(items.size());
+  B.solveDev = B.mem.alloc<SolveDev>(B.solves.size());
+  B.stageDev = B.mem.alloc<SolveStage>(B.solves.size());
+  B.prepMap = B.mem.alloc<int4>(prepMap.size());
+  B.slotMap = B.mem.alloc<int4>(slotMap.size());
+  B.counter = B.mem.alloc<int>(1);
+  upload(B.items, items, s);
+  upload(B.prepMap, prepMap, s);
+  upload(B.slotMap, slotMap, s);
+  std::vector<SolveDev> sd;
+  std::vector<SolveStage> ss;
+  for (auto& p : B.solves) {
+    sd.push_back(p->dev);
+    ss.push_back(p->stage);
+  }
+  upload(B.solveDev, sd, s);
+  upload(B.stageDev, ss, s);
+  LPM_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(int), s));
+  LPM_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
+}
+
+// Re-uploads the per-solve parameter tables (caller pointers, dt, Omega, eps).
+void refreshTables(Batch& B, cudaStream_t s) {
+  std::vector<SolveDev> sd;
+  std::vector<SolveStage> ss;
+  for (auto& p : B.solves) {
+    sd.push_back(p->dev);
+    ss.push_back(p->stage);
+  }
+  upload(B.solveDev, sd, s);
+  upload(B.stageDev, ss, s);
+  LPM_CUDA(cudaStreamSynchronize(s));
+}
+
+// One evaluation of the direct sums for every solve of the batch.
+void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s) {
+  LPM_CUDA(launchPrep(B.stageDev, B.prepMap, B.nPrepBlocks, prepStage, B.prec, B.counter, s));
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (B.timer) {
+    e0 = B.timer->get();
+    e1 = B.timer->get();
+    LPM_CUDA(cudaEventRecord(e0, s));
+  }
+  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.solveDev, B.items, B.nitems, B.counter, B.grid, s));
+  if (B.timer) {
+    LPM_CUDA(cudaEventRecord(e1, s));
+    B.timer->pending.emplace_back(e0, e1);
+  }
+  LPM_CUDA(launchEpilogue(B.stageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
+}
+
+// One RK4 step (src/LpmBVERK4_Impl.hpp:42-130) for every solve of the batch.
+void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s) {
+  enqueueEval(B, 1, 1, false, true, s);   // RK4-2: x + x_1/2
+  enqueueEval(B, 2, 2, false, true, s);   // RK4-3: x + x_2/2
+  enqueueEval(B, 3, 3, false, true, s);   // RK4-4: x + x_3
+  LPM_CUDA(launchCombine(B.stageDev, B.slotMap, B.nSlotBlocks, quirk, renorm, s));
+  enqueueEval(B, 0, 0, false, true, s);   // RK4-0: u at the new positions
+}
+
+}  // namespace lpm
+
+// ---------------------------------------------------------------------------------------
+// context and C ABI
+// ---------------------------------------------------------------------------------------
+struct lpm_bve_ctx {
+  lpm::DeviceInfo dev;
+  int autotune = 0, verbose = 0;
+  std::string err;
+  cudaStream_t capture = nullptr;  // private stream for graph capture
+  // cached plans
+  std::unique_ptr<lpm::Batch> velBatch;
+  lpm::Mode velMode = lpm::Mode::Distinct;
+  std::unique_ptr<lpm::Batch> rkBatch;
+  std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
+};
+
+struct lpm_bve_ensemble {
+  lpm_bve_ctx* ctx = nullptr;
+  std::unique_ptr<lpm::Batch> batch;
+  unsigned flags = 0;
+};
+
+namespace lpm {
+namespace {
+
+int handle(lpm_bve_ctx* ctx, const Error& e) {
+  if (ctx) ctx->err = e.msg;
+  return e.code;
+}
+
+void setDevice(lpm_bve_ctx* ctx) {
+  int cur = -1;
+  LPM_CUDA(cudaGetDevice(&cur));
+  if (cur != ctx->dev.device) LPM_CUDA(cudaSetDevice(ctx->dev.device));
+}
+
+Precision precOf(unsigned flags) { return (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64; }
+
+PairShape shapeFor(Precision p) { return p == Precision::FP32C ? kDefaultFP32C : kFP64Shape; }
+
+bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si && a.sc == b.sc; }
+
+// True when a cached single-solve batch was built for the same geometry.
+bool sameGeometry(const Batch* B, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask,
+                  bool skipMasked, bool sort, double eps) {
+  if (!B || B->solves.size() != 1) return false;
+  const SolvePlan& P = *B->solves[0];
+  return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
+         sameVec(P.io.bx, io.bx) && P.mask == mask && P.skipMasked == skipMasked && P.sorted == sort &&
+         P.eps2 == eps * eps;
+}
+
+std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io,
+                                  const uint8_t* mask, bool skipMasked, bool sort, double eps, cudaStream_t s) {
+  auto B = std::make_unique<Batch>();
+  B->prec = prec;
+  B->shape = shapeFor(prec);
+  B->rk4 = (mode == Mode::RK4);
+  B->solves.emplace_back(new SolvePlan());
+  buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), s);
+  finalizeBatch(*B, ctx->dev, s);
+  if (ctx->verbose)
+    std::fprintf(stderr, "[lpm_bve] plan: mode=%d prec=%d slots=%d sources=%d tiles=%d chunks=%d items=%d grid=%d\n",
+                 (int)mode, (int)prec, B->solves[0]->nslots, B->solves[0]->ns, B->solves[0]->ntiles,
+                 B->solves[0]->nchunks, B->nitems, B->grid);
+  return B;
+}
+
+// Updates the caller-facing pointers and scalars of a cached plan; re-uploads if changed.
+void bindIO(Batch& B, size_t m, const ParticleIO& io, double dt, double omega, cudaStream_t s, bool& changed) {
+  SolvePlan& P = *B.solves[m];
+  SolveStage& S = P.stage;
+  const ParticleIO& o = S.io;
+  const bool diff = !(sameVec(o.au, io.au) && sameVec(o.bu, io.bu) && o.azeta == io.azeta && o.bzeta == io.bzeta &&
+                      o.apsi == io.apsi && o.bpsi == io.bpsi && o.barea == io.barea && S.dt == dt && S.omega == omega);
+  if (diff) {
+    S.io = io;
+    S.dt = dt;
+    S.omega = omega;
+    P.io = io;
+    changed = true;
+  }
+  (void)s;
+}
+
+}  // namespace
+}  // namespace lpm
+
+using namespace lpm;
+
+extern "C" {
+
+int lpm_bve_ctx_create(lpm_bve_ctx** out, const lpm_bve_opts* opts) {
+  if (!out) return LPM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto* ctx = new lpm_bve_ctx();
+  try {
+    int dev = opts ? opts->device : -1;
+    if (dev < 0) LPM_CUDA(cudaGetDevice(&dev));
+    LPM_CUDA(cudaSetDevice(dev));
+    ctx->dev.device = dev;
+    LPM_CUDA(cudaDeviceGetAttribute(&ctx->dev.sms, cudaDevAttrMultiProcessorCount, dev));
+    int major = 0, minor = 0;
+    LPM_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    LPM_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3)
+      fail(LPM_ERR_NOT_SUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a (GB300) only", dev, major,
+           minor);
+    ctx->autotune = opts ? opts->autotune : 0;
+    ctx->verbose = opts ? opts->verbose : 0;
+    LPM_CUDA(cudaStreamCreateWithFlags(&ctx->capture, cudaStreamNonBlocking));
+  } catch (const Error& e) {
+    const int code = e.code;
+    std::fprintf(stderr, "lpm_bve_ctx_create: %s\n", e.msg.c_str());
+    delete ctx;
+    return code;
+  }
+  *out = ctx;
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_destroy(lpm_bve_ctx* ctx) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  cudaSetDevice(ctx->dev.device);
+  cudaDeviceSynchronize();
+  ctx->velBatch.reset();
+  ctx->rkBatch.reset();
+  if (ctx->capture) cudaStreamDestroy(ctx->capture);
+  delete ctx;
+  return LPM_OK;
+}
+
+const char* lpm_bve_last_error(const lpm_bve_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    LPM_CUDA(cudaDeviceSynchronize());
+    ctx->velBatch.reset();
+    ctx->rkBatch.reset();
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    if (enable && !ctx->timer) ctx->timer = std::make_unique<PairTimer>();
+    if (!enable && ctx->timer) {
+      ctx->timer->collect();
+      ctx->timer.reset();
+    }
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches, int reset) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    double ms = 0.0;
+    int64_t n = 0;
+    if (ctx->timer) {
+      ctx->timer->collect();
+      ms = ctx->timer->totalMs;
+      n = ctx->timer->launches;
+      if (reset) {
+        ctx->timer->totalMs = 0.0;
+        ctx->timer->launches = 0;
+      }
+    }
+    if (pair_ms) *pair_ms = ms;
+    if (pair_launches) *pair_launches = n;
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources* src, double* u, int64_t u_si,
+                     int64_t u_sc, double* psi, unsigned flags, double eps, lpm_stream_t stream) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!src) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: null source set");
+    const bool colloc = flags & LPM_BVE_COLLOCATED;
+    const bool wantVel = !(flags & LPM_BVE_NO_VELOCITY);
+    const bool wantPsi = flags & LPM_BVE_PSI;
+    if (!wantVel && !wantPsi) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: nothing requested (NO_VELOCITY without PSI)");
+    if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: eps must be finite and >= 0");
+    const lpm_points& S = src->pts;
+    checkVec("sources", S.x, S.n, S.stride_i, S.stride_c);
+    if (S.n > 0 && (!src->zeta || !src->area)) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: null zeta/area");
+    int64_t nt = S.n;
+    if (!colloc) {
+      if (!tgt) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: null target set");
+      checkVec("targets", tgt->x, tgt->n, tgt->stride_i, tgt->stride_c);
+      nt = tgt->n;
+    }
+    if (wantVel) checkVec("u", u, nt, u_si, u_sc);
+    if (wantPsi && nt > 0 && !psi) fail(LPM_ERR_INVALID_ARGUMENT, "velocity: PSI requested with null psi");
+    if (nt == 0) return LPM_OK;
+
+    ParticleIO io;
+    io.nb = S.n;
+    io.bx = DVec{const_cast<double*>(S.x), S.stride_i, S.stride_c};
+    io.bzeta = const_cast<double*>(src->zeta);
+    io.barea = src->area;
+    const Mode mode = colloc ? Mode::Collocated : Mode::Distinct;
+    if (colloc) {
+      io.na = 0;
+      io.bu = DVec{wantVel ? u : nullptr, u_si, u_sc};
+      io.bpsi = wantPsi ? psi : nullptr;
+    } else {
+      io.na = tgt->n;
+      io.ax = DVec{const_cast<double*>(tgt->x), tgt->stride_i, tgt->stride_c};
+      io.au = DVec{wantVel ? u : nullptr, u_si, u_sc};
+      io.apsi = wantPsi ? psi : nullptr;
+    }
+    const Precision prec = precOf(flags);
+    const bool sort = !(flags & LPM_BVE_NO_SORT);
+    const bool skip = colloc && (flags & LPM_BVE_SKIP_MASKED_TARGETS);
+    if (!sameGeometry(ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps)) {
+      if (ctx->velBatch) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
+      ctx->velBatch.reset();
+      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, s);
+      ctx->velBatch->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
+    }
+    Batch& B = *ctx->velBatch;
+    bool changed = false;
+    bindIO(B, 0, io, 0.0, 0.0, s, changed);
+    if (changed) refreshTables(B, s);
+    B.timer = ctx->timer.get();
+    enqueueEval(B, 0, 0, wantPsi, wantVel, s);
+    B.timer = nullptr;
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, double Omega, int nsteps, unsigned flags,
+                     double eps, lpm_stream_t stream) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!st) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: null state");
+    if (nsteps < 0) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: negative step count");
+    if (!std::isfinite(dt) || !std::isfinite(Omega)) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: dt/Omega not finite");
+    if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: eps must be finite and >= 0");
+    checkVec("vx", st->vx, st->nverts, st->vx_stride_i, st->vx_stride_c);
+    checkVec("vvel", st->vvel, st->nverts, st->vvel_stride_i, st->vvel_stride_c);
+    checkVec("fx", st->fx, st->nfaces, st->fx_stride_i, st->fx_stride_c);
+    checkVec("fvel", st->fvel, st->nfaces, st->fvel_stride_i, st->fvel_stride_c);
+    if (st->nverts > 0 && !st->vzeta) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: null vzeta");
+    if (st->nfaces > 0 && (!st->fzeta || !st->farea)) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_step: null fzeta/farea");
+    if (nsteps == 0 || st->nverts + st->nfaces == 0) return LPM_OK;
+
+    ParticleIO io;
+    io.na = st->nverts;
+    io.nb = st->nfaces;
+    io.ax = DVec{st->vx, st->vx_stride_i, st->vx_stride_c};
+    io.au = DVec{st->vvel, st->vvel_stride_i, st->vvel_stride_c};
+    io.azeta = st->vzeta;
+    io.bx = DVec{st->fx, st->fx_stride_i, st->fx_stride_c};
+    io.bu = DVec{st->fvel, st->fvel_stride_i, st->fvel_stride_c};
+    io.bzeta = st->fzeta;
+    io.barea = st->farea;
+    const Precision prec = precOf(flags);
+    const bool sort = !(flags & LPM_BVE_NO_SORT);
+    const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
+    if (!sameGeometry(ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps)) {
+      if (ctx->rkBatch) LPM_CUDA(cudaDeviceSynchronize());
+      ctx->rkBatch.reset();
+      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, s);
+      ctx->rkBatch->solves[0]->stage.io = ParticleIO{};
+    }
+    Batch& B = *ctx->rkBatch;
+    bool changed = false;
+    bindIO(B, 0, io, dt, Omega, s, changed);
+    if (changed) refreshTables(B, s);
+    const bool quirk = !(flags & LPM_BVE_RK4_FIX_QUIRK);
+    const bool renorm = flags & LPM_BVE_RENORM;
+    if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer) {
+      B.timer = ctx->timer.get();
+      for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
+      B.timer = nullptr;
+    } else {
+      if (B.graph && (B.graphQuirk != quirk || B.graphRenorm != renorm)) {
+        cudaGraphExecDestroy(B.graph);
+        B.graph = nullptr;
+      }
+      if (!B.graph) {
+        cudaGraph_t g = nullptr;
+        LPM_CUDA(cudaStreamBeginCapture(ctx->capture, cudaStreamCaptureModeThreadLocal));
+        try {
+          enqueueStep(B, quirk, renorm, ctx->capture);
+        } catch (...) {
+          cudaStreamEndCapture(ctx->capture, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        LPM_CUDA(cudaStreamEndCapture(ctx->capture, &g));
+        const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
+        cudaGraphDestroy(g);
+        LPM_CUDA(ie);
+        B.graphQuirk = quirk;
+        B.graphRenorm = renorm;
+      }
+      for (int k = 0; k < nsteps; ++k) LPM_CUDA(cudaGraphLaunch(B.graph, s));
+    }
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// ensembles: many independent solves advanced by one persistent launch per RK4 evaluation
+// ---------------------------------------------------------------------------------------
+int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int nsolves, unsigned flags, double eps,
+                            lpm_stream_t stream, lpm_bve_ensemble** out) {
+  if (!ctx || !out) return LPM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nsolves <= 0 || !states) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_create: no solves");
+    if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_create: bad eps");
+    auto E = std::make_unique<lpm_bve_ensemble>();
+    E->ctx = ctx;
+    E->flags = flags;
+    E->batch = std::make_unique<Batch>();
+    Batch& B = *E->batch;
+    B.prec = precOf(flags);
+    B.shape = shapeFor(B.prec);
+    B.rk4 = true;
+    const bool sort = !(flags & LPM_BVE_NO_SORT);
+    const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
+    for (int m = 0; m < nsolves; ++m) {
+      const lpm_bve_state* st = &states[m];
+      checkVec("vx", st->vx, st->nverts, st->vx_stride_i, st->vx_stride_c);
+      checkVec("vvel", st->vvel, st->nverts, st->vvel_stride_i, st->vvel_stride_c);
+      checkVec("fx", st->fx, st->nfaces, st->fx_stride_i, st->fx_stride_c);
+      checkVec("fvel", st->fvel, st->nfaces, st->fvel_stride_i, st->fvel_stride_c);
+      if (st->nverts + st->nfaces == 0) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_create: solve %d is empty", m);
+      ParticleIO io;
+      io.na = st->nverts;
+      io.nb = st->nfaces;
+      io.ax = DVec{st->vx, st->vx_stride_i, st->vx_stride_c};
+      io.au = DVec{st->vvel, st->vvel_stride_i, st->vvel_stride_c};
+      io.azeta = st->vzeta;
+      io.bx = DVec{st->fx, st->fx_stride_i, st->fx_stride_c};
+      io.bu = DVec{st->fvel, st->fvel_stride_i, st->fvel_stride_c};
+      io.bzeta = st->fzeta;
+      io.barea = st->farea;
+      B.solves.emplace_back(new SolvePlan());
+      buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), s);
+    }
+    finalizeBatch(B, ctx->dev, s);
+    if (ctx->verbose)
+      std::fprintf(stderr, "[lpm_bve] ensemble: %d solves, %d items, grid %d\n", nsolves, B.nitems, B.grid);
+    *out = E.release();
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* Omega, int nsteps, lpm_stream_t stream) {
+  if (!E || !E->ctx) return LPM_ERR_INVALID_ARGUMENT;
+  lpm_bve_ctx* ctx = E->ctx;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!dt || !Omega) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_step: null dt/Omega");
+    if (nsteps < 0) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_step: negative step count");
+    Batch& B = *E->batch;
+    bool changed = false;
+    for (size_t m = 0; m < B.solves.size(); ++m) {
+      if (!std::isfinite(dt[m]) || !std::isfinite(Omega[m])) fail(LPM_ERR_INVALID_ARGUMENT, "ensemble_step: bad dt");
+      SolveStage& S = B.solves[m]->stage;
+      if (S.dt != dt[m] || S.omega != Omega[m]) {
+        S.dt = dt[m];
+        S.omega = Omega[m];
+        changed = true;
+      }
+    }
+    if (changed) refreshTables(B, s);
+    const bool quirk = !(E->flags & LPM_BVE_RK4_FIX_QUIRK);
+    const bool renorm = E->flags & LPM_BVE_RENORM;
+    if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer) {
+      B.timer = ctx->timer.get();
+      for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
+      B.timer = nullptr;
+    } else {
+      if (!B.graph) {
+        cudaGraph_t g = nullptr;
+        LPM_CUDA(cudaStreamBeginCapture(ctx->capture, cudaStreamCaptureModeThreadLocal));
+        try {
+          enqueueStep(B, quirk, renorm, ctx->capture);
+        } catch (...) {
+          cudaStreamEndCapture(ctx->capture, &g);
+          if (g) cudaGraphDestroy(g);
+          throw;
+        }
+        LPM_CUDA(cudaStreamEndCapture(ctx->capture, &g));
+        const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
+        cudaGraphDestroy(g);
+        LPM_CUDA(ie);
+      }
+      for (int k = 0; k < nsteps; ++k) LPM_CUDA(cudaGraphLaunch(B.graph, s));
+    }
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_ensemble_info(const lpm_bve_ensemble* E, int* nsolves, int* nitems, int* grid, int64_t* pairs_per_eval,
+                          size_t* device_bytes) {
+  if (!E || !E->batch) return LPM_ERR_INVALID_ARGUMENT;
+  const Batch& B = *E->batch;
+  int64_t pairs = 0;
+  size_t bytes = B.mem.bytes();
+  for (auto& p : B.solves) {
+    pairs += (int64_t)p->nslots * p->ns;
+    bytes += p->mem.bytes();
+  }
+  if (nsolves) *nsolves = (int)B.solves.size();
+  if (nitems) *nitems = B.nitems;
+  if (grid) *grid = B.grid;
+  if (pairs_per_eval) *pairs_per_eval = pairs;
+  if (device_bytes) *device_bytes = bytes;
+  return LPM_OK;
+}
+
+int lpm_bve_ensemble_destroy(lpm_bve_ensemble* E) {
+  if (!E) return LPM_ERR_INVALID_ARGUMENT;
+  if (E->ctx) {
+    cudaSetDevice(E->ctx->dev.device);
+    cudaDeviceSynchronize();
+  }
+  delete E;
+  return LPM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// engine.hpp -- internal data layout shared by the BVE kernels and the host engine.
+//
+// One evaluation of the direct sum is organised as:
+//   prep      (O(N))  : stage positions x + c*k in FP64, packed source records,
+//   pair      (O(N^2)): persistent CTAs pull work items (target tile x source chunk)
+//                       and write one partial sum per (chunk, target),
+//   epilogue  (O(N))  : fixed-order sum of the partials, FP64 cross product,
+//                       velocity written to the caller's arrays, RK4 stage increments.
+// Targets live in "slots": a spatially sorted permutation of the caller's vertices and
+// faces, so that each target tile is compact on the sphere.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lpm {
+
+constexpr double kPi = 3.1415926535897932384626433832795027975;
+
+// A caller-owned FP64 vector array: element (i, c) at p[i*si + c*sc].
+struct DVec {
+  double* p = nullptr;
+  int64_t si = 0, sc = 0;
+};
+
+// The particles of one solve as the caller sees them.  "a" particles are targets only
+// (vertices, or the target points of a distinct-set call); "b" particles are faces:
+// sources when unmasked, and targets too when they appear in the slot list.
+struct ParticleIO {
+  int64_t na = 0, nb = 0;
+  DVec ax, au;                 // positions / velocity output of the a-particles
+  double* azeta = nullptr;     // a-particle vorticity (RK4: integrated, not a source)
+  double* apsi = nullptr;      // stream function output (a)
+  DVec bx, bu;                 // positions / velocity output of the b-particles
+  double* bzeta = nullptr;     // b-particle (source) vorticity
+  double* bpsi = nullptr;
+  const double* barea = nullptr;
+};
+
+// Pair-kernel work item: one target tile against one contiguous source chunk.
+struct WorkItem {
+  int solve;     // index into the SolveDev table
+  int tile;      // target tile within the solve
+  int s0, s1;    // source range [s0, s1) within the solve
+  int chunk;     // partial-sum slot (chunk index within the tile's row)
+  int pad0, pad1, pad2;
+};
+
+// Device-side description of one solve for the pair kernels.
+struct SolveDev {
+  const double* tx;          // [3][nslots] stage positions of the target slots (SoA)
+  const float4* sp0;         // [ns] FP32C: (x_hi, y_hi, z_hi, w = -zeta*A/(2 pi))
+  const float4* sp1;         // [ns] FP32C: (x_lo, y_lo, z_lo, D = 1 - |x|^2)
+  const double4_32a* sd;         // [ns] FP64 : (x, y, z, -zeta*A)
+  const int* self;           // [nslots] source index of the same particle, -1 if none
+  const int2* tileSelf;      // [ntiles] min/max self index of the tile (-1,-2 if none)
+  double* partial;           // [nchunks][ncomp][nslots]
+  int nslots, ns, tileSize, nchunks;
+  double eps2;
+};
+
+// Per-solve parameters for the O(N) kernels.
+struct SolveStage {
+  ParticleIO io;
+  const int* perm;           // [nslots] slot -> particle id (id < na: a-particle, else face id - na)
+  const int* srcFace;        // [ns] source -> face index
+  const int* srcSlot;        // [ns] source -> slot of the same face (-1 if the face is not a target)
+  double* tx;                // [3][nslots]
+  float4* sp0; float4* sp1; double4_32a* sd;
+  double* kx[4];             // [3][nslots] RK4 position increments x_k = dt*u
+  double* kz[4];             // [nslots]    RK4 vorticity increments
+  const double* partial;     // [nchunks][ncomp][nslots]
+  int nslots, ns, nchunks;
+  double dt, omega;
+};
+
+// Launch-shape of the FP32C pair kernel.
+struct PairShape {
+  int threads;   // CTA size
+  int k;         // targets per thread
+  int srcTile;   // sources staged in shared memory per step
+  int tileSize() const { return threads * k; }
+};
+
+enum class Precision { FP64 = 0, FP32C = 1 };
+
+// ---- kernel launchers (pair_kernels.cu / stage_kernels.cu) ----------------------------
+// The O(N) kernels walk a block map of int4 {solve, first index, kind, 0}; kind 0 = target
+// slots, kind 1 = source records (prep only).
+// prep stage: 0 = plain evaluation at x, 1 = RK4 stage-2 inputs (x + x_1/2 with x_1 = dt*u
+// from the stored velocity), 2 = stage-3 inputs (x + x_2/2), 3 = stage-4 inputs (x + x_3).
+cudaError_t launchPrep(const SolveStage* st, const int4* map, int nblocks, int stage, Precision prec, int* counter,
+                       cudaStream_t s);
+// stageOut: 0 = no increments, 1..3 = write x_k/zeta_k of RK4 stage k+1.
+cudaError_t launchEpilogue(const SolveStage* st, const int4* map, int nblocks, Precision prec, bool psi,
+                           bool velocity, int stageOut, cudaStream_t s);
+cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bool quirk, bool renorm,
+                          cudaStream_t s);
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, const SolveDev* solves,
+                       const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s);
+int stageBlockSize();
+int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi);
+bool pairShapeSupported(Precision prec, const PairShape& shape);
+int pairNumComponents(Precision prec, bool psi);  // partial-sum components per (chunk, slot)
+
+}  // namespace lpm

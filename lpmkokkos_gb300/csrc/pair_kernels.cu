@@ -1,0 +1,326 @@
+// pair_kernels.cu -- the O(N^2) direct sums of the BVE path for sm_103a.
+//
+// Two kernels evaluate the spherical Biot-Savart velocity (and optionally the stream
+// function) of pbosler/lpmKokkos (src/LpmBVEKernels.hpp:21-44 greensFn / biotSavart,
+// reductions :49-102 and :188-234) over work items (target tile x source chunk):
+//
+//  * pairFP64  -- the plain FP64 path (the GPU oracle).  Per pair it evaluates the
+//    reference expression with the same operation order; multiplications and additions
+//    are issued as __dmul_rn/__dadd_rn so no fused multiply-add changes a single pair's
+//    rounding against the CPU.  Only the summation order differs (unpinned in Kokkos).
+//
+//  * pairFP32C -- the FP32-compensated path.  With d_j = x_j - x_i and
+//    1 - x_i.x_j = |d|^2/2 + delta_i + delta_j (delta = (1 - |x|^2)/2, exact identity),
+//      u_i = x_i x sum_j s_j d_j,   s_j = (-zeta_j A_j / 2 pi) / (|d|^2 + D_i + D_j + 2 eps^2),
+//    D = 1 - |x|^2.  Coordinates are FP64 hi/lo float pairs; each CTA subtracts the centre
+//    of its target tile once per staged source, so every FP32 difference is taken between
+//    nearby small numbers.  Per pair: 13 FP32 FMA-pipe ops + one MUFU.RCP
+//    (3 FADD d, 1 FADD + 3 FFMA for 2q, 2 FFMA Newton step, 1 FMUL, 3 FFMA accumulate).
+//    Each 32-source sub-block is summed in FP32 and added to a Kahan-compensated FP32
+//    accumulator; partials leave the kernel in FP64 and the epilogue forms the FP64 cross
+//    product.  Stream function: + MUFU.LG2, 1 FFMA, 1 FADD per pair.
+//
+// Both kernels are persistent: each CTA takes work items from an atomic counter until
+// the list is exhausted.  Self pairs (i == j, collocated face targets) are excluded by
+// index only on the few source tiles that can contain them (tileSelf range), so the
+// common path carries no compare.
+
+#include "engine.hpp"
+
+#include <cstdio>
+
+namespace lpm {
+namespace {
+
+__device__ __forceinline__ float rcpApprox(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2Approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+
+// Kahan step: add v into the compensated pair (h, c); the represented value is h - c.
+__device__ __forceinline__ void kahanAdd(float& h, float& c, float v) {
+  const float y = v - c;
+  const float t = h + y;
+  c = (t - h) - y;
+  h = t;
+}
+
+// FP32 relative coordinate (x - centre) from an FP64 value split as hi + lo.
+__device__ __forceinline__ float relCoord(float hi, float lo, float chi, float clo) {
+  return (hi - chi) + (lo - clo);
+}
+
+constexpr int kSub = 32;  // sources per FP32 sub-block before the compensated add
+
+template <int K, bool PSI, bool CHECKED>
+__device__ __forceinline__ void fp32cTile(const float4* __restrict__ sP, const float* __restrict__ sD, int nsrc,
+                                          int jbase, const float (&ax)[K], const float (&ay)[K], const float (&az)[K],
+                                          const float (&C)[K], const int (&self)[K],
+                                          float (&hx)[K], float (&hy)[K], float (&hz)[K],
+                                          float (&cx)[K], float (&cy)[K], float (&cz)[K],
+                                          float (&hp)[K], float (&cp)[K], float (&hw)[K], float (&cw)[K]) {
+#pragma unroll 1
+  for (int j0 = 0; j0 < nsrc; j0 += kSub) {
+    float vx[K], vy[K], vz[K], vp[K], vw[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) { vx[k] = 0.f; vy[k] = 0.f; vz[k] = 0.f; vp[k] = 0.f; vw[k] = 0.f; }
+#pragma unroll 4
+    for (int j = j0; j < j0 + kSub; ++j) {
+      const float4 P = sP[j];
+      const float Dj = sD[j];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const float dx = P.x - ax[k];
+        const float dy = P.y - ay[k];
+        const float dz = P.z - az[k];
+        const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, Dj + C[k])));
+        float r = rcpApprox(q2);
+        const float e = fmaf(-q2, r, 1.0f);
+        r = fmaf(r, e, r);
+        float s = P.w * r;
+        float wl = 0.f, ww = 0.f;
+        if (PSI) { wl = P.w * lg2Approx(q2); ww = P.w; }
+        if (CHECKED) {
+          const bool me = (jbase + j) == self[k];
+          s = me ? 0.f : s;
+          if (PSI) { wl = me ? 0.f : wl; ww = me ? 0.f : ww; }
+        }
+        vx[k] = fmaf(s, dx, vx[k]);
+        vy[k] = fmaf(s, dy, vy[k]);
+        vz[k] = fmaf(s, dz, vz[k]);
+        if (PSI) { vp[k] += wl; vw[k] += ww; }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      kahanAdd(hx[k], cx[k], vx[k]);
+      kahanAdd(hy[k], cy[k], vy[k]);
+      kahanAdd(hz[k], cz[k], vz[k]);
+      if (PSI) { kahanAdd(hp[k], cp[k], vp[k]); kahanAdd(hw[k], cw[k], vw[k]); }
+    }
+  }
+}
+
+template <int NTH, int K, int ST, bool PSI>
+__global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ solves,
+                                                 const WorkItem* __restrict__ items, int nitems,
+                                                 int* __restrict__ counter) {
+  static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
+  __shared__ float4 sP[ST];
+  __shared__ float sD[ST];
+  __shared__ int sItem;
+
+  for (;;) {
+    if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = sItem;
+    __syncthreads();
+    if (it >= nitems) return;
+    const WorkItem w = items[it];
+    const SolveDev& S = solves[w.solve];
+    const int n = S.nslots;
+    const int tile0 = w.tile * (NTH * K);
+    const int tcount = min(NTH * K, n - tile0);
+
+    // Tile centre: the middle target of the tile (slots are spatially sorted).
+    const int cs = tile0 + (tcount >> 1);
+    const double cxd = S.tx[cs], cyd = S.tx[n + cs], czd = S.tx[2 * n + cs];
+    const float chx = __double2float_rn(cxd), chy = __double2float_rn(cyd), chz = __double2float_rn(czd);
+    const float clx = __double2float_rn(cxd - (double)chx);
+    const float cly = __double2float_rn(cyd - (double)chy);
+    const float clz = __double2float_rn(czd - (double)chz);
+
+    float ax[K], ay[K], az[K], C[K];
+    int self[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int slot = tile0 + threadIdx.x + k * NTH;
+      if (threadIdx.x + k * NTH < tcount) {
+        const double x = S.tx[slot], y = S.tx[n + slot], z = S.tx[2 * n + slot];
+        const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+        ax[k] = relCoord(hx, __double2float_rn(x - (double)hx), chx, clx);
+        ay[k] = relCoord(hy, __double2float_rn(y - (double)hy), chy, cly);
+        az[k] = relCoord(hz, __double2float_rn(z - (double)hz), chz, clz);
+        C[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * S.eps2);
+        self[k] = S.self[slot];
+      } else {
+        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; C[k] = 1.f; self[k] = -1;
+      }
+    }
+    float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
+      hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
+    }
+    const int2 ts = S.tileSelf[w.tile];
+
+    for (int b0 = w.s0; b0 < w.s1; b0 += ST) {
+      // Stage ST sources relative to the tile centre; padding (w = 0, D = 1) adds exactly 0.
+      for (int j = threadIdx.x; j < ST; j += NTH) {
+        const int s = b0 + j;
+        if (s < w.s1) {
+          const float4 p0 = S.sp0[s];
+          const float4 p1 = S.sp1[s];
+          sP[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
+                              relCoord(p0.z, p1.z, chz, clz), p0.w);
+          sD[j] = p1.w;
+        } else {
+          sP[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+          sD[j] = 1.f;
+        }
+      }
+      __syncthreads();
+      const bool checked = (ts.x <= b0 + ST - 1) && (ts.y >= b0);
+      if (checked)
+        fp32cTile<K, PSI, true>(sP, sD, ST, b0, ax, ay, az, C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+      else
+        fp32cTile<K, PSI, false>(sP, sD, ST, b0, ax, ay, az, C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+      __syncthreads();
+    }
+
+    // Partials: [chunk][comp][slot], FP64.
+    double* out = S.partial + (size_t)w.chunk * (PSI ? 5 : 3) * n;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      const int slot = tile0 + threadIdx.x + k * NTH;
+      if (threadIdx.x + k * NTH < tcount) {
+        out[slot] = (double)hx[k] - (double)cx[k];
+        out[n + slot] = (double)hy[k] - (double)cy[k];
+        out[2 * n + slot] = (double)hz[k] - (double)cz[k];
+        if (PSI) {
+          out[3 * n + slot] = (double)hp[k] - (double)cp[k];
+          out[4 * n + slot] = (double)hw[k] - (double)cw[k];
+        }
+      }
+    }
+  }
+}
+
+constexpr int kFP64Threads = 128;
+constexpr int kFP64Tile = 128;
+constexpr double kFourPi = 4 * kPi;
+
+template <bool PSI>
+__global__ void __launch_bounds__(kFP64Threads) pairFP64(const SolveDev* __restrict__ solves,
+                                                         const WorkItem* __restrict__ items, int nitems,
+                                                         int* __restrict__ counter) {
+  __shared__ double4_32a sS[kFP64Tile];
+  __shared__ int sItem;
+  for (;;) {
+    if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = sItem;
+    __syncthreads();
+    if (it >= nitems) return;
+    const WorkItem w = items[it];
+    const SolveDev& S = solves[w.solve];
+    const int n = S.nslots;
+    const int slot = w.tile * kFP64Threads + threadIdx.x;
+    const bool live = slot < n;
+    double tx = 0.0, ty = 0.0, tz = 0.0;
+    int self = -1;
+    if (live) { tx = S.tx[slot]; ty = S.tx[n + slot]; tz = S.tx[2 * n + slot]; self = S.self[slot]; }
+    const double eps2 = S.eps2;
+    double u0 = 0.0, u1 = 0.0, u2 = 0.0, ps = 0.0;
+    for (int b0 = w.s0; b0 < w.s1; b0 += kFP64Tile) {
+      const int cnt = min(kFP64Tile, w.s1 - b0);
+      if (threadIdx.x < cnt) sS[threadIdx.x] = S.sd[b0 + threadIdx.x];
+      __syncthreads();
+      for (int j = 0; j < cnt; ++j) {
+        if (b0 + j == self) continue;
+        const double4_32a s = sS[j];
+        // biotSavart: cross(tgt, src) * (-zeta*A) / (4 pi (1 - dot(src, tgt)))
+        const double dp = __dadd_rn(__dadd_rn(__dmul_rn(s.x, tx), __dmul_rn(s.y, ty)), __dmul_rn(s.z, tz));
+        const double omd = __dadd_rn(__dsub_rn(1.0, dp), eps2);
+        const double strength = s.w / __dmul_rn(kFourPi, omd);
+        const double c0 = __dsub_rn(__dmul_rn(ty, s.z), __dmul_rn(tz, s.y));
+        const double c1 = __dsub_rn(__dmul_rn(tz, s.x), __dmul_rn(tx, s.z));
+        const double c2 = __dsub_rn(__dmul_rn(tx, s.y), __dmul_rn(ty, s.x));
+        u0 = __dadd_rn(u0, __dmul_rn(c0, strength));
+        u1 = __dadd_rn(u1, __dmul_rn(c1, strength));
+        u2 = __dadd_rn(u2, __dmul_rn(c2, strength));
+        if (PSI) ps = __dadd_rn(ps, __dmul_rn(log(omd), s.w) / kFourPi);  // greensFn
+      }
+      __syncthreads();
+    }
+    if (live) {
+      double* out = S.partial + (size_t)w.chunk * (PSI ? 4 : 3) * n;
+      out[slot] = u0; out[n + slot] = u1; out[2 * n + slot] = u2;
+      if (PSI) out[3 * n + slot] = ps;
+    }
+  }
+}
+
+template <int NTH, int K, int ST>
+struct FP32CEntry {
+  static void* fn(bool psi) {
+    return psi ? (void*)pairFP32C<NTH, K, ST, true> : (void*)pairFP32C<NTH, K, ST, false>;
+  }
+};
+
+// Instantiated launch shapes (the autotuner chooses among these).
+struct ShapeFn { int threads, k, srcTile; void* fnPlain; void* fnPsi; };
+const ShapeFn kShapes[] = {
+  {128, 4, 256, (void*)pairFP32C<128, 4, 256, false>, (void*)pairFP32C<128, 4, 256, true>},
+  {128, 2, 256, (void*)pairFP32C<128, 2, 256, false>, (void*)pairFP32C<128, 2, 256, true>},
+  {256, 2, 256, (void*)pairFP32C<256, 2, 256, false>, (void*)pairFP32C<256, 2, 256, true>},
+  {256, 4, 512, (void*)pairFP32C<256, 4, 512, false>, (void*)pairFP32C<256, 4, 512, true>},
+  {128, 8, 256, (void*)pairFP32C<128, 8, 256, false>, (void*)pairFP32C<128, 8, 256, true>},
+};
+
+const ShapeFn* findShape(const PairShape& s) {
+  for (const auto& e : kShapes)
+    if (e.threads == s.threads && e.k == s.k && e.srcTile == s.srcTile) return &e;
+  return nullptr;
+}
+
+void* kernelFor(Precision prec, const PairShape& shape, bool psi, int& threads) {
+  if (prec == Precision::FP64) {
+    threads = kFP64Threads;
+    return psi ? (void*)pairFP64<true> : (void*)pairFP64<false>;
+  }
+  const ShapeFn* e = findShape(shape);
+  if (!e) return nullptr;
+  threads = e->threads;
+  return psi ? e->fnPsi : e->fnPlain;
+}
+
+}  // namespace
+
+bool pairShapeSupported(Precision prec, const PairShape& shape) {
+  if (prec == Precision::FP64) return shape.threads == kFP64Threads && shape.k == 1 && shape.srcTile == kFP64Tile;
+  return findShape(shape) != nullptr;
+}
+
+int pairNumComponents(Precision prec, bool psi) {
+  if (prec == Precision::FP64) return psi ? 4 : 3;
+  return psi ? 5 : 3;
+}
+
+int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {
+  int threads = 0;
+  void* fn = kernelFor(prec, shape, psi, threads);
+  if (!fn) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, 0) != cudaSuccess) return 0;
+  return nb;
+}
+
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, const SolveDev* solves,
+                       const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s) {
+  int threads = 0;
+  void* fn = kernelFor(prec, shape, psi, threads);
+  if (!fn) return cudaErrorInvalidValue;
+  if (nitems <= 0 || grid <= 0) return cudaSuccess;
+  void* args[] = {(void*)&solves, (void*)&items, (void*)&nitems, (void*)&counter};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, 0, s);
+}
+
+}  // namespace lpm

@@ -24,6 +24,7 @@
 #include <cstdint>
 #include <cstdlib>
 #include <cstring>
+#include <random>
 #include <vector>
 #include <stdexcept>
 #include <string>
@@ -574,6 +575,29 @@ void oracle_ic_solid_body(const double* x, long n, double* zeta) {            //
   const Real OMEGA = 2*PI;
   for (long i = 0; i < n; ++i) zeta[i] = 2*OMEGA*x[3*i+2];
 }
+// Seeded Gaussian-vortex parameters (input generation, no reference counterpart):
+// centres = normalised 3-vectors of Box-Muller normals, amplitudes U(lo, hi); uniforms are the
+// top 53 bits of std::mt19937_64 draws.
+void oracle_gaussian_params(unsigned long long seed, int ng, double lo, double hi, double* centers, double* amps) {
+  std::mt19937_64 gen(seed);
+  auto u53 = [&]() { return (double)(gen() >> 11) * (1.0 / 9007199254740992.0); };
+  for (int g = 0; g < ng; ++g) {
+    double v[3], r2 = 0.0;
+    do {
+      r2 = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        const double a = 1.0 - u53();
+        const double b = u53();
+        v[k] = std::sqrt(-2.0*std::log(a)) * std::cos(2.0*PI*b);
+        r2 += v[k]*v[k];
+      }
+    } while (r2 < 1e-20);
+    const double sc = 1.0 / std::sqrt(r2);
+    for (int k = 0; k < 3; ++k) centers[3*g+k] = v[k]*sc;
+    amps[g] = lo + (hi - lo)*u53();
+  }
+}
+
 void oracle_ic_gaussians_add(const double* x, long n, const double* centers, const double* amps, int ng,
                              double width, double* zeta) {
   for (long i = 0; i < n; ++i) {

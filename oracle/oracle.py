@@ -76,6 +76,7 @@ def _setup(L):
     for name in ("oracle_ic_rh54", "oracle_rh54_velocity", "oracle_ic_solid_body"):
         getattr(L, name).argtypes = [D, ctypes.c_long, D]
     L.oracle_ic_gaussians_add.argtypes = [D, ctypes.c_long, D, D, ctypes.c_int, ctypes.c_double, D]
+    L.oracle_gaussian_params.argtypes = [ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D]
     L.oracle_errnorms_vec.argtypes = [D, D, D, ctypes.c_long, D]
     L.oracle_poisson.argtypes = [ctypes.c_int, ctypes.c_int, D]
     L.oracle_poisson.restype = ctypes.c_int
@@ -176,6 +177,21 @@ def ic_gaussians_add(x, zeta, centers, amps, width):
     c = np.ascontiguousarray(centers, dtype=np.float64)
     a = np.ascontiguousarray(amps, dtype=np.float64)
     lib().oracle_ic_gaussians_add(_dp(x), x.shape[0], _dp(c), _dp(a), a.shape[0], float(width), _dp(z))
+    return z
+
+
+def gaussian_params(seed, ng, lo=-2.0, hi=2.0):
+    c = np.zeros((ng, 3)); a = np.zeros(ng)
+    lib().oracle_gaussian_params(int(seed), int(ng), float(lo), float(hi), _dp(c), _dp(a))
+    return c, a
+
+
+def rh54_gaussians(x, seed, ng, width=0.1):
+    """RH54 relative vorticity plus ng seeded Gaussian vortices (the benchmark's initial data)."""
+    z = ic_rh54(x)
+    if ng > 0:
+        c, a = gaussian_params(seed, ng)
+        z = ic_gaussians_add(x, z, c, a, width)
     return z
 
 

@@ -1,0 +1,155 @@
+"""GPU parity of the RK4 stepper (lpm_bve_rk4_step) and the ensemble engine.
+
+Checked over vertices and leaf faces (masked parents are advanced but excluded):
+  FP64  vs oracle RK4     : max-relative <= 1e-12 on positions, vorticity, velocity
+  FP32C vs FP64 (GPU)     : relative L2 <= 1e-6 on velocity and vorticity after a few steps
+  ensemble vs single solve: bitwise identical (per-target summation order is fixed)
+  graph vs direct launch  : bitwise identical
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import lpmkokkos_gb300 as P
+
+pytestmark = pytest.mark.gpu
+
+OMEGA = 2 * math.pi
+
+
+def _sphere(ctx, seed, level, prec, ng=3, rseed=20261203, layout="left"):
+    from lpmkokkos_gb300 import bve
+    s = bve.BVESphere(seed, level, layout=layout)
+    s.init_vorticity(bve.rh54_gaussians(rseed, ng), ctx, flags=prec)
+    torch.cuda.synchronize()
+    return s
+
+
+def _host(st):
+    return [t.cpu().numpy().copy() for t in (st.vx, st.vzeta, st.vvel, st.fx, st.fzeta, st.fvel)]
+
+
+def _same(x, y):
+    """Bitwise equality where NaN == NaN (masked parents that coincide with a leaf are inf/nan,
+    as in the reference)."""
+    return bool(torch.equal(torch.isnan(x), torch.isnan(y))) and bool(torch.equal(torch.nan_to_num(x),
+                                                                                      torch.nan_to_num(y)))
+
+
+def _maxrel(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+def _l2rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("quirk", [True, False])
+@pytest.mark.parametrize("seed,level", [(0, 2), (1, 3)])
+def test_fp64_rk4_matches_oracle(ctx, oracle, seed, level, quirk):
+    s = _sphere(ctx, seed, level, P.FP64)
+    st = s.state()
+    h = _host(st)
+    flags = P.FP64 | (0 if quirk else P.RK4_FIX_QUIRK)
+    nsteps, dt = 3, 0.01
+    ctx.rk4_step(st, dt, OMEGA, nsteps, flags=flags)
+    torch.cuda.synchronize()
+    ref = oracle.rk4(*h, s.mesh["farea"], s.mesh["fmask"], dt, OMEGA, nsteps, quirk=quirk)
+    got = _host(st)
+    leaf = s.mesh["fmask"] == 0
+    for k, name in enumerate(("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")):
+        g, r = got[k], ref[k]
+        if k >= 3:
+            g, r = g[leaf], r[leaf]
+        assert _maxrel(g, r) <= 1e-12, (name, _maxrel(g, r))
+
+
+def test_quirk_changes_only_face_vorticity(ctx):
+    a = _sphere(ctx, 0, 2, P.FP64); b = _sphere(ctx, 0, 2, P.FP64)
+    ctx.rk4_step(a.state(), 0.01, OMEGA, 1, flags=P.FP64)
+    ctx.rk4_step(b.state(), 0.01, OMEGA, 1, flags=P.FP64 | P.RK4_FIX_QUIRK)
+    torch.cuda.synchronize()
+    same = _same
+    assert same(a.physVerts, b.physVerts) and same(a.relVortVerts, b.relVortVerts)
+    assert same(a.physFaces, b.physFaces)
+    assert not same(a.relVortFaces, b.relVortFaces)
+
+
+@pytest.mark.parametrize("seed,level", [(0, 4), (1, 4)])
+def test_fp32c_rk4_tracks_fp64(ctx, seed, level):
+    a = _sphere(ctx, seed, level, P.FP64)
+    b = _sphere(ctx, seed, level, P.FP32C)
+    leaf = torch.from_numpy(a.mesh["fmask"] == 0).cuda()
+    for step in range(3):
+        ctx.rk4_step(a.state(), 0.01, OMEGA, 1, flags=P.FP64)
+        ctx.rk4_step(b.state(), 0.01, OMEGA, 1, flags=P.FP32C)
+        torch.cuda.synchronize()
+        ua = torch.cat([a.velocityVerts, a.velocityFaces[leaf]]).cpu().numpy()
+        ub = torch.cat([b.velocityVerts, b.velocityFaces[leaf]]).cpu().numpy()
+        za = a.relVortFaces[leaf].cpu().numpy(); zb = b.relVortFaces[leaf].cpu().numpy()
+        assert _l2rel(ub, ua) <= 1e-6, (step, _l2rel(ub, ua))
+        assert _l2rel(zb, za) <= 1e-6, (step, _l2rel(zb, za))
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32C])
+def test_graph_equals_direct(ctx, prec):
+    a = _sphere(ctx, 0, 3, prec); b = _sphere(ctx, 0, 3, prec)
+    ctx.rk4_step(a.state(), 0.01, OMEGA, 2, flags=prec)
+    ctx.rk4_step(b.state(), 0.01, OMEGA, 2, flags=prec | P.NO_GRAPH)
+    torch.cuda.synchronize()
+    for x, y in ((a.physVerts, b.physVerts), (a.velocityFaces, b.velocityFaces), (a.relVortFaces, b.relVortFaces)):
+        assert _same(x, y)
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32C])
+def test_layouts_agree(ctx, prec):
+    a = _sphere(ctx, 1, 3, prec, layout="left"); b = _sphere(ctx, 1, 3, prec, layout="right")
+    ctx.rk4_step(a.state(), 0.01, OMEGA, 2, flags=prec)
+    ctx.rk4_step(b.state(), 0.01, OMEGA, 2, flags=prec)
+    torch.cuda.synchronize()
+    assert _same(a.physFaces, b.physFaces) and _same(a.velocityVerts, b.velocityVerts)
+
+
+def test_solid_body_rotation(ctx):
+    """tests/LpmBVETest.cpp: zeta = 2*Omega*z rotates rigidly; u ~ Omega(-y, x, 0)."""
+    from lpmkokkos_gb300 import bve
+    s = bve.BVESphere(1, 3)
+    s.init_vorticity(bve.ic_solid_body, ctx, flags=P.FP64)
+    torch.cuda.synchronize()
+    x = s.physFaces.cpu().numpy(); u = s.velocityFaces.cpu().numpy()
+    leaf = s.mesh["fmask"] == 0
+    exact = np.stack([-OMEGA * x[:, 1], OMEGA * x[:, 0], 0 * x[:, 0]], axis=1)
+    err = np.linalg.norm(u[leaf] - exact[leaf]) / np.linalg.norm(exact[leaf])
+    assert err < 0.05  # cubed sphere level 3: discretisation error only
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32C])
+def test_ensemble_equals_single(ctx, prec):
+    from lpmkokkos_gb300 import bve
+    specs = [(0, 2, 1), (1, 3, 2), (0, 3, 3), (1, 2, 4)]
+    singles = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
+    ens = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
+    dts = [0.01, 0.02, 0.005, 0.01]
+    for s, dt in zip(singles, dts):
+        ctx.rk4_step(s.state(), dt, OMEGA, 2, flags=prec)
+    e = ctx.ensemble([s.state() for s in ens], flags=prec)
+    e.step(dts, [OMEGA] * 4, 2)
+    torch.cuda.synchronize()
+    info = e.info()
+    assert info["nsolves"] == 4 and info["nitems"] > 0
+    for s, t in zip(singles, ens):
+        assert _same(s.physFaces, t.physFaces)
+        assert _same(s.velocityVerts, t.velocityVerts)
+        assert _same(s.relVortFaces, t.relVortFaces)
+    e.close()
+
+
+def test_pair_timing(ctx):
+    s = _sphere(ctx, 0, 3, P.FP32C)
+    ctx.set_timing(True)
+    ctx.rk4_step(s.state(), 0.01, OMEGA, 2, flags=P.FP32C)
+    ms, n = ctx.timing()
+    ctx.set_timing(False)
+    assert n == 8 and ms > 0.0

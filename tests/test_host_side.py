@@ -1,0 +1,88 @@
+"""Host-side parts of the product checked on CPU: mesh builder, initial conditions, and the
+C ABI library's exported symbols (no compute call needs a GPU here)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+@pytest.mark.parametrize("level", [0, 1, 2, 3, 4, 5])
+def test_product_mesh_equals_oracle_bitwise(native, oracle, seed, level):
+    from lpmkokkos_gb300 import bve
+    a = bve.build_mesh(seed, level)
+    b = oracle.mesh(seed, level)
+    assert (a["nverts"], a["nfaces"], a["nleaves"]) == (b["nverts"], b["nfaces"], b["nleaves"])
+    for k in ("vx", "fx", "farea", "fmask"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_mesh_counts(native):
+    from lpmkokkos_gb300 import bve
+    # SURVEY table: icos L4/L7/L8 and cube L4/L7
+    assert bve.mesh_counts(0, 4) == (2562, 6820, 5120)
+    assert bve.mesh_counts(0, 7) == (163842, 436900, 327680)
+    assert bve.mesh_counts(0, 8) == (655362, 1747620, 1310720)
+    assert bve.mesh_counts(1, 4) == (1538, 2046, 1536)
+    assert bve.mesh_counts(1, 7) == (98306, 131070, 98304)
+
+
+def test_initial_conditions_equal_oracle(native, oracle):
+    from lpmkokkos_gb300 import bve
+    m = oracle.mesh(0, 4)
+    for x in (m["vx"], m["fx"]):
+        assert np.array_equal(bve.ic_rh54(x), oracle.ic_rh54(x))
+        assert np.array_equal(bve.rh54_velocity(x), oracle.rh54_velocity(x))
+        assert np.array_equal(bve.ic_solid_body(x), oracle.ic_solid_body(x))
+    c, a = bve.gaussian_params(20261204, 8)
+    c2, a2 = oracle.gaussian_params(20261204, 8)
+    assert np.array_equal(c, c2) and np.array_equal(a, a2)
+    assert np.allclose(np.linalg.norm(c, axis=1), 1.0, atol=1e-15)
+    assert np.all((a >= -2) & (a < 2))
+    z = bve.ic_gaussians_add(m["fx"], bve.ic_rh54(m["fx"]), c, a, 0.1)
+    assert np.array_equal(z, oracle.rh54_gaussians(m["fx"], 20261204, 8, 0.1))
+
+
+def test_invalid_host_arguments(native):
+    from lpmkokkos_gb300 import _lib as L
+    lib = L.lib()
+    assert lib.lpm_mesh_build(7, 2, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_mesh_build(0, -1, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_ic_gaussians_add(None, 4, None, None, 0, 0.1, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_bve_ctx_destroy(None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_bve_velocity(None, None, None, None, 0, 0, None, 0, 0.0, None) == L.LPM_ERR_INVALID_ARGUMENT
+
+
+def _declared_functions():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in sorted(os.listdir(inc)):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_\s\*]*?\b(lpm_[a-z0-9_]+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(native):
+    names = _declared_functions()
+    assert {"lpm_bve_velocity", "lpm_bve_rk4_step", "lpm_bve_ctx_create", "lpm_bve_last_error",
+            "lpm_bve_ensemble_create", "lpm_mesh_build"} <= names
+    lib = ctypes.CDLL(native._name)
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
+    """The product refuses to run if the native library is missing."""
+    from lpmkokkos_gb300 import _build, _lib
+    monkeypatch.setattr(_build, "LIB", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError):
+        _lib.lib()
