@@ -53,6 +53,10 @@ typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = l
 #define LPM_BVE_SKIP_MASKED_TARGETS (1u << 6) /* rk4: no velocity at masked faces (their x, zeta stay fixed) */
 #define LPM_BVE_NO_GRAPH            (1u << 7) /* rk4: launch kernels directly, no captured CUDA graph */
 #define LPM_BVE_NO_SORT             (1u << 8) /* keep the caller's target order (no spatial sort) */
+#define LPM_BVE_MESH_TARGETS        (1u << 9) /* velocity(), distinct targets: they are mesh points (e.g. the
+                                                 vertices of the source mesh), each at least about half a mesh
+                                                 spacing from every source.  Lets FP32C use its 13-op pair
+                                                 formulation; without it arbitrary points get the hi/lo one. */
 
 /* ---- context ---------------------------------------------------------------- */
 typedef struct lpm_bve_ctx lpm_bve_ctx;
@@ -77,6 +81,13 @@ int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx);
  * on the recorded events and returns the summed pair-kernel milliseconds and launch count. */
 int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable);
 int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches, int reset);
+
+/* Launch shape of the FP32C pair kernel: CTA threads x targets per thread, sources staged in
+ * shared memory per step.  lpm_bve_ctx_shapes lists the compiled shapes (returns their number,
+ * fills up to `capacity`); lpm_bve_ctx_set_shape fixes one for plans built afterwards
+ * (threads = 0 restores the default).  The autotuner times these same shapes. */
+int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int capacity);
+int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile);
 
 /* ---- particle sets -------------------------------------------------------------- */
 typedef struct {

@@ -29,6 +29,7 @@ RENORM = 1 << 5
 SKIP_MASKED_TARGETS = 1 << 6
 NO_GRAPH = 1 << 7
 NO_SORT = 1 << 8
+MESH_TARGETS = 1 << 9
 
 SEED_ICOS_TRI = 0
 SEED_CUBED = 1
@@ -80,6 +81,9 @@ def _declare(L):
     L.lpm_bve_plan_invalidate.argtypes = [vp]
     L.lpm_bve_ctx_set_timing.argtypes = [vp, ctypes.c_int]
     L.lpm_bve_ctx_timing.argtypes = [vp, c_dp, ctypes.POINTER(c_i64), ctypes.c_int]
+    ip = ctypes.POINTER(ctypes.c_int)
+    L.lpm_bve_ctx_shapes.argtypes = [ip, ip, ip, ctypes.c_int]
+    L.lpm_bve_ctx_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.lpm_bve_velocity.argtypes = [vp, ctypes.POINTER(Points), ctypes.POINTER(Sources), vp, c_i64, c_i64, vp,
                                    ctypes.c_uint, ctypes.c_double, vp]
     L.lpm_bve_rk4_step.argtypes = [vp, ctypes.POINTER(State), ctypes.c_double, ctypes.c_double, ctypes.c_int,

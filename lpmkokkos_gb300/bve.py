@@ -174,6 +174,19 @@ class Context:
         """Bracket every pair-kernel launch with CUDA events (RK4 steps then launch directly)."""
         L.check(self._lib.lpm_bve_ctx_set_timing(self.handle, int(enable)), self.handle)
 
+    @staticmethod
+    def shapes():
+        """FP32C pair-kernel launch shapes compiled into the library: (threads, K, source tile)."""
+        n = L.lib().lpm_bve_ctx_shapes(None, None, None, 0)
+        t, k, s = (ctypes.c_int * n)(), (ctypes.c_int * n)(), (ctypes.c_int * n)()
+        L.lib().lpm_bve_ctx_shapes(t, k, s, n)
+        return [(t[i], k[i], s[i]) for i in range(n)]
+
+    def set_shape(self, shape=None):
+        """Fix the FP32C launch shape for plans built afterwards (None = default)."""
+        t, k, s = shape if shape else (0, 0, 0)
+        L.check(self._lib.lpm_bve_ctx_set_shape(self.handle, t, k, s), self.handle)
+
     def timing(self, reset: bool = True):
         """(summed pair-kernel milliseconds, launches) since the last reset."""
         ms, n = ctypes.c_double(), L.c_i64()
@@ -315,7 +328,8 @@ class BVESphere:
         prec = flags & L.FP32C
         f = prec | (L.PSI if psi else 0)
         ctx.velocity(self.physVerts, self.physFaces, self.relVortFaces, self.faces_area, self.faces_mask,
-                     u=self.velocityVerts, psi=self.streamFnVerts if psi else None, flags=f, eps=eps)
+                     u=self.velocityVerts, psi=self.streamFnVerts if psi else None, flags=f | L.MESH_TARGETS,
+                     eps=eps)
         ctx.velocity(None, self.physFaces, self.relVortFaces, self.faces_area, self.faces_mask,
                      u=self.velocityFaces, psi=self.streamFnFaces if psi else None, flags=f | L.COLLOCATED, eps=eps)
 

@@ -182,6 +182,7 @@ struct Batch {
   Precision prec = Precision::FP64;
   PairShape shape = kFP64Shape;
   bool rk4 = false;
+  bool precise = false;  // FP32C hi/lo differences (arbitrary distinct targets)
   int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
   DeviceArena mem;
   WorkItem* items = nullptr;
@@ -436,7 +437,7 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
     e1 = B.timer->get();
     LPM_CUDA(cudaEventRecord(e0, s));
   }
-  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.solveDev, B.items, B.nitems, B.counter, B.grid, s));
+  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.solveDev, B.items, B.nitems, B.counter, B.grid, s));
   if (B.timer) {
     LPM_CUDA(cudaEventRecord(e1, s));
     B.timer->pending.emplace_back(e0, e1);
@@ -468,6 +469,7 @@ struct lpm_bve_ctx {
   lpm::Mode velMode = lpm::Mode::Distinct;
   std::unique_ptr<lpm::Batch> rkBatch;
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
+  lpm::PairShape forced{0, 0, 0};          // FP32C launch shape chosen by the caller (threads 0 = none)
 };
 
 struct lpm_bve_ensemble {
@@ -492,14 +494,19 @@ void setDevice(lpm_bve_ctx* ctx) {
 
 Precision precOf(unsigned flags) { return (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64; }
 
-PairShape shapeFor(Precision p) { return p == Precision::FP32C ? kDefaultFP32C : kFP64Shape; }
+PairShape shapeFor(const lpm_bve_ctx* ctx, Precision p) {
+  if (p != Precision::FP32C) return kFP64Shape;
+  return ctx && ctx->forced.threads > 0 ? ctx->forced : kDefaultFP32C;
+}
 
 bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si && a.sc == b.sc; }
 
 // True when a cached single-solve batch was built for the same geometry.
-bool sameGeometry(const Batch* B, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask,
-                  bool skipMasked, bool sort, double eps) {
+bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision prec, const ParticleIO& io,
+                  const uint8_t* mask, bool skipMasked, bool sort, double eps) {
   if (!B || B->solves.size() != 1) return false;
+  const PairShape sh = shapeFor(ctx, prec);
+  if (sh.threads != B->shape.threads || sh.k != B->shape.k || sh.srcTile != B->shape.srcTile) return false;
   const SolvePlan& P = *B->solves[0];
   return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
          sameVec(P.io.bx, io.bx) && P.mask == mask && P.skipMasked == skipMasked && P.sorted == sort &&
@@ -510,7 +517,7 @@ std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, c
                                   const uint8_t* mask, bool skipMasked, bool sort, double eps, cudaStream_t s) {
   auto B = std::make_unique<Batch>();
   B->prec = prec;
-  B->shape = shapeFor(prec);
+  B->shape = shapeFor(ctx, prec);
   B->rk4 = (mode == Mode::RK4);
   B->solves.emplace_back(new SolvePlan());
   buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), s);
@@ -616,6 +623,32 @@ int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable) {
   return LPM_OK;
 }
 
+int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  if (threads == 0) {
+    ctx->forced = PairShape{0, 0, 0};
+    return LPM_OK;
+  }
+  const PairShape sh{threads, targets_per_thread, source_tile};
+  if (!pairShapeSupported(Precision::FP32C, sh)) {
+    ctx->err = "set_shape: launch shape not compiled in";
+    return LPM_ERR_NOT_SUPPORTED;
+  }
+  ctx->forced = sh;
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int capacity) {
+  const int n = pairShapeCount();
+  for (int i = 0; i < n && i < capacity; ++i) {
+    const PairShape sh = pairShapeAt(i);
+    if (threads) threads[i] = sh.threads;
+    if (targets_per_thread) targets_per_thread[i] = sh.k;
+    if (source_tile) source_tile[i] = sh.srcTile;
+  }
+  return n;
+}
+
 int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches, int reset) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
   try {
@@ -683,13 +716,15 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     const Precision prec = precOf(flags);
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = colloc && (flags & LPM_BVE_SKIP_MASKED_TARGETS);
-    if (!sameGeometry(ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps)) {
+    if (!sameGeometry(ctx, ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps)) {
       if (ctx->velBatch) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
       ctx->velBatch.reset();
       ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, s);
       ctx->velBatch->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
     Batch& B = *ctx->velBatch;
+    // Distinct targets are arbitrary points unless the caller says they are mesh points.
+    B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
     bool changed = false;
     bindIO(B, 0, io, 0.0, 0.0, s, changed);
     if (changed) refreshTables(B, s);
@@ -733,7 +768,7 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const Precision prec = precOf(flags);
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
-    if (!sameGeometry(ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps)) {
+    if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps)) {
       if (ctx->rkBatch) LPM_CUDA(cudaDeviceSynchronize());
       ctx->rkBatch.reset();
       ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, s);
@@ -797,7 +832,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     E->batch = std::make_unique<Batch>();
     Batch& B = *E->batch;
     B.prec = precOf(flags);
-    B.shape = shapeFor(B.prec);
+    B.shape = shapeFor(ctx, B.prec);
     B.rk4 = true;
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;

@@ -96,8 +96,11 @@ cudaError_t launchEpilogue(const SolveStage* st, const int4* map, int nblocks, P
                            bool velocity, int stageOut, cudaStream_t s);
 cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bool quirk, bool renorm,
                           cudaStream_t s);
-cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, const SolveDev* solves,
+// precise: FP32C with hi/lo target-source differences (arbitrary distinct targets).
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, const SolveDev* solves,
                        const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s);
+int pairShapeCount();              // FP32C launch shapes compiled in
+PairShape pairShapeAt(int i);
 int stageBlockSize();
 int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi);
 bool pairShapeSupported(Precision prec, const PairShape& shape);

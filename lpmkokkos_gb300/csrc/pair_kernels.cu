@@ -56,11 +56,15 @@ __device__ __forceinline__ float relCoord(float hi, float lo, float chi, float c
   return (hi - chi) + (lo - clo);
 }
 
-constexpr int kSub = 32;  // sources per FP32 sub-block before the compensated add
+constexpr int kSub = 64;  // sources per FP32 sub-block before the compensated add
 
-template <int K, bool PSI, bool CHECKED>
-__device__ __forceinline__ void fp32cTile(const float4* __restrict__ sP, const float* __restrict__ sD, int nsrc,
+// Shared-memory record of one staged source: A = (x, y, z, w) and B = (x_lo, y_lo, z_lo, D).
+// Fast formulation: A.xyz = x_j - c relative to the tile centre c, B.w = D_j (B.xyz unused).
+// Precise formulation: A.xyz = hi(x_j), B.xyz = lo(x_j) (x = hi + lo exactly to ~2^-48).
+template <int K, bool PSI, bool CHECKED, bool PRECISE>
+__device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const float4* __restrict__ sB, int nsrc,
                                           int jbase, const float (&ax)[K], const float (&ay)[K], const float (&az)[K],
+                                          const float (&lx)[K], const float (&ly)[K], const float (&lz)[K],
                                           const float (&C)[K], const int (&self)[K],
                                           float (&hx)[K], float (&hy)[K], float (&hz)[K],
                                           float (&cx)[K], float (&cy)[K], float (&cz)[K],
@@ -72,20 +76,27 @@ __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sP, const f
     for (int k = 0; k < K; ++k) { vx[k] = 0.f; vy[k] = 0.f; vz[k] = 0.f; vp[k] = 0.f; vw[k] = 0.f; }
 #pragma unroll 4
     for (int j = j0; j < j0 + kSub; ++j) {
-      const float4 P = sP[j];
-      const float Dj = sD[j];
+      const float4 A = sA[j];
+      const float4 B = sB[j];
 #pragma unroll
       for (int k = 0; k < K; ++k) {
-        const float dx = P.x - ax[k];
-        const float dy = P.y - ay[k];
-        const float dz = P.z - az[k];
-        const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, Dj + C[k])));
+        float dx, dy, dz;
+        if (PRECISE) {  // hi parts subtract exactly when close; lo parts restore the rest
+          dx = (A.x - ax[k]) + (B.x - lx[k]);
+          dy = (A.y - ay[k]) + (B.y - ly[k]);
+          dz = (A.z - az[k]) + (B.z - lz[k]);
+        } else {
+          dx = A.x - ax[k];
+          dy = A.y - ay[k];
+          dz = A.z - az[k];
+        }
+        const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, B.w + C[k])));
         float r = rcpApprox(q2);
         const float e = fmaf(-q2, r, 1.0f);
         r = fmaf(r, e, r);
-        float s = P.w * r;
+        float s = A.w * r;
         float wl = 0.f, ww = 0.f;
-        if (PSI) { wl = P.w * lg2Approx(q2); ww = P.w; }
+        if (PSI) { wl = A.w * lg2Approx(q2); ww = A.w; }
         if (CHECKED) {
           const bool me = (jbase + j) == self[k];
           s = me ? 0.f : s;
@@ -107,13 +118,18 @@ __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sP, const f
   }
 }
 
-template <int NTH, int K, int ST, bool PSI>
+// PRECISE = false: targets are mesh points (vertices / face centres), which keep about half a
+//   mesh spacing from every other source; coordinates relative to the tile centre keep the
+//   FP32 differences accurate to ~1e-7 * (tile radius / spacing).  13 FMA-pipe ops per pair.
+// PRECISE = true: arbitrary target points (possibly very close to a source); differences
+//   are formed from hi/lo float pairs, accurate to ~1e-7 relative.  19 FMA-pipe ops per pair.
+template <int NTH, int K, int ST, bool PSI, bool PRECISE>
 __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ solves,
                                                  const WorkItem* __restrict__ items, int nitems,
                                                  int* __restrict__ counter) {
   static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
-  __shared__ float4 sP[ST];
-  __shared__ float sD[ST];
+  __shared__ float4 sA[ST];
+  __shared__ float4 sB[ST];
   __shared__ int sItem;
 
   for (;;) {
@@ -129,14 +145,17 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
     const int tcount = min(NTH * K, n - tile0);
 
     // Tile centre: the middle target of the tile (slots are spatially sorted).
-    const int cs = tile0 + (tcount >> 1);
-    const double cxd = S.tx[cs], cyd = S.tx[n + cs], czd = S.tx[2 * n + cs];
-    const float chx = __double2float_rn(cxd), chy = __double2float_rn(cyd), chz = __double2float_rn(czd);
-    const float clx = __double2float_rn(cxd - (double)chx);
-    const float cly = __double2float_rn(cyd - (double)chy);
-    const float clz = __double2float_rn(czd - (double)chz);
+    float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
+    if (!PRECISE) {
+      const int cs = tile0 + (tcount >> 1);
+      const double cxd = S.tx[cs], cyd = S.tx[n + cs], czd = S.tx[2 * n + cs];
+      chx = __double2float_rn(cxd); chy = __double2float_rn(cyd); chz = __double2float_rn(czd);
+      clx = __double2float_rn(cxd - (double)chx);
+      cly = __double2float_rn(cyd - (double)chy);
+      clz = __double2float_rn(czd - (double)chz);
+    }
 
-    float ax[K], ay[K], az[K], C[K];
+    float ax[K], ay[K], az[K], lx[K], ly[K], lz[K], C[K];
     int self[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -144,13 +163,20 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
       if (threadIdx.x + k * NTH < tcount) {
         const double x = S.tx[slot], y = S.tx[n + slot], z = S.tx[2 * n + slot];
         const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
-        ax[k] = relCoord(hx, __double2float_rn(x - (double)hx), chx, clx);
-        ay[k] = relCoord(hy, __double2float_rn(y - (double)hy), chy, cly);
-        az[k] = relCoord(hz, __double2float_rn(z - (double)hz), chz, clz);
+        const float ex = __double2float_rn(x - (double)hx), ey = __double2float_rn(y - (double)hy),
+                    ez = __double2float_rn(z - (double)hz);
+        if (PRECISE) {
+          ax[k] = hx; ay[k] = hy; az[k] = hz; lx[k] = ex; ly[k] = ey; lz[k] = ez;
+        } else {
+          ax[k] = relCoord(hx, ex, chx, clx);
+          ay[k] = relCoord(hy, ey, chy, cly);
+          az[k] = relCoord(hz, ez, chz, clz);
+          lx[k] = ly[k] = lz[k] = 0.f;
+        }
         C[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * S.eps2);
         self[k] = S.self[slot];
       } else {
-        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; C[k] = 1.f; self[k] = -1;
+        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; lx[k] = ly[k] = lz[k] = 0.f; C[k] = 1.f; self[k] = -1;
       }
     }
     float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
@@ -162,26 +188,33 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
     const int2 ts = S.tileSelf[w.tile];
 
     for (int b0 = w.s0; b0 < w.s1; b0 += ST) {
-      // Stage ST sources relative to the tile centre; padding (w = 0, D = 1) adds exactly 0.
+      // Stage ST sources; padding (w = 0, D = 1) adds exactly 0.
       for (int j = threadIdx.x; j < ST; j += NTH) {
         const int s = b0 + j;
         if (s < w.s1) {
           const float4 p0 = S.sp0[s];
           const float4 p1 = S.sp1[s];
-          sP[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
-                              relCoord(p0.z, p1.z, chz, clz), p0.w);
-          sD[j] = p1.w;
-        } else {
-          sP[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-          sD[j] = 1.f;
+          if (PRECISE) {
+            sA[j] = p0;
+            sB[j] = p1;
+          } else {
+            sA[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
+                                relCoord(p0.z, p1.z, chz, clz), p0.w);
+            sB[j] = make_float4(0.f, 0.f, 0.f, p1.w);
+          }
+        } else {  // at the centre (fast) or at the origin (precise): finite q, zero weight
+          sA[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+          sB[j] = make_float4(0.f, 0.f, 0.f, 1.f);
         }
       }
       __syncthreads();
       const bool checked = (ts.x <= b0 + ST - 1) && (ts.y >= b0);
       if (checked)
-        fp32cTile<K, PSI, true>(sP, sD, ST, b0, ax, ay, az, C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+        fp32cTile<K, PSI, true, PRECISE>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
+                                         hp, cp, hw, cw);
       else
-        fp32cTile<K, PSI, false>(sP, sD, ST, b0, ax, ay, az, C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+        fp32cTile<K, PSI, false, PRECISE>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
+                                          hp, cp, hw, cw);
       __syncthreads();
     }
 
@@ -258,22 +291,21 @@ __global__ void __launch_bounds__(kFP64Threads) pairFP64(const SolveDev* __restr
   }
 }
 
-template <int NTH, int K, int ST>
-struct FP32CEntry {
-  static void* fn(bool psi) {
-    return psi ? (void*)pairFP32C<NTH, K, ST, true> : (void*)pairFP32C<NTH, K, ST, false>;
-  }
-};
-
 // Instantiated launch shapes (the autotuner chooses among these).
-struct ShapeFn { int threads, k, srcTile; void* fnPlain; void* fnPsi; };
-const ShapeFn kShapes[] = {
-  {128, 4, 256, (void*)pairFP32C<128, 4, 256, false>, (void*)pairFP32C<128, 4, 256, true>},
-  {128, 2, 256, (void*)pairFP32C<128, 2, 256, false>, (void*)pairFP32C<128, 2, 256, true>},
-  {256, 2, 256, (void*)pairFP32C<256, 2, 256, false>, (void*)pairFP32C<256, 2, 256, true>},
-  {256, 4, 512, (void*)pairFP32C<256, 4, 512, false>, (void*)pairFP32C<256, 4, 512, true>},
-  {128, 8, 256, (void*)pairFP32C<128, 8, 256, false>, (void*)pairFP32C<128, 8, 256, true>},
+struct ShapeFn {
+  int threads, k, srcTile;
+  void* fn[2][2];  // [precise][psi]
 };
+#define LPM_SHAPE(T, K, S)                                                                                 \
+  {T, K, S, {{(void*)pairFP32C<T, K, S, false, false>, (void*)pairFP32C<T, K, S, true, false>},            \
+             {(void*)pairFP32C<T, K, S, false, true>, (void*)pairFP32C<T, K, S, true, true>}}}
+const ShapeFn kShapes[] = {
+  LPM_SHAPE(128, 4, 256),
+  LPM_SHAPE(128, 8, 256),
+  LPM_SHAPE(256, 2, 256),
+  LPM_SHAPE(256, 4, 256),
+};
+#undef LPM_SHAPE
 
 const ShapeFn* findShape(const PairShape& s) {
   for (const auto& e : kShapes)
@@ -281,7 +313,7 @@ const ShapeFn* findShape(const PairShape& s) {
   return nullptr;
 }
 
-void* kernelFor(Precision prec, const PairShape& shape, bool psi, int& threads) {
+void* kernelFor(Precision prec, const PairShape& shape, bool psi, bool precise, int& threads) {
   if (prec == Precision::FP64) {
     threads = kFP64Threads;
     return psi ? (void*)pairFP64<true> : (void*)pairFP64<false>;
@@ -289,10 +321,14 @@ void* kernelFor(Precision prec, const PairShape& shape, bool psi, int& threads) 
   const ShapeFn* e = findShape(shape);
   if (!e) return nullptr;
   threads = e->threads;
-  return psi ? e->fnPsi : e->fnPlain;
+  return e->fn[precise ? 1 : 0][psi ? 1 : 0];
 }
 
 }  // namespace
+
+int pairShapeCount() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
+
+PairShape pairShapeAt(int i) { return PairShape{kShapes[i].threads, kShapes[i].k, kShapes[i].srcTile}; }
 
 bool pairShapeSupported(Precision prec, const PairShape& shape) {
   if (prec == Precision::FP64) return shape.threads == kFP64Threads && shape.k == 1 && shape.srcTile == kFP64Tile;
@@ -306,17 +342,17 @@ int pairNumComponents(Precision prec, bool psi) {
 
 int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {
   int threads = 0;
-  void* fn = kernelFor(prec, shape, psi, threads);
+  void* fn = kernelFor(prec, shape, psi, false, threads);
   if (!fn) return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, 0) != cudaSuccess) return 0;
   return nb;
 }
 
-cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, const SolveDev* solves,
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, const SolveDev* solves,
                        const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s) {
   int threads = 0;
-  void* fn = kernelFor(prec, shape, psi, threads);
+  void* fn = kernelFor(prec, shape, psi, precise, threads);
   if (!fn) return cudaErrorInvalidValue;
   if (nitems <= 0 || grid <= 0) return cudaSuccess;
   void* args[] = {(void*)&solves, (void*)&items, (void*)&nitems, (void*)&counter};
