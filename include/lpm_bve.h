@@ -118,6 +118,23 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
                      double* u, int64_t u_stride_i, int64_t u_stride_c, double* psi,
                      unsigned flags, double eps, lpm_stream_t stream);
 
+/* Same velocity / stream-function sums as lpm_bve_velocity, for callers that cannot
+ * allocate device memory (no counterpart in the reference, which always allocates through
+ * Kokkos).  It needs no context and never calls cudaMalloc, cudaFree or any allocating
+ * library routine: besides the caller's inputs and outputs it uses one file-scope
+ * __device__ scratch array (about 18 MiB) that the CUDA runtime places on every device
+ * that loads this library and keeps until the process exits.
+ *   - Precision: LPM_BVE_FP32C only (other precisions return LPM_ERR_NOT_SUPPORTED).
+ *   - Limits: at most 524,288 source faces (masked or not) per call; larger inputs return
+ *     LPM_ERR_NOT_SUPPORTED with a message on stderr.  Targets are taken in the caller's order.
+ *   - The first call on a device looks up the scratch array's device address; make that
+ *     first call before capturing a stream into a CUDA graph.
+ *   - Every call on a device shares the one scratch array and leaves its contents behind;
+ *     two calls whose kernels can run at the same time (unordered streams) race on it. */
+int lpm_bve_velocity_noalloc(const lpm_points* tgt, const lpm_sources* src,
+                             double* u, int64_t u_stride_i, int64_t u_stride_c, double* psi,
+                             unsigned flags, double eps, lpm_stream_t stream);
+
 /* ---- RK4 stepper ------------------------------------------------------------------ */
 typedef struct {
   int64_t nverts, nfaces;                                          /* BVERK4::nverts / nfaces */

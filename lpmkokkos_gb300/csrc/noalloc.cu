@@ -1,0 +1,336 @@
+// noalloc.cu -- lpm_bve_velocity_noalloc: the FP32-compensated direct sum for callers
+// that cannot allocate device memory.
+//
+// Some hosts own all device memory themselves: a model that hands this library its
+// particle arrays from a pre-sized memory pool and forbids any later cudaMalloc (for
+// example while its time loop runs inside a CUDA graph, or in a deployment that fixes
+// the memory footprint at start-up).  The regular entry points allocate plans and
+// workspace; this one uses only the caller's inputs and outputs plus one file-scope
+// __device__ array, which the CUDA runtime places in device memory when the library is
+// loaded on a device and keeps there until the process exits.
+//
+// Scratch (kScratchBytes, about 18 MiB per device):
+//   packed sources   2 x float4 per unmasked face, up to kMaxFaces faces
+//   source index     one int per face: its position in the packed list, -1 if masked
+//   block counts / offsets for the deterministic mask compaction
+// Limit: at most kMaxFaces faces (sources, masked or not) and kMaxTargets targets.
+//
+// Pipeline on `stream`: count unmasked faces per block, scan the counts (one CTA), pack
+// the sources in face order, then one CTA per target tile sums over every packed source
+// (the arithmetic of the pair kernel in pair_kernels.cu, unsorted targets, no source
+// chunks) and writes u = x_i x V (and psi) straight to the caller's arrays.
+// The scratch is shared by every call on the device and keeps the last call's contents;
+// calls whose kernels overlap on the GPU (different streams, no ordering) race on it.
+
+#include "lpm_bve.h"
+
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdio>
+#include <mutex>
+
+namespace {
+
+constexpr int kMaxFaces = 1 << 19;          // 524,288 faces (icosahedral level 7 has 436,900)
+constexpr int64_t kMaxTargets = INT_MAX / 4;
+constexpr int kCountBlock = 1024;           // faces per compaction block
+constexpr int kMaxBlocks = kMaxFaces / kCountBlock;
+
+// Byte offsets of the scratch regions (each 256-byte aligned).
+constexpr size_t kOffSp0 = 0;
+constexpr size_t kOffSp1 = kOffSp0 + sizeof(float4) * kMaxFaces;
+constexpr size_t kOffIdx = kOffSp1 + sizeof(float4) * kMaxFaces;
+constexpr size_t kOffCnt = kOffIdx + sizeof(int) * kMaxFaces;
+constexpr size_t kOffOfs = kOffCnt + sizeof(int) * kMaxBlocks;
+constexpr size_t kOffLive = kOffOfs + sizeof(int) * kMaxBlocks;
+constexpr size_t kScratchBytes = kOffLive + 256;
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
+
+constexpr int kNth = 128;   // CTA size of the pair kernel
+constexpr int kK = 4;       // targets per thread
+constexpr int kSt = 256;    // sources staged per step
+constexpr int kSub = 32;    // FP32 sub-block before the compensated add
+constexpr double kPi = 3.1415926535897932384626433832795027975;
+
+struct Scratch {
+  float4* sp0;
+  float4* sp1;
+  int* srcIdx;
+  int* blockCount;
+  int* blockOffset;
+  int* nlive;
+};
+
+__host__ __device__ inline Scratch carve(unsigned char* base) {
+  Scratch s;
+  s.sp0 = reinterpret_cast<float4*>(base + kOffSp0);
+  s.sp1 = reinterpret_cast<float4*>(base + kOffSp1);
+  s.srcIdx = reinterpret_cast<int*>(base + kOffIdx);
+  s.blockCount = reinterpret_cast<int*>(base + kOffCnt);
+  s.blockOffset = reinterpret_cast<int*>(base + kOffOfs);
+  s.nlive = reinterpret_cast<int*>(base + kOffLive);
+  return s;
+}
+
+struct Pts {
+  const double* x;
+  int64_t n, si, sc;
+};
+
+__global__ void __launch_bounds__(kCountBlock) countKernel(unsigned char* base, const uint8_t* mask, int n) {
+  const Scratch S = carve(base);
+  const int f = blockIdx.x * kCountBlock + threadIdx.x;
+  const int live = (f < n) && !(mask && mask[f]);
+  const int c = __syncthreads_count(live);
+  if (threadIdx.x == 0) S.blockCount[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(kMaxBlocks) scanKernel(unsigned char* base, int nblocks) {
+  const Scratch S = carve(base);
+  __shared__ int buf[kMaxBlocks];
+  const int t = threadIdx.x;
+  buf[t] = t < nblocks ? S.blockCount[t] : 0;
+  __syncthreads();
+  for (int d = 1; d < kMaxBlocks; d <<= 1) {   // inclusive Hillis-Steele scan
+    const int v = t >= d ? buf[t - d] : 0;
+    __syncthreads();
+    buf[t] += v;
+    __syncthreads();
+  }
+  if (t < nblocks) S.blockOffset[t] = buf[t] - S.blockCount[t];
+  if (t == 0) *S.nlive = nblocks > 0 ? buf[nblocks - 1] : 0;
+}
+
+__global__ void __launch_bounds__(kCountBlock) packKernel(unsigned char* base, Pts src, const double* zeta,
+                                                          const double* area, const uint8_t* mask, int n) {
+  const Scratch S = carve(base);
+  __shared__ int warpSum[kCountBlock / 32];
+  const int f = blockIdx.x * kCountBlock + threadIdx.x;
+  const int live = (f < n) && !(mask && mask[f]);
+  const unsigned ballot = __ballot_sync(0xffffffffu, live);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) warpSum[warp] = __popc(ballot);
+  __syncthreads();
+  int before = 0;
+  for (int w = 0; w < warp; ++w) before += warpSum[w];
+  const int rank = before + __popc(ballot & ((1u << lane) - 1u));
+  if (f >= n) return;
+  if (!live) {
+    S.srcIdx[f] = -1;
+    return;
+  }
+  const int s = S.blockOffset[blockIdx.x] + rank;
+  S.srcIdx[f] = s;
+  const double x[3] = {src.x[f * src.si], src.x[f * src.si + src.sc], src.x[f * src.si + 2 * src.sc]};
+  float hi[3], lo[3];
+  for (int c = 0; c < 3; ++c) {
+    hi[c] = __double2float_rn(x[c]);
+    lo[c] = __double2float_rn(x[c] - (double)hi[c]);
+  }
+  const double circ = -zeta[f] * area[f];
+  S.sp0[s] = make_float4(hi[0], hi[1], hi[2], __double2float_rn(circ * (1.0 / (2.0 * kPi))));
+  S.sp1[s] = make_float4(lo[0], lo[1], lo[2], __double2float_rn(1.0 - (x[0] * x[0] + x[1] * x[1] + x[2] * x[2])));
+}
+
+__device__ __forceinline__ float rcpApprox(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ float lg2Approx(float x) {
+  float r;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ void kahanAdd(float& h, float& c, float v) {
+  const float y = v - c;
+  const float t = h + y;
+  c = (t - h) - y;
+  h = t;
+}
+__device__ __forceinline__ float relCoord(float hi, float lo, float chi, float clo) { return (hi - chi) + (lo - clo); }
+
+// One CTA per tile of kNth*kK targets, all packed sources, epilogue fused.
+template <bool PSI>
+__global__ void __launch_bounds__(kNth) pairKernel(unsigned char* base, Pts tgt, bool colloc, double eps2,
+                                                   double* u, int64_t usi, int64_t usc, double* psi) {
+  const Scratch S = carve(base);
+  __shared__ float4 sP[kSt];
+  __shared__ float sD[kSt];
+  __shared__ int sLo, sHi;
+  const int n = (int)tgt.n;
+  const int ns = *S.nlive;
+  const int tile0 = blockIdx.x * (kNth * kK);
+  const int tcount = min(kNth * kK, n - tile0);
+  const int cs = tile0 + (tcount >> 1);
+  const double cxd = tgt.x[cs * tgt.si], cyd = tgt.x[cs * tgt.si + tgt.sc], czd = tgt.x[cs * tgt.si + 2 * tgt.sc];
+  const float chx = __double2float_rn(cxd), chy = __double2float_rn(cyd), chz = __double2float_rn(czd);
+  const float clx = __double2float_rn(cxd - (double)chx), cly = __double2float_rn(cyd - (double)chy),
+              clz = __double2float_rn(czd - (double)chz);
+  if (threadIdx.x == 0) { sLo = INT_MAX; sHi = -1; }
+  __syncthreads();
+  float ax[kK], ay[kK], az[kK], C[kK];
+  double X[kK][3];
+  int self[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    const int i = tile0 + threadIdx.x + k * kNth;
+    self[k] = -1;
+    if (threadIdx.x + k * kNth < tcount) {
+      for (int c = 0; c < 3; ++c) X[k][c] = tgt.x[(int64_t)i * tgt.si + c * tgt.sc];
+      const float hx = __double2float_rn(X[k][0]), hy = __double2float_rn(X[k][1]), hz = __double2float_rn(X[k][2]);
+      ax[k] = relCoord(hx, __double2float_rn(X[k][0] - (double)hx), chx, clx);
+      ay[k] = relCoord(hy, __double2float_rn(X[k][1] - (double)hy), chy, cly);
+      az[k] = relCoord(hz, __double2float_rn(X[k][2] - (double)hz), chz, clz);
+      C[k] = __double2float_rn((1.0 - (X[k][0] * X[k][0] + X[k][1] * X[k][1] + X[k][2] * X[k][2])) + 2.0 * eps2);
+      if (colloc) {
+        self[k] = S.srcIdx[i];
+        if (self[k] >= 0) { atomicMin(&sLo, self[k]); atomicMax(&sHi, self[k]); }
+      }
+    } else {
+      ax[k] = ay[k] = az[k] = 0.f; C[k] = 1.f;
+      X[k][0] = X[k][1] = X[k][2] = 0.0;
+    }
+  }
+  __syncthreads();
+  const int lo = sLo, hi = sHi;
+  float hx[kK], hy[kK], hz[kK], cx[kK], cy[kK], cz[kK], hp[kK], cp[kK], hw[kK], cw[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
+
+  for (int b0 = 0; b0 < ns; b0 += kSt) {
+    __syncthreads();
+    for (int j = threadIdx.x; j < kSt; j += kNth) {
+      const int s = b0 + j;
+      if (s < ns) {
+        const float4 p0 = S.sp0[s], p1 = S.sp1[s];
+        sP[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
+                            relCoord(p0.z, p1.z, chz, clz), p0.w);
+        sD[j] = p1.w;
+      } else {
+        sP[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        sD[j] = 1.f;
+      }
+    }
+    __syncthreads();
+    const bool checked = lo <= b0 + kSt - 1 && hi >= b0;
+#pragma unroll 1
+    for (int j0 = 0; j0 < kSt; j0 += kSub) {
+      float vx[kK], vy[kK], vz[kK], vp[kK], vw[kK];
+#pragma unroll
+      for (int k = 0; k < kK; ++k) vx[k] = vy[k] = vz[k] = vp[k] = vw[k] = 0.f;
+#pragma unroll 4
+      for (int j = j0; j < j0 + kSub; ++j) {
+        const float4 P = sP[j];
+        const float Dj = sD[j];
+#pragma unroll
+        for (int k = 0; k < kK; ++k) {
+          const float dx = P.x - ax[k], dy = P.y - ay[k], dz = P.z - az[k];
+          const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, Dj + C[k])));
+          float r = rcpApprox(q2);
+          const float e = fmaf(-q2, r, 1.0f);
+          r = fmaf(r, e, r);
+          float s = P.w * r;
+          float wl = 0.f, ww = 0.f;
+          if (PSI) { wl = P.w * lg2Approx(q2); ww = P.w; }
+          if (checked && (b0 + j) == self[k]) { s = 0.f; wl = 0.f; ww = 0.f; }
+          vx[k] = fmaf(s, dx, vx[k]);
+          vy[k] = fmaf(s, dy, vy[k]);
+          vz[k] = fmaf(s, dz, vz[k]);
+          if (PSI) { vp[k] += wl; vw[k] += ww; }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        kahanAdd(hx[k], cx[k], vx[k]); kahanAdd(hy[k], cy[k], vy[k]); kahanAdd(hz[k], cz[k], vz[k]);
+        if (PSI) { kahanAdd(hp[k], cp[k], vp[k]); kahanAdd(hw[k], cw[k], vw[k]); }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kK; ++k) {
+    const int64_t i = tile0 + threadIdx.x + k * kNth;
+    if (threadIdx.x + k * kNth >= tcount) continue;
+    const double V0 = (double)hx[k] - (double)cx[k], V1 = (double)hy[k] - (double)cy[k],
+                 V2 = (double)hz[k] - (double)cz[k];
+    if (u) {
+      u[i * usi] = X[k][1] * V2 - X[k][2] * V1;
+      u[i * usi + usc] = X[k][2] * V0 - X[k][0] * V2;
+      u[i * usi + 2 * usc] = X[k][0] * V1 - X[k][1] * V0;
+    }
+    if (PSI && psi) psi[i] = 0.34657359027997264 * (((double)hp[k] - (double)cp[k]) - ((double)hw[k] - (double)cw[k]));
+  }
+}
+
+// Device address of the scratch array, looked up once per device.
+constexpr int kMaxDevices = 64;
+unsigned char* g_scratchPtr[kMaxDevices];
+cudaError_t g_scratchErr[kMaxDevices];
+std::once_flag g_scratchOnce[kMaxDevices];
+
+}  // namespace
+
+extern "C" int lpm_bve_velocity_noalloc(const lpm_points* tgt, const lpm_sources* src, double* u, int64_t u_stride_i,
+                                        int64_t u_stride_c, double* psi, unsigned flags, double eps,
+                                        lpm_stream_t stream) {
+  if (!src) return LPM_ERR_INVALID_ARGUMENT;
+  const bool colloc = flags & LPM_BVE_COLLOCATED;
+  const bool wantVel = !(flags & LPM_BVE_NO_VELOCITY);
+  const bool wantPsi = flags & LPM_BVE_PSI;
+  if (!(flags & LPM_BVE_FP32C)) {
+    std::fprintf(stderr, "lpm_bve_velocity_noalloc: only the FP32C precision (LPM_BVE_FP32C) is provided\n");
+    return LPM_ERR_NOT_SUPPORTED;
+  }
+  const lpm_points& sp = src->pts;
+  const lpm_points* tp = colloc ? &sp : tgt;
+  if (!tp || sp.n < 0 || tp->n < 0 || !(eps >= 0.0) || (!wantVel && !wantPsi)) return LPM_ERR_INVALID_ARGUMENT;
+  if (sp.n > kMaxFaces || tp->n > kMaxTargets) {
+    std::fprintf(stderr,
+                 "lpm_bve_velocity_noalloc: %lld sources / %lld targets exceed the static scratch limit "
+                 "(%d sources, %lld targets); use lpm_bve_velocity\n",
+                 (long long)sp.n, (long long)tp->n, kMaxFaces, (long long)kMaxTargets);
+    return LPM_ERR_NOT_SUPPORTED;
+  }
+  if ((sp.n > 0 && (!sp.x || !src->zeta || !src->area)) || (tp->n > 0 && !tp->x) ||
+      (wantVel && tp->n > 0 && !u) || (wantPsi && tp->n > 0 && !psi))
+    return LPM_ERR_INVALID_ARGUMENT;
+  if (tp->n == 0) return LPM_OK;
+
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return LPM_ERR_CUDA;
+  // First call on this device: look up the array's device address (do this before any
+  // stream capture; later calls only read the cached pointer).
+  std::call_once(g_scratchOnce[dev], [dev]() {
+    void* p = nullptr;
+    g_scratchErr[dev] = cudaGetSymbolAddress(&p, g_noallocScratch);
+    g_scratchPtr[dev] = static_cast<unsigned char*>(p);
+  });
+  if (g_scratchErr[dev] != cudaSuccess || !g_scratchPtr[dev]) {
+    std::fprintf(stderr, "lpm_bve_velocity_noalloc: cudaGetSymbolAddress failed: %s\n",
+                 cudaGetErrorString(g_scratchErr[dev]));
+    return LPM_ERR_CUDA;
+  }
+  unsigned char* base = g_scratchPtr[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  const int nf = (int)sp.n;
+  const int nblocks = (nf + kCountBlock - 1) / kCountBlock;
+  const Pts S{sp.x, sp.n, sp.stride_i, sp.stride_c};
+  const Pts T{tp->x, tp->n, tp->stride_i, tp->stride_c};
+  if (nblocks > 0) countKernel<<<nblocks, kCountBlock, 0, s>>>(base, src->mask, nf);
+  scanKernel<<<1, kMaxBlocks, 0, s>>>(base, nblocks);   // also sets the live count (0 without faces)
+  if (nblocks > 0) packKernel<<<nblocks, kCountBlock, 0, s>>>(base, S, src->zeta, src->area, src->mask, nf);
+  const int tiles = (int)((tp->n + kNth * kK - 1) / (kNth * kK));
+  double* uo = wantVel ? u : nullptr;
+  if (wantPsi)
+    pairKernel<true><<<tiles, kNth, 0, s>>>(base, T, colloc, eps * eps, uo, u_stride_i, u_stride_c, psi);
+  else
+    pairKernel<false><<<tiles, kNth, 0, s>>>(base, T, colloc, eps * eps, uo, u_stride_i, u_stride_c, nullptr);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    std::fprintf(stderr, "lpm_bve_velocity_noalloc: launch failed: %s\n", cudaGetErrorString(e));
+    return LPM_ERR_CUDA;
+  }
+  return LPM_OK;
+}
