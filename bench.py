@@ -37,8 +37,15 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 SEED_BASE = 20261203
-WORKLOAD = dict(seed_kind=0, level=7, ngauss=3, width=0.1, dt=0.01, omega=2 * math.pi, eps=0.0,
-                ic_seed=SEED_BASE + 1)
+WORKLOAD = dict(seed_kind=0, level=7, ngauss=3, width=0.1, omega=2 * math.pi, eps=0.0, ic_seed=SEED_BASE + 1)
+
+
+def time_step(level: int) -> float:
+    """dt = 0.01 at level 4 (the CPU-runnable configuration), halved per level: the Courant
+    number 2 pi dt / sqrt(4 pi / N_faces) of tests/LpmBVETest.cpp:22 stays at its level-4 value.
+    A fixed dt = 0.01 at level 7 moves stage positions ~2 mesh spacings off the sphere, where
+    the reference's 1 - x.y denominator crosses zero for nearest neighbours."""
+    return 0.01 * 2.0 ** (4 - level)
 OPS_PER_PAIR = 13  # FP32 FMA-pipe lane operations per velocity pair in the FP32C kernel
 
 
@@ -76,7 +83,7 @@ def whole_job_rate(world: int, units_per_rank: int, max_elapsed_ms: float) -> fl
 def workload_desc(level):
     w = dict(WORKLOAD, level=level)
     return (f"icosahedral level {level}, RH54 + {w['ngauss']} Gaussian vortices (seed {w['ic_seed']}, "
-            f"amp U(-2,2), width {w['width']}), eps {w['eps']}, dt {w['dt']}, Omega 2pi")
+            f"amp U(-2,2), width {w['width']}), eps {w['eps']}, dt {time_step(level):g}, Omega 2pi")
 
 
 def mesh_sizes(level):
@@ -151,7 +158,7 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     ctx = bve.Context(local_rank)
     prec = P.FP32C if args.prec == "fp32c" else P.FP64
-    w = dict(WORKLOAD, level=args.level)
+    w = dict(WORKLOAD, level=args.level, dt=time_step(args.level))
     nv, nall, nl = mesh_sizes(args.level)
 
     t0 = time.time()

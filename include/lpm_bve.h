@@ -57,6 +57,9 @@ typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = l
                                                  vertices of the source mesh), each at least about half a mesh
                                                  spacing from every source.  Lets FP32C use its 13-op pair
                                                  formulation; without it arbitrary points get the hi/lo one. */
+#define LPM_BVE_RCP_APPROX          (1u << 10) /* FP32C: use the hardware reciprocal without its Newton step
+                                                  (11 instead of 13 FMA-pipe ops per pair, about one more
+                                                  FP32 rounding per pair) */
 
 /* ---- context ---------------------------------------------------------------- */
 typedef struct lpm_bve_ctx lpm_bve_ctx;
@@ -156,6 +159,14 @@ typedef struct {
  * context (BVERK4::init, src/LpmBVERK4.cpp:5-37). */
 int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, double Omega, int nsteps,
                      unsigned flags, double eps, lpm_stream_t stream);
+
+/* Inspection of the last lpm_bve_rk4_step on this context: copies the increments of RK4 stage
+ * `stage` (0..3: x_k = dt u_k and zeta_k = -2 Omega u_k,z dt of stages 1..4, the vertx1..4 /
+ * facex1..4 and vertvort1..4 / facevort1..4 workspaces of src/LpmBVERK4.hpp:38-63) to HOST
+ * arrays in particle order: vx_inc (nverts x 3, row-major), vzeta_inc (nverts), fx_inc
+ * (nfaces x 3), fzeta_inc (nfaces); any may be NULL.  Synchronises the stream. */
+int lpm_bve_rk4_increments(lpm_bve_ctx* ctx, int stage, double* vx_inc, double* vzeta_inc, double* fx_inc,
+                           double* fzeta_inc, lpm_stream_t stream);
 
 /* ---- host-side mesh and initial conditions ------------------------------------------ */
 #define LPM_SEED_ICOS_TRI 0 /* IcosTriSphereSeed  (src/LpmMeshSeed.hpp:134-152) */

@@ -230,8 +230,10 @@ class BVESphere {
                     faceArea.data(), reinterpret_cast<const uint8_t*>(faceMask.data())};
     lpm_points tv{vertCrds.data(), nverts_, vertCrds.stride(0), vertCrds.stride(1)};
     const bool psi = flags & LPM_BVE_PSI;
+    // Vertices are mesh points: they keep about half a mesh spacing from every source.
     throwIf(lpm_bve_velocity(ctx, &tv, &src, velocityVerts.data(), velocityVerts.stride(0), velocityVerts.stride(1),
-                             psi ? streamFnVerts.data() : nullptr, flags, eps, nullptr), ctx, "vertex solve");
+                             psi ? streamFnVerts.data() : nullptr, flags | LPM_BVE_MESH_TARGETS, eps, nullptr),
+            ctx, "vertex solve");
     throwIf(lpm_bve_velocity(ctx, nullptr, &src, velocityFaces.data(), velocityFaces.stride(0),
                              velocityFaces.stride(1), psi ? streamFnFaces.data() : nullptr,
                              flags | LPM_BVE_COLLOCATED, eps, nullptr), ctx, "face solve");

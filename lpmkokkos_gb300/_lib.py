@@ -30,6 +30,7 @@ SKIP_MASKED_TARGETS = 1 << 6
 NO_GRAPH = 1 << 7
 NO_SORT = 1 << 8
 MESH_TARGETS = 1 << 9
+RCP_APPROX = 1 << 10
 
 SEED_ICOS_TRI = 0
 SEED_CUBED = 1
@@ -86,6 +87,7 @@ def _declare(L):
     L.lpm_bve_ctx_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.lpm_bve_velocity.argtypes = [vp, ctypes.POINTER(Points), ctypes.POINTER(Sources), vp, c_i64, c_i64, vp,
                                    ctypes.c_uint, ctypes.c_double, vp]
+    L.lpm_bve_rk4_increments.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]
     L.lpm_bve_rk4_step.argtypes = [vp, ctypes.POINTER(State), ctypes.c_double, ctypes.c_double, ctypes.c_int,
                                    ctypes.c_uint, ctypes.c_double, vp]
     L.lpm_bve_ensemble_create.argtypes = [vp, ctypes.POINTER(State), ctypes.c_int, ctypes.c_uint, ctypes.c_double,

@@ -219,6 +219,13 @@ class Context:
                                         _stream(stream))
         L.check(rc, self.handle)
 
+    def rk4_increments(self, stage: int, nverts: int, nfaces: int, stream=None):
+        """Stage increments (x_k, zeta_k) of the last RK4 step, host arrays in particle order."""
+        vx = np.zeros((nverts, 3)); vz = np.zeros(nverts); fx = np.zeros((nfaces, 3)); fz = np.zeros(nfaces)
+        L.check(self._lib.lpm_bve_rk4_increments(self.handle, stage, _np_ptr(vx), _np_ptr(vz), _np_ptr(fx),
+                                                 _np_ptr(fz), _stream(stream)), self.handle)
+        return vx, vz, fx, fz
+
     def ensemble(self, states: Sequence[BVEState], flags: int = 0, eps: float = 0.0, stream=None) -> "Ensemble":
         return Ensemble(self, states, flags, eps, stream)
 

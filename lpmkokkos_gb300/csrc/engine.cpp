@@ -182,7 +182,8 @@ struct Batch {
   Precision prec = Precision::FP64;
   PairShape shape = kFP64Shape;
   bool rk4 = false;
-  bool precise = false;  // FP32C hi/lo differences (arbitrary distinct targets)
+  bool precise = false;    // FP32C hi/lo differences (arbitrary distinct targets)
+  bool rcpApprox = false;  // FP32C without the Newton step (LPM_BVE_RCP_APPROX)
   int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
   DeviceArena mem;
   WorkItem* items = nullptr;
@@ -193,7 +194,7 @@ struct Batch {
   int* counter = nullptr;
   // captured RK4 step
   cudaGraphExec_t graph = nullptr;
-  bool graphQuirk = false, graphRenorm = false;
+  bool graphQuirk = false, graphRenorm = false, graphRcp = false;
   ~Batch() {
     if (graph) cudaGraphExecDestroy(graph);
   }
@@ -272,18 +273,34 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
       r.x = std::min(r.x, self[t]);
       r.y = std::max(r.y, self[t]);
     }
+  // Tile centres: the target nearest the middle of each tile that is not a masked face
+  // (masked parents can sit on a leaf and run away; vertices and leaves stay on the sphere).
+  std::vector<int> tileCentre((size_t)P.ntiles);
+  for (int t = 0; t < P.ntiles; ++t) {
+    const int t0 = t * tileSize, cnt = std::min(tileSize, nslots - t0), mid = t0 + cnt / 2;
+    int best = mid;
+    for (int d = 0; d < cnt; ++d) {
+      const int a = mid - d, b = mid + d;
+      auto ok = [&](int q) { return q >= t0 && q < t0 + cnt && (ids[q] < na || !hmask[ids[q] - na]); };
+      if (ok(a)) { best = a; break; }
+      if (ok(b)) { best = b; break; }
+    }
+    tileCentre[t] = best;
+  }
 
   DeviceArena& M = P.mem;
   M.release();
   int* dPerm = M.alloc<int>(nslots);
   int* dSelf = M.alloc<int>(nslots);
   int2* dTileSelf = M.alloc<int2>(P.ntiles);
+  int* dTileCentre = M.alloc<int>(P.ntiles);
   int* dSrcFace = M.alloc<int>(ns);
   int* dSrcSlot = M.alloc<int>(ns);
   double* dTx = M.alloc<double>(3 * (size_t)nslots);
   upload(dPerm, ids, s);
   upload(dSelf, self, s);
   upload(dTileSelf, P.tileSelfHost, s);
+  upload(dTileCentre, tileCentre, s);
   upload(dSrcFace, srcFace, s);
   upload(dSrcSlot, srcSlot, s);
 
@@ -317,6 +334,7 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   D.sd = S.sd;
   D.self = dSelf;
   D.tileSelf = dTileSelf;
+  D.tileCentre = dTileCentre;
   D.nslots = nslots;
   D.ns = ns;
   D.tileSize = tileSize;
@@ -437,7 +455,8 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
     e1 = B.timer->get();
     LPM_CUDA(cudaEventRecord(e0, s));
   }
-  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.solveDev, B.items, B.nitems, B.counter, B.grid, s));
+  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.items, B.nitems, B.counter,
+                      B.grid, s));
   if (B.timer) {
     LPM_CUDA(cudaEventRecord(e1, s));
     B.timer->pending.emplace_back(e0, e1);
@@ -725,6 +744,7 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     Batch& B = *ctx->velBatch;
     // Distinct targets are arbitrary points unless the caller says they are mesh points.
     B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
+    B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
     bool changed = false;
     bindIO(B, 0, io, 0.0, 0.0, s, changed);
     if (changed) refreshTables(B, s);
@@ -780,12 +800,14 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     if (changed) refreshTables(B, s);
     const bool quirk = !(flags & LPM_BVE_RK4_FIX_QUIRK);
     const bool renorm = flags & LPM_BVE_RENORM;
+    const bool rcp = flags & LPM_BVE_RCP_APPROX;
+    B.rcpApprox = rcp;
     if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer) {
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
       B.timer = nullptr;
     } else {
-      if (B.graph && (B.graphQuirk != quirk || B.graphRenorm != renorm)) {
+      if (B.graph && (B.graphQuirk != quirk || B.graphRenorm != renorm || B.graphRcp != rcp)) {
         cudaGraphExecDestroy(B.graph);
         B.graph = nullptr;
       }
@@ -805,8 +827,45 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
         LPM_CUDA(ie);
         B.graphQuirk = quirk;
         B.graphRenorm = renorm;
+        B.graphRcp = rcp;
       }
       for (int k = 0; k < nsteps; ++k) LPM_CUDA(cudaGraphLaunch(B.graph, s));
+    }
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_rk4_increments(lpm_bve_ctx* ctx, int stage, double* vx_inc, double* vzeta_inc, double* fx_inc,
+                           double* fzeta_inc, lpm_stream_t stream) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (stage < 0 || stage > 3) fail(LPM_ERR_INVALID_ARGUMENT, "rk4_increments: stage must be 0..3");
+    if (!ctx->rkBatch) fail(LPM_ERR_STATE, "rk4_increments: no RK4 step has run on this context");
+    const SolvePlan& P = *ctx->rkBatch->solves[0];
+    const int n = P.nslots;
+    std::vector<double> kx(3 * (size_t)n), kz((size_t)n);
+    std::vector<int> perm((size_t)n);
+    LPM_CUDA(cudaMemcpyAsync(kx.data(), P.stage.kx[stage], sizeof(double) * kx.size(), cudaMemcpyDeviceToHost, s));
+    LPM_CUDA(cudaMemcpyAsync(kz.data(), P.stage.kz[stage], sizeof(double) * kz.size(), cudaMemcpyDeviceToHost, s));
+    LPM_CUDA(cudaMemcpyAsync(perm.data(), P.stage.perm, sizeof(int) * perm.size(), cudaMemcpyDeviceToHost, s));
+    LPM_CUDA(cudaStreamSynchronize(s));
+    const int64_t na = P.io.na, nb = P.io.nb;
+    if (vx_inc) std::fill(vx_inc, vx_inc + 3 * na, 0.0);
+    if (vzeta_inc) std::fill(vzeta_inc, vzeta_inc + na, 0.0);
+    if (fx_inc) std::fill(fx_inc, fx_inc + 3 * nb, 0.0);
+    if (fzeta_inc) std::fill(fzeta_inc, fzeta_inc + nb, 0.0);
+    for (int t = 0; t < n; ++t) {
+      const int p = perm[t];
+      double* X = p < na ? vx_inc : fx_inc;
+      double* Z = p < na ? vzeta_inc : fzeta_inc;
+      const int64_t q = p < na ? p : p - na;
+      if (X)
+        for (int c = 0; c < 3; ++c) X[3 * q + c] = kx[(size_t)c * n + t];
+      if (Z) Z[q] = kz[t];
     }
   } catch (const Error& e) {
     return handle(ctx, e);
@@ -834,6 +893,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     B.prec = precOf(flags);
     B.shape = shapeFor(ctx, B.prec);
     B.rk4 = true;
+    B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
     for (int m = 0; m < nsolves; ++m) {

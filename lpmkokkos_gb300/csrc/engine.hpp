@@ -53,7 +53,8 @@ struct SolveDev {
   const float4* sp1;         // [ns] FP32C: (x_lo, y_lo, z_lo, D = 1 - |x|^2)
   const double4_32a* sd;         // [ns] FP64 : (x, y, z, -zeta*A)
   const int* self;           // [nslots] source index of the same particle, -1 if none
-  const int2* tileSelf;      // [ntiles] min/max self index of the tile (-1,-2 if none)
+  const int2* tileSelf;      // [ntiles] min/max self index of the tile (INT_MAX,-1 if none)
+  const int* tileCentre;     // [ntiles] slot of the tile's centre target (a vertex or leaf face)
   double* partial;           // [nchunks][ncomp][nslots]
   int nslots, ns, tileSize, nchunks;
   double eps2;
@@ -97,8 +98,10 @@ cudaError_t launchEpilogue(const SolveStage* st, const int4* map, int nblocks, P
 cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bool quirk, bool renorm,
                           cudaStream_t s);
 // precise: FP32C with hi/lo target-source differences (arbitrary distinct targets).
-cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, const SolveDev* solves,
-                       const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s);
+// rcpApprox: FP32C fast formulation without the Newton step on the reciprocal.
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
+                       const SolveDev* solves, const WorkItem* items, int nitems, int* counter, int grid,
+                       cudaStream_t s);
 int pairShapeCount();              // FP32C launch shapes compiled in
 PairShape pairShapeAt(int i);
 int stageBlockSize();

@@ -164,8 +164,31 @@ __global__ void __launch_bounds__(kNth) pairKernel(unsigned char* base, Pts tgt,
   const int ns = *S.nlive;
   const int tile0 = blockIdx.x * (kNth * kK);
   const int tcount = min(kNth * kK, n - tile0);
-  const int cs = tile0 + (tcount >> 1);
-  const double cxd = tgt.x[cs * tgt.si], cyd = tgt.x[cs * tgt.si + tgt.sc], czd = tgt.x[cs * tgt.si + 2 * tgt.sc];
+  // Centre: the middle target, or (if its position is inf/NaN or far off the sphere, e.g. a
+  // masked parent that coincides with a leaf) the first target near the sphere, or the origin.
+  __shared__ int sCentre;
+  int cs = tile0 + (tcount >> 1);
+  double cxd = tgt.x[cs * tgt.si], cyd = tgt.x[cs * tgt.si + tgt.sc], czd = tgt.x[cs * tgt.si + 2 * tgt.sc];
+  auto sane = [](double x, double y, double z) {  // near the unit sphere (false for NaN)
+    const double r2 = x * x + y * y + z * z;
+    return r2 >= 0.25 && r2 <= 4.0;
+  };
+  if (!sane(cxd, cyd, czd)) {
+    if (threadIdx.x == 0) sCentre = INT_MAX;
+    __syncthreads();
+    for (int t = threadIdx.x; t < tcount; t += kNth) {
+      const int64_t q = (int64_t)(tile0 + t) * tgt.si;
+      if (sane(tgt.x[q], tgt.x[q + tgt.sc], tgt.x[q + 2 * tgt.sc])) atomicMin(&sCentre, t);
+    }
+    __syncthreads();
+    cs = sCentre;
+    if (cs == INT_MAX) {
+      cxd = cyd = czd = 0.0;
+    } else {
+      const int64_t q = (int64_t)(tile0 + cs) * tgt.si;
+      cxd = tgt.x[q]; cyd = tgt.x[q + tgt.sc]; czd = tgt.x[q + 2 * tgt.sc];
+    }
+  }
   const float chx = __double2float_rn(cxd), chy = __double2float_rn(cyd), chz = __double2float_rn(czd);
   const float clx = __double2float_rn(cxd - (double)chx), cly = __double2float_rn(cyd - (double)chy),
               clz = __double2float_rn(czd - (double)chz);

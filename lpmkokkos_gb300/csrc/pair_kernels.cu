@@ -27,6 +27,7 @@
 
 #include "engine.hpp"
 
+#include <climits>
 #include <cstdio>
 
 namespace lpm {
@@ -58,10 +59,36 @@ __device__ __forceinline__ float relCoord(float hi, float lo, float chi, float c
 
 constexpr int kSub = 64;  // sources per FP32 sub-block before the compensated add
 
+// A usable tile centre lies near the unit sphere.  Masked parent faces that (nearly) coincide
+// with a leaf get inf/NaN or huge velocities, as in the reference, and drift arbitrarily far.
+__device__ __forceinline__ bool saneCentre(double x, double y, double z) {
+  const double r2 = x * x + y * y + z * z;
+  return r2 >= 0.25 && r2 <= 4.0;  // false for NaN too
+}
+
+// Centre of a target tile: the plan's centre slot (a vertex or leaf face near the middle of the
+// tile) if its position is sane, else the first sane target of the tile, else the origin.
+// The fallback branch is uniform across the CTA.
+__device__ __forceinline__ void tileCentre(const double* __restrict__ tx, int n, int tile0, int tcount, int nth,
+                                           int cs, int* sCentre, double& cx, double& cy, double& cz) {
+  cx = tx[cs]; cy = tx[n + cs]; cz = tx[2 * n + cs];
+  if (saneCentre(cx, cy, cz)) return;
+  if (threadIdx.x == 0) *sCentre = INT_MAX;
+  __syncthreads();
+  for (int t = threadIdx.x; t < tcount; t += nth) {
+    const int q = tile0 + t;
+    if (saneCentre(tx[q], tx[n + q], tx[2 * n + q])) atomicMin(sCentre, t);
+  }
+  __syncthreads();
+  const int c = *sCentre;
+  if (c == INT_MAX) { cx = cy = cz = 0.0; return; }
+  cx = tx[tile0 + c]; cy = tx[n + tile0 + c]; cz = tx[2 * n + tile0 + c];
+}
+
 // Shared-memory record of one staged source: A = (x, y, z, w) and B = (x_lo, y_lo, z_lo, D).
 // Fast formulation: A.xyz = x_j - c relative to the tile centre c, B.w = D_j (B.xyz unused).
 // Precise formulation: A.xyz = hi(x_j), B.xyz = lo(x_j) (x = hi + lo exactly to ~2^-48).
-template <int K, bool PSI, bool CHECKED, bool PRECISE>
+template <int K, bool PSI, bool CHECKED, bool PRECISE, bool NEWTON>
 __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const float4* __restrict__ sB, int nsrc,
                                           int jbase, const float (&ax)[K], const float (&ay)[K], const float (&az)[K],
                                           const float (&lx)[K], const float (&ly)[K], const float (&lz)[K],
@@ -92,8 +119,10 @@ __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const f
         }
         const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, B.w + C[k])));
         float r = rcpApprox(q2);
-        const float e = fmaf(-q2, r, 1.0f);
-        r = fmaf(r, e, r);
+        if (NEWTON) {  // one Newton step: r (2 - q2 r)
+          const float e = fmaf(-q2, r, 1.0f);
+          r = fmaf(r, e, r);
+        }
         float s = A.w * r;
         float wl = 0.f, ww = 0.f;
         if (PSI) { wl = A.w * lg2Approx(q2); ww = A.w; }
@@ -123,7 +152,9 @@ __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const f
 //   FP32 differences accurate to ~1e-7 * (tile radius / spacing).  13 FMA-pipe ops per pair.
 // PRECISE = true: arbitrary target points (possibly very close to a source); differences
 //   are formed from hi/lo float pairs, accurate to ~1e-7 relative.  19 FMA-pipe ops per pair.
-template <int NTH, int K, int ST, bool PSI, bool PRECISE>
+// NEWTON = false skips the Newton refinement of the hardware reciprocal (11 FMA-pipe ops per
+//   pair in the fast formulation); selected by LPM_BVE_RCP_APPROX.
+template <int NTH, int K, int ST, bool PSI, bool PRECISE, bool NEWTON>
 __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ solves,
                                                  const WorkItem* __restrict__ items, int nitems,
                                                  int* __restrict__ counter) {
@@ -131,6 +162,7 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
   __shared__ float4 sA[ST];
   __shared__ float4 sB[ST];
   __shared__ int sItem;
+  __shared__ int sCentre;
 
   for (;;) {
     if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
@@ -144,11 +176,13 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
     const int tile0 = w.tile * (NTH * K);
     const int tcount = min(NTH * K, n - tile0);
 
-    // Tile centre: the middle target of the tile (slots are spatially sorted).
+    // Tile centre (slots are spatially sorted).  A masked parent that coincides with a leaf
+    // carries inf/NaN or a runaway position (as in the reference); it must never become the
+    // centre, or every target of the tile would lose its precision.
     float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
     if (!PRECISE) {
-      const int cs = tile0 + (tcount >> 1);
-      const double cxd = S.tx[cs], cyd = S.tx[n + cs], czd = S.tx[2 * n + cs];
+      double cxd, cyd, czd;
+      tileCentre(S.tx, n, tile0, tcount, NTH, S.tileCentre[w.tile], &sCentre, cxd, cyd, czd);
       chx = __double2float_rn(cxd); chy = __double2float_rn(cyd); chz = __double2float_rn(czd);
       clx = __double2float_rn(cxd - (double)chx);
       cly = __double2float_rn(cyd - (double)chy);
@@ -210,10 +244,10 @@ __global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ so
       __syncthreads();
       const bool checked = (ts.x <= b0 + ST - 1) && (ts.y >= b0);
       if (checked)
-        fp32cTile<K, PSI, true, PRECISE>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
+        fp32cTile<K, PSI, true, PRECISE, NEWTON>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
                                          hp, cp, hw, cw);
       else
-        fp32cTile<K, PSI, false, PRECISE>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
+        fp32cTile<K, PSI, false, PRECISE, NEWTON>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
                                           hp, cp, hw, cw);
       __syncthreads();
     }
@@ -291,14 +325,16 @@ __global__ void __launch_bounds__(kFP64Threads) pairFP64(const SolveDev* __restr
   }
 }
 
-// Instantiated launch shapes (the autotuner chooses among these).
+// Instantiated launch shapes (the autotuner chooses among these).  Variants per shape:
+// [0] fast, [1] precise (hi/lo), [2] fast without the Newton step; each without / with psi.
 struct ShapeFn {
   int threads, k, srcTile;
-  void* fn[2][2];  // [precise][psi]
+  void* fn[3][2];
 };
-#define LPM_SHAPE(T, K, S)                                                                                 \
-  {T, K, S, {{(void*)pairFP32C<T, K, S, false, false>, (void*)pairFP32C<T, K, S, true, false>},            \
-             {(void*)pairFP32C<T, K, S, false, true>, (void*)pairFP32C<T, K, S, true, true>}}}
+#define LPM_SHAPE(T, K, S)                                                                                        \
+  {T, K, S, {{(void*)pairFP32C<T, K, S, false, false, true>, (void*)pairFP32C<T, K, S, true, false, true>},        \
+             {(void*)pairFP32C<T, K, S, false, true, true>, (void*)pairFP32C<T, K, S, true, true, true>},          \
+             {(void*)pairFP32C<T, K, S, false, false, false>, (void*)pairFP32C<T, K, S, true, false, false>}}}
 const ShapeFn kShapes[] = {
   LPM_SHAPE(128, 4, 256),
   LPM_SHAPE(128, 8, 256),
@@ -313,7 +349,7 @@ const ShapeFn* findShape(const PairShape& s) {
   return nullptr;
 }
 
-void* kernelFor(Precision prec, const PairShape& shape, bool psi, bool precise, int& threads) {
+void* kernelFor(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox, int& threads) {
   if (prec == Precision::FP64) {
     threads = kFP64Threads;
     return psi ? (void*)pairFP64<true> : (void*)pairFP64<false>;
@@ -321,7 +357,8 @@ void* kernelFor(Precision prec, const PairShape& shape, bool psi, bool precise, 
   const ShapeFn* e = findShape(shape);
   if (!e) return nullptr;
   threads = e->threads;
-  return e->fn[precise ? 1 : 0][psi ? 1 : 0];
+  const int variant = precise ? 1 : (rcpApprox ? 2 : 0);
+  return e->fn[variant][psi ? 1 : 0];
 }
 
 }  // namespace
@@ -342,17 +379,18 @@ int pairNumComponents(Precision prec, bool psi) {
 
 int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {
   int threads = 0;
-  void* fn = kernelFor(prec, shape, psi, false, threads);
+  void* fn = kernelFor(prec, shape, psi, false, false, threads);
   if (!fn) return 0;
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, 0) != cudaSuccess) return 0;
   return nb;
 }
 
-cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, const SolveDev* solves,
-                       const WorkItem* items, int nitems, int* counter, int grid, cudaStream_t s) {
+cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
+                       const SolveDev* solves, const WorkItem* items, int nitems, int* counter, int grid,
+                       cudaStream_t s) {
   int threads = 0;
-  void* fn = kernelFor(prec, shape, psi, precise, threads);
+  void* fn = kernelFor(prec, shape, psi, precise, rcpApprox, threads);
   if (!fn) return cudaErrorInvalidValue;
   if (nitems <= 0 || grid <= 0) return cudaSuccess;
   void* args[] = {(void*)&solves, (void*)&items, (void*)&nitems, (void*)&counter};

@@ -93,6 +93,48 @@ def test_fp32c_rk4_tracks_fp64(ctx, seed, level):
         assert _l2rel(zb, za) <= 1e-6, (step, _l2rel(zb, za))
 
 
+def test_fp32c_rk4_level6_stays_finite_and_tracks_fp64(ctx):
+    """Level 6 has masked parents in the middle of target tiles once they turn inf/NaN; the
+    vertices and leaves must stay finite and within 1e-6 of the FP64 trajectory."""
+    a = _sphere(ctx, 0, 6, P.FP64)
+    b = _sphere(ctx, 0, 6, P.FP32C)
+    leaf = torch.from_numpy(a.mesh["fmask"] == 0).cuda()
+    dt = 0.0025  # level-4 Courant number (dt halves per level)
+    for step in range(2):
+        ctx.rk4_step(a.state(), dt, OMEGA, 1, flags=P.FP64)
+        ctx.rk4_step(b.state(), dt, OMEGA, 1, flags=P.FP32C)
+        torch.cuda.synchronize()
+        ub = torch.cat([b.velocityVerts, b.velocityFaces[leaf]])
+        assert torch.isfinite(ub).all() and torch.isfinite(b.physFaces[leaf]).all()
+        ua = torch.cat([a.velocityVerts, a.velocityFaces[leaf]]).cpu().numpy()
+        assert _l2rel(ub.cpu().numpy(), ua) <= 1e-6, step
+
+
+def test_fp32c_rk4_level7_state_stays_accurate(ctx):
+    """Level 7 (the benchmark size): after FP32C steps every vertex and leaf stays on the sphere
+    (|x| = 1 to the RK4 drift) and an FP32C evaluation on that state matches FP64 at 8,192
+    sampled vertices.  Masked parents that run away must not leak into any other target."""
+    b = _sphere(ctx, 0, 7, P.FP32C)
+    leaf = torch.from_numpy(b.mesh["fmask"] == 0).cuda()
+    # dt at the level-4 Courant number.  (With dt = 0.01 the stage positions leave the sphere by
+    # more than the nearest-neighbour spacing allows and the reference's 1 - x.y crosses zero.)
+    ctx.rk4_step(b.state(), 0.00125, OMEGA, 3, flags=P.FP32C)
+    torch.cuda.synchronize()
+    for x in (b.physVerts, b.physFaces[leaf]):
+        r = torch.linalg.norm(x, dim=1)
+        assert torch.isfinite(r).all() and (r - 1).abs().max().item() < 1e-7
+    rng = np.random.default_rng(3)
+    idx = torch.from_numpy(rng.choice(b.physVerts.shape[0], 8192, replace=False)).cuda()
+    tgt = b.physVerts[idx].contiguous()
+    src = (b.physFaces, b.relVortFaces, b.faces_area, b.faces_mask)
+    u64, _ = ctx.velocity(tgt, *src, flags=P.FP64)
+    u32, _ = ctx.velocity(tgt, *src, flags=P.FP32C | P.MESH_TARGETS)
+    torch.cuda.synchronize()
+    assert _l2rel(u32.cpu().numpy(), u64.cpu().numpy()) <= 1e-6
+    # the stored velocity at those vertices is the FP32C evaluation of the same state
+    assert _l2rel(b.velocityVerts[idx].cpu().numpy(), u64.cpu().numpy()) <= 1e-6
+
+
 @pytest.mark.parametrize("prec", [P.FP64, P.FP32C])
 def test_graph_equals_direct(ctx, prec):
     a = _sphere(ctx, 0, 3, prec); b = _sphere(ctx, 0, 3, prec)

@@ -174,3 +174,23 @@ def test_poisson_known_answer(ctx):
         ev = np.abs(pv - fv / 30.0).max()
         ef = np.abs(pf[leaf] - ff[leaf] / 30.0).max()
         assert abs(ev - lv) <= 5e-6 * lv and abs(ef - lf) <= 5e-6 * lf, (level, ev, ef)
+
+
+@pytest.mark.parametrize("flags", [P.FP64, P.FP32C | P.MESH_TARGETS, P.FP32C])
+def test_nan_targets_do_not_contaminate(ctx, flags):
+    """Masked parents that coincide with a leaf carry inf/NaN positions after a step (as in
+    the reference).  A NaN target, even in the middle of a target tile (the FP32C tile centre),
+    must leave every other target's result finite and unchanged to the FP32C tolerance."""
+    m, zf = _problem(0, 4)
+    x = m["vx"].copy()
+    bad = np.array([0, 255, 256, 511, 768, 1024 + 256, 2000])   # tile middles for 512-target tiles
+    fx = _dev(m["fx"]); z = _dev(zf); a = _dev(m["farea"]); mk = torch.from_numpy(m["fmask"]).cuda()
+    ref, _ = ctx.velocity(_dev(x), fx, z, a, mk, flags=flags | P.NO_SORT)
+    x[bad] = np.nan
+    got, _ = ctx.velocity(_dev(x), fx, z, a, mk, flags=flags | P.NO_SORT)
+    torch.cuda.synchronize()
+    keep = np.ones(len(x), bool); keep[bad] = False
+    g, r = got.cpu().numpy()[keep], ref.cpu().numpy()[keep]
+    assert np.isfinite(g).all()
+    tol = FP64_TOL if flags == P.FP64 else FP32C_TOL
+    assert _l2rel(g, r) <= tol

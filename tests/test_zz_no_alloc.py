@@ -109,3 +109,19 @@ def test_noalloc_rejects_oversized_and_fp64():
     rc = _fn()(ctypes.byref(_pts(prob["vx"])), ctypes.byref(src), u.data_ptr(), u.stride(0), u.stride(1), None,
                P.FP64, 0.0, None)
     assert rc == L.LPM_ERR_NOT_SUPPORTED
+
+
+def test_noalloc_nan_target_at_tile_middle():
+    """A target with an inf/NaN position (a masked parent that coincides with a leaf) in the
+    middle of a target tile leaves the other targets of the tile finite."""
+    torch.cuda.set_device(0)
+    prob = _problem(0, 4, 5)
+    vx = prob["vx"].clone()
+    ref, _ = _noalloc(prob, colloc=False, psi=False)
+    vx[256] = float("nan")
+    prob2 = dict(prob, vx=vx)
+    got, _ = _noalloc(prob2, colloc=False, psi=False)
+    torch.cuda.synchronize()
+    keep = torch.ones(vx.shape[0], dtype=torch.bool, device="cuda"); keep[256] = False
+    assert torch.isfinite(got[keep]).all()
+    assert _l2(got[keep], ref[keep]) <= FP32C_TOL
