@@ -61,6 +61,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
+    ap.add_argument("--config", choices=["c2", "c3", "c5"], default="c2",
+                    help="c2: single solve icos L7 (default, the headline); c3: 64-solve uneven ensemble; "
+                         "c5: icos L8, eps 0.01, 8 vortices, then the stream function at all targets")
+    ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     return ap.parse_args()
 
 
@@ -156,7 +160,7 @@ def run_ours(args, rank, world, local_rank):
     P.build()
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    ctx = bve.Context(local_rank)
+    ctx = bve.Context(local_rank, autotune=args.autotune)
     prec = P.FP32C if args.prec == "fp32c" else P.FP64
     w = dict(WORKLOAD, level=args.level, dt=time_step(args.level))
     nv, nall, nl = mesh_sizes(args.level)
@@ -318,7 +322,7 @@ def run_ours(args, rank, world, local_rank):
     ctx.close()
 
 
-def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step):
+def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step, eps=0.0):
     """Plain FP64 GPU path on 8192 sampled vertex targets; FP32C error on the same targets.
     (Vertices: a face centre given as a distinct target would coincide with its own source.)"""
     rng = np.random.default_rng(5)
@@ -328,12 +332,12 @@ def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step):
     tgt = pts[idx].contiguous()
     src = (sphere.physFaces, sphere.relVortFaces, sphere.faces_area, sphere.faces_mask)
     res = {}
-    for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C)):
-        ctx.velocity(tgt, *src, flags=flags)  # plan
+    for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C | P.MESH_TARGETS)):
+        ctx.velocity(tgt, *src, flags=flags, eps=eps)  # plan
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
         e0.record()
-        u, _ = ctx.velocity(tgt, *src, flags=flags)
+        u, _ = ctx.velocity(tgt, *src, flags=flags, eps=eps)
         e1.record()
         torch.cuda.synchronize()
         res[name] = (u.cpu().numpy(), e0.elapsed_time(e1))
@@ -379,6 +383,155 @@ def cpu_baseline(st, sphere, w, args, pairs_done):
             "pairs_per_s": rate,
             "sample": f"FP64 velocity at {n} random targets from all {ns} leaf sources, {t:.1f} s, "
                       f"extrapolated to one RK4 step (4 evaluations of {pairs_done} pairs)"}
+
+
+# ------------------------------------------------------------------------------------------
+# further configurations (not the default line)
+# ------------------------------------------------------------------------------------------
+def courant_dt(seed_kind: int, level: int) -> float:
+    """dt at the Courant number 2 pi dt / sqrt(4 pi / N_faces) of icosahedral level 4, dt = 0.01."""
+    nf = (20 * (4 ** (level + 1) - 1) // 3) if seed_kind == 0 else 2 * (4 ** (level + 1) - 1)
+    nf4 = 20 * (4 ** 5 - 1) // 3
+    return 0.01 * math.sqrt(nf4 / nf)
+
+
+def _timed_region(torch, stream, fn, nsteps, flush):
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(nsteps):
+        flush.zero_()
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def run_ensemble(args, rank, world, local_rank):
+    """Config 3: 64 independent solves, levels drawn uniformly from icosahedral and cubed-sphere
+    levels 4-7, RH54 + 3 seeded Gaussian vortices each, FP32C, one persistent pair launch per RK4
+    evaluation for all solves, graph-captured steps."""
+    import numpy as np
+    import torch
+
+    import lpmkokkos_gb300 as P
+    from lpmkokkos_gb300 import bve
+    P.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = bve.Context(local_rank, autotune=args.autotune)
+    rng = np.random.default_rng(SEED_BASE + 3)
+    menu = [(0, 4), (0, 5), (0, 6), (0, 7), (1, 4), (1, 5), (1, 6), (1, 7)]
+    picks = [menu[i] for i in rng.integers(0, len(menu), size=64)]
+    meshes, spheres = {}, []
+    t0 = time.time()
+    for m, (sk, lv) in enumerate(picks):
+        if (sk, lv) not in meshes:
+            meshes[(sk, lv)] = bve.build_mesh(sk, lv)
+        s = bve.BVESphere(sk, lv, device=dev, mesh=meshes[(sk, lv)])
+        s.init_vorticity(bve.rh54_gaussians(SEED_BASE + 3 + 1000 * m, 3), ctx, flags=P.FP32C)
+        spheres.append(s)
+    torch.cuda.synchronize()
+    t_init = time.time() - t0
+    dts = [courant_dt(sk, lv) for sk, lv in picks]
+    oms = [2 * math.pi] * len(picks)
+    ens = ctx.ensemble([s.state() for s in spheres], flags=P.FP32C)
+    info = ens.info()
+    ens.step(dts, oms, max(1, args.warmup))
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    el = max_over_ranks(_timed_region(torch, stream, lambda: ens.step(dts, oms, 1), args.steps, flush), world, dev)
+    steps_per_s = whole_job_rate(world, args.steps, el)
+    alg = 0
+    for sk, lv in picks:
+        nv = 2 + (10 if sk == 0 else 6) * 4 ** lv
+        nl = (20 if sk == 0 else 6) * 4 ** lv
+        alg += (nv + nl) * nl
+    finite = all(bool(torch.isfinite(s.velocityVerts).all()) for s in spheres)
+    out = {
+        "metric": "ensemble RK4 steps/s", "value": steps_per_s, "unit": "steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": el / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32c",
+        "data": "synthetic (seeded RH54 + Gaussian vortices, 64 generated meshes)",
+        "config": {"workload": "64 solves, levels uniform over icosahedral 4-7 and cubed sphere 4-7 "
+                               f"(seed {SEED_BASE + 3}), dt at the level-4 Courant number, FP32C",
+                   "levels": {f"{'icos' if k[0] == 0 else 'cube'}{k[1]}": picks.count(k) for k in menu},
+                   "work_items": info["nitems"], "grid": info["grid"], "device_bytes": info["device_bytes"],
+                   "autotune": bool(args.autotune)},
+        "pair_interactions_per_s": world * 4 * alg * args.steps / (el * 1e-3),
+        "computed_pairs_per_s": world * 4 * info["pairs_per_eval"] * args.steps / (el * 1e-3),
+        "gpu_launches": 13 * args.steps, "init_s": t_init, "all_vertex_velocities_finite": finite,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ens.close()
+    ctx.close()
+
+
+def run_large(args, rank, world, local_rank):
+    """Config 5: icosahedral level 8 (655,362 vertices, 1,747,620 faces, 1,310,720 sources), RH54 + 8
+    Gaussian vortices, eps = 0.01, RK4 steps, then the stream function at all targets."""
+    import numpy as np
+    import torch
+
+    import lpmkokkos_gb300 as P
+    from lpmkokkos_gb300 import bve
+    P.build()
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    ctx = bve.Context(local_rank, autotune=args.autotune)
+    level, eps = 8, 0.01
+    dt = time_step(level)
+    nv, nall, nl = mesh_sizes(level)
+    t0 = time.time()
+    s = bve.BVESphere(0, level, device=dev)
+    s.init_vorticity(bve.rh54_gaussians(SEED_BASE + 5, 8), ctx, flags=P.FP32C, eps=eps)
+    torch.cuda.synchronize()
+    t_init = time.time() - t0
+    st = s.state()
+    ctx.rk4_step(st, dt, 2 * math.pi, max(1, args.warmup), flags=P.FP32C, eps=eps)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    ctx.set_timing(True); ctx.timing()
+    el = _timed_region(torch, stream, lambda: ctx.rk4_step(st, dt, 2 * math.pi, 1, flags=P.FP32C, eps=eps),
+                       args.steps, flush)
+    pair_ms, pair_n = ctx.timing(); ctx.set_timing(False)
+    el = max_over_ranks(el, world, dev)
+    # stream function (and velocity) at every vertex and face
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    s.solve(ctx, flags=P.FP32C, eps=eps, psi=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    psi_ms = e0.elapsed_time(e1)
+    r, ms = __import__("ctypes").c_double(), __import__("ctypes").c_double()
+    P._lib.check(P.lib().lpm_probe_fp32_fma(local_rank, 200000, __import__("ctypes").byref(r),
+                                            __import__("ctypes").byref(ms)))
+    pairs_alg = (nv + nl) * nl
+    achieved = pairs_alg / (pair_ms / pair_n * 1e-3) / 1e9
+    peak = r.value / OPS_PER_PAIR / 1e9
+    fp64 = fp64_sample(ctx, s, dict(WORKLOAD, level=level, dt=dt), P, torch, np, (nv + nall) * nl,
+                       el / args.steps, eps=eps)
+    out = {
+        "metric": "pair-interactions/s", "value": world * 4 * pairs_alg * args.steps / (el * 1e-3),
+        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": el / args.steps, "rk4_steps_per_s": whole_job_rate(world, args.steps, el),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32c",
+        "data": "synthetic (seeded RH54 + 8 Gaussian vortices on a generated icosahedral mesh)",
+        "config": {"workload": f"icosahedral level 8, RH54 + 8 Gaussian vortices (seed {SEED_BASE + 5}), "
+                               f"eps {eps}, dt {dt:g}, Omega 2pi; stream function at all targets after the steps",
+                   "targets": nv + nall, "sources": nl, "autotune": bool(args.autotune)},
+        "psi_and_velocity_all_targets_ms": psi_ms,
+        "roofline": {"bound": "fp32_fma_pipe", "kernel": "pairFP32C", "achieved": achieved, "peak": peak,
+                     "unit": "Gpair/s", "frac": achieved / peak, "pair_launch_ms_avg": pair_ms / pair_n,
+                     "peak_source": "FP32 FMA-pipe probe / 13 lane-ops per pair", "traffic": None},
+        "fp64_gpu": fp64, "init_s": t_init,
+    }
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    ctx.close()
 
 
 # ------------------------------------------------------------------------------------------
@@ -446,7 +599,7 @@ def main():
             torch.cuda.set_device(local_rank)
         dist.init_process_group(backend=backend)
     try:
-        run_ours(args, rank, world, local_rank)
+        {"c2": run_ours, "c3": run_ensemble, "c5": run_large}[args.config](args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

@@ -86,11 +86,12 @@ int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable);
 int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches, int reset);
 
 /* Launch shape of the FP32C pair kernel: CTA threads x targets per thread, sources staged in
- * shared memory per step.  lpm_bve_ctx_shapes lists the compiled shapes (returns their number,
+ * shared memory per step, and the resident CTAs per SM its register budget is sized for
+ * (1 = compiler's choice).  lpm_bve_ctx_shapes lists the compiled shapes (returns their number,
  * fills up to `capacity`); lpm_bve_ctx_set_shape fixes one for plans built afterwards
  * (threads = 0 restores the default).  The autotuner times these same shapes. */
-int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int capacity);
-int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile);
+int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int* min_blocks, int capacity);
+int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile, int min_blocks);
 
 /* ---- particle sets -------------------------------------------------------------- */
 typedef struct {

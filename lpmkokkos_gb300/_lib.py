@@ -83,8 +83,8 @@ def _declare(L):
     L.lpm_bve_ctx_set_timing.argtypes = [vp, ctypes.c_int]
     L.lpm_bve_ctx_timing.argtypes = [vp, c_dp, ctypes.POINTER(c_i64), ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
-    L.lpm_bve_ctx_shapes.argtypes = [ip, ip, ip, ctypes.c_int]
-    L.lpm_bve_ctx_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    L.lpm_bve_ctx_shapes.argtypes = [ip, ip, ip, ip, ctypes.c_int]
+    L.lpm_bve_ctx_set_shape.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
     L.lpm_bve_velocity.argtypes = [vp, ctypes.POINTER(Points), ctypes.POINTER(Sources), vp, c_i64, c_i64, vp,
                                    ctypes.c_uint, ctypes.c_double, vp]
     L.lpm_bve_rk4_increments.argtypes = [vp, ctypes.c_int, vp, vp, vp, vp, vp]

@@ -176,16 +176,17 @@ class Context:
 
     @staticmethod
     def shapes():
-        """FP32C pair-kernel launch shapes compiled into the library: (threads, K, source tile)."""
-        n = L.lib().lpm_bve_ctx_shapes(None, None, None, 0)
-        t, k, s = (ctypes.c_int * n)(), (ctypes.c_int * n)(), (ctypes.c_int * n)()
-        L.lib().lpm_bve_ctx_shapes(t, k, s, n)
-        return [(t[i], k[i], s[i]) for i in range(n)]
+        """FP32C pair-kernel launch shapes compiled into the library: (threads, K, source tile, min blocks)."""
+        n = L.lib().lpm_bve_ctx_shapes(None, None, None, None, 0)
+        t, k, s, b = [(ctypes.c_int * n)() for _ in range(4)]
+        L.lib().lpm_bve_ctx_shapes(t, k, s, b, n)
+        return [(t[i], k[i], s[i], b[i]) for i in range(n)]
 
     def set_shape(self, shape=None):
-        """Fix the FP32C launch shape for plans built afterwards (None = default)."""
-        t, k, s = shape if shape else (0, 0, 0)
-        L.check(self._lib.lpm_bve_ctx_set_shape(self.handle, t, k, s), self.handle)
+        """Fix the FP32C launch shape (threads, K, source tile, min blocks) for plans built
+        afterwards (None = default)."""
+        t, k, s, b = shape if shape else (0, 0, 0, 0)
+        L.check(self._lib.lpm_bve_ctx_set_shape(self.handle, t, k, s, b), self.handle)
 
     def timing(self, reset: bool = True):
         """(summed pair-kernel milliseconds, launches) since the last reset."""
@@ -288,8 +289,9 @@ class BVESphere:
     streamFn*, velocity*, faces area and mask, and the Lagrangian copies of the coordinates.
     """
 
-    def __init__(self, seed: int, level: int, omega: float = 2 * PI, layout: str = "left", device="cuda"):
-        m = build_mesh(seed, level)
+    def __init__(self, seed: int, level: int, omega: float = 2 * PI, layout: str = "left", device="cuda",
+                 mesh: Optional[dict] = None):
+        m = mesh if mesh is not None else build_mesh(seed, level)
         self.seed, self.level, self.layout, self.device = seed, level, layout, torch.device(device)
         self.mesh = m
         self.Omega = omega

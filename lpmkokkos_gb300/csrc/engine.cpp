@@ -13,6 +13,8 @@
 #include "engine.hpp"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <climits>
 #include <cmath>
 #include <cstdarg>
@@ -129,8 +131,8 @@ enum class Mode { Distinct = 0, Collocated = 1, RK4 = 2 };
 
 // Launch shape used when the autotuner is off (measured best on GB300 among the
 // instantiated shapes; the autotuner may choose another one per problem size).
-constexpr PairShape kDefaultFP32C{128, 4, 256};
-constexpr PairShape kFP64Shape{128, 1, 128};
+constexpr PairShape kDefaultFP32C{128, 4, 256, 1};
+constexpr PairShape kFP64Shape{128, 1, 128, 1};
 
 struct SolvePlan {
   Mode mode = Mode::Distinct;
@@ -185,6 +187,7 @@ struct Batch {
   bool precise = false;    // FP32C hi/lo differences (arbitrary distinct targets)
   bool rcpApprox = false;  // FP32C without the Newton step (LPM_BVE_RCP_APPROX)
   int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
+  std::vector<double> itemPairs;  // target-source pairs of each work item (host, launch order)
   DeviceArena mem;
   WorkItem* items = nullptr;
   SolveDev* solveDev = nullptr;
@@ -204,20 +207,22 @@ struct DeviceInfo {
   int device = 0, sms = 0;
 };
 
-// Builds the per-solve index structures (host) and its device buffers.
-void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
-                bool sort, double eps, int tileSize, cudaStream_t s) {
-  P.mode = mode;
-  P.prec = prec;
-  P.io = io;
-  P.mask = mask;
-  P.skipMasked = skipMasked;
-  P.sorted = sort;
-  P.eps2 = eps * eps;
-  P.tileSize = tileSize;
-  const int64_t na = io.na, nb = io.nb;
+// Shape-independent part of a plan, computed on the host: target slot order, compacted
+// source list, and the maps between them.
+struct HostPlan {
+  int64_t na = 0, nb = 0;
+  std::vector<uint8_t> hmask;
+  std::vector<int> ids, srcFace, self, srcSlot;
+};
 
-  std::vector<uint8_t> hmask((size_t)nb, 0);
+HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
+                     cudaStream_t s) {
+  HostPlan H;
+  const int64_t na = io.na, nb = io.nb;
+  H.na = na;
+  H.nb = nb;
+  std::vector<uint8_t>& hmask = H.hmask;
+  hmask.assign((size_t)nb, 0);
   if (mask && nb > 0) {
     LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)nb, cudaMemcpyDeviceToHost, s));
     LPM_CUDA(cudaStreamSynchronize(s));
@@ -262,6 +267,31 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
     }
   std::vector<int> srcSlot((size_t)ns, -1);
   for (int i = 0; i < ns; ++i) srcSlot[i] = slotOf[srcFace[i]];
+  H.ids = std::move(ids);
+  H.srcFace = std::move(srcFace);
+  H.self = std::move(self);
+  H.srcSlot = std::move(srcSlot);
+  return H;
+}
+
+// Builds the per-solve device buffers for target tiles of `tileSize` from a host plan.
+void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
+                bool sort, double eps, int tileSize, const HostPlan& H, cudaStream_t s) {
+  P.mode = mode;
+  P.prec = prec;
+  P.io = io;
+  P.mask = mask;
+  P.skipMasked = skipMasked;
+  P.sorted = sort;
+  P.eps2 = eps * eps;
+  P.tileSize = tileSize;
+  const int64_t na = H.na;
+  const std::vector<uint8_t>& hmask = H.hmask;
+  const std::vector<int>& ids = H.ids;
+  const std::vector<int>& srcFace = H.srcFace;
+  const std::vector<int>& self = H.self;
+  const std::vector<int>& srcSlot = H.srcSlot;
+  const int nslots = (int)ids.size(), ns = (int)srcFace.size();
 
   P.nslots = nslots;
   P.ns = ns;
@@ -394,6 +424,12 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   }
   B.nitems = (int)items.size();
   B.grid = std::min(B.nitems, slots);
+  B.itemPairs.resize(items.size());
+  for (size_t i = 0; i < items.size(); ++i) {
+    const SolvePlan& P = *B.solves[items[i].solve];
+    const int t0 = items[i].tile * B.shape.tileSize();
+    B.itemPairs[i] = (double)std::min(B.shape.tileSize(), P.nslots - t0) * (items[i].s1 - items[i].s0);
+  }
 
   const int bs = stageBlockSize();
   std::vector<int4> prepMap, slotMap;
@@ -488,7 +524,8 @@ struct lpm_bve_ctx {
   lpm::Mode velMode = lpm::Mode::Distinct;
   std::unique_ptr<lpm::Batch> rkBatch;
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
-  lpm::PairShape forced{0, 0, 0};          // FP32C launch shape chosen by the caller (threads 0 = none)
+  lpm::PairShape forced{0, 0, 0, 0};       // FP32C launch shape chosen by the caller (threads 0 = none)
+  std::map<std::array<int, 5>, lpm::PairShape> tuned;  // autotuner results per size bucket
 };
 
 struct lpm_bve_ensemble {
@@ -524,28 +561,97 @@ bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si &
 bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision prec, const ParticleIO& io,
                   const uint8_t* mask, bool skipMasked, bool sort, double eps) {
   if (!B || B->solves.size() != 1) return false;
-  const PairShape sh = shapeFor(ctx, prec);
-  if (sh.threads != B->shape.threads || sh.k != B->shape.k || sh.srcTile != B->shape.srcTile) return false;
+  if (!(shapeFor(ctx, prec) == B->shape)) return false;
   const SolvePlan& P = *B->solves[0];
   return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
          sameVec(P.io.bx, io.bx) && P.mask == mask && P.skipMasked == skipMasked && P.sorted == sort &&
          P.eps2 == eps * eps;
 }
 
+// Times every compiled FP32C launch shape on this problem (prep + a bounded number of pair
+// work items; nothing the caller owns is written) and caches the fastest per size bucket.
+PairShape autotune(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask,
+                   bool skipMasked, bool sort, double eps, bool precise, const HostPlan& H, cudaStream_t s);
+
 std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io,
-                                  const uint8_t* mask, bool skipMasked, bool sort, double eps, cudaStream_t s) {
+                                  const uint8_t* mask, bool skipMasked, bool sort, double eps, bool precise,
+                                  cudaStream_t s) {
+  const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s);
   auto B = std::make_unique<Batch>();
   B->prec = prec;
   B->shape = shapeFor(ctx, prec);
+  if (prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0)
+    B->shape = autotune(ctx, mode, prec, io, mask, skipMasked, sort, eps, precise, H, s);
   B->rk4 = (mode == Mode::RK4);
+  B->precise = precise;
   B->solves.emplace_back(new SolvePlan());
-  buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), s);
+  buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), H, s);
   finalizeBatch(*B, ctx->dev, s);
   if (ctx->verbose)
     std::fprintf(stderr, "[lpm_bve] plan: mode=%d prec=%d slots=%d sources=%d tiles=%d chunks=%d items=%d grid=%d\n",
                  (int)mode, (int)prec, B->solves[0]->nslots, B->solves[0]->ns, B->solves[0]->ntiles,
                  B->solves[0]->nchunks, B->nitems, B->grid);
   return B;
+}
+
+int log2Bucket(int64_t n) {
+  int b = 0;
+  while ((int64_t(1) << b) < n && b < 62) ++b;
+  return b;
+}
+
+PairShape autotune(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask,
+                   bool skipMasked, bool sort, double eps, bool precise, const HostPlan& H, cudaStream_t s) {
+  const std::array<int, 5> key{(int)mode, (int)prec, precise ? 1 : 0, log2Bucket((int64_t)H.ids.size()),
+                               log2Bucket((int64_t)H.srcFace.size())};
+  auto it = ctx->tuned.find(key);
+  if (it != ctx->tuned.end()) return it->second;
+  PairShape best = kDefaultFP32C;
+  double bestRate = -1.0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  LPM_CUDA(cudaEventCreate(&e0));
+  LPM_CUDA(cudaEventCreate(&e1));
+  try {
+    for (int i = 0; i < pairShapeCount(); ++i) {
+      const PairShape sh = pairShapeAt(i);
+      Batch T;
+      T.prec = prec;
+      T.shape = sh;
+      T.precise = precise;
+      T.solves.emplace_back(new SolvePlan());
+      buildSolve(*T.solves[0], mode, prec, io, mask, skipMasked, sort, eps, sh.tileSize(), H, s);
+      finalizeBatch(T, ctx->dev, s);
+      // A bounded trial: a few waves of work items are enough to rank shapes.
+      const int ntrial = std::min(T.nitems, std::max(1, 4 * T.grid));
+      double pairs = 0.0;
+      for (int k = 0; k < ntrial; ++k) pairs += T.itemPairs[k];
+      float ms = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {
+        LPM_CUDA(launchPrep(T.stageDev, T.prepMap, T.nPrepBlocks, 0, prec, T.counter, s));
+        LPM_CUDA(cudaEventRecord(e0, s));
+        LPM_CUDA(launchPair(prec, sh, false, precise, false, T.solveDev, T.items, ntrial, T.counter, T.grid, s));
+        LPM_CUDA(cudaEventRecord(e1, s));
+        LPM_CUDA(cudaEventSynchronize(e1));
+        LPM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      }
+      const double rate = pairs / std::max(1e-6, (double)ms);
+      if (ctx->verbose)
+        std::fprintf(stderr, "[lpm_bve] autotune: shape %dx%d st=%d minb=%d: %.3f ms for %.3e pairs (%.3e pairs/s)\n",
+                     sh.threads, sh.k, sh.srcTile, sh.minBlocks, ms, pairs, rate * 1e3);
+      if (rate > bestRate) {
+        bestRate = rate;
+        best = sh;
+      }
+    }
+  } catch (...) {
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    throw;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx->tuned[key] = best;
+  return best;
 }
 
 // Updates the caller-facing pointers and scalars of a cached plan; re-uploads if changed.
@@ -642,13 +748,13 @@ int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable) {
   return LPM_OK;
 }
 
-int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile) {
+int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread, int source_tile, int min_blocks) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
   if (threads == 0) {
-    ctx->forced = PairShape{0, 0, 0};
+    ctx->forced = PairShape{0, 0, 0, 0};
     return LPM_OK;
   }
-  const PairShape sh{threads, targets_per_thread, source_tile};
+  const PairShape sh{threads, targets_per_thread, source_tile, min_blocks};
   if (!pairShapeSupported(Precision::FP32C, sh)) {
     ctx->err = "set_shape: launch shape not compiled in";
     return LPM_ERR_NOT_SUPPORTED;
@@ -657,13 +763,14 @@ int lpm_bve_ctx_set_shape(lpm_bve_ctx* ctx, int threads, int targets_per_thread,
   return LPM_OK;
 }
 
-int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int capacity) {
+int lpm_bve_ctx_shapes(int* threads, int* targets_per_thread, int* source_tile, int* min_blocks, int capacity) {
   const int n = pairShapeCount();
   for (int i = 0; i < n && i < capacity; ++i) {
     const PairShape sh = pairShapeAt(i);
     if (threads) threads[i] = sh.threads;
     if (targets_per_thread) targets_per_thread[i] = sh.k;
     if (source_tile) source_tile[i] = sh.srcTile;
+    if (min_blocks) min_blocks[i] = sh.minBlocks;
   }
   return n;
 }
@@ -738,7 +845,8 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     if (!sameGeometry(ctx, ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps)) {
       if (ctx->velBatch) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
       ctx->velBatch.reset();
-      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, s);
+      const bool precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
+      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, s);
       ctx->velBatch->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
     Batch& B = *ctx->velBatch;
@@ -791,7 +899,7 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps)) {
       if (ctx->rkBatch) LPM_CUDA(cudaDeviceSynchronize());
       ctx->rkBatch.reset();
-      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, s);
+      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, false, s);
       ctx->rkBatch->solves[0]->stage.io = ParticleIO{};
     }
     Batch& B = *ctx->rkBatch;
@@ -896,6 +1004,29 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
+    auto ioOf = [](const lpm_bve_state* st) {
+      ParticleIO io;
+      io.na = st->nverts;
+      io.nb = st->nfaces;
+      io.ax = DVec{st->vx, st->vx_stride_i, st->vx_stride_c};
+      io.au = DVec{st->vvel, st->vvel_stride_i, st->vvel_stride_c};
+      io.azeta = st->vzeta;
+      io.bx = DVec{st->fx, st->fx_stride_i, st->fx_stride_c};
+      io.bu = DVec{st->fvel, st->fvel_stride_i, st->fvel_stride_c};
+      io.bzeta = st->fzeta;
+      io.barea = st->farea;
+      return io;
+    };
+    if (B.prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0) {
+      int big = 0;  // tune on the solve with the most pairs: it dominates the launch
+      for (int m = 1; m < nsolves; ++m)
+        if ((states[m].nverts + states[m].nfaces) * states[m].nfaces >
+            (states[big].nverts + states[big].nfaces) * states[big].nfaces)
+          big = m;
+      const ParticleIO io = ioOf(&states[big]);
+      const HostPlan H = prepareHost(Mode::RK4, io, states[big].fmask, skip, sort, s);
+      B.shape = autotune(ctx, Mode::RK4, B.prec, io, states[big].fmask, skip, sort, eps, false, H, s);
+    }
     for (int m = 0; m < nsolves; ++m) {
       const lpm_bve_state* st = &states[m];
       checkVec("vx", st->vx, st->nverts, st->vx_stride_i, st->vx_stride_c);
@@ -914,7 +1045,8 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
       io.bzeta = st->fzeta;
       io.barea = st->farea;
       B.solves.emplace_back(new SolvePlan());
-      buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), s);
+      const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s);
+      buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), H, s);
     }
     finalizeBatch(B, ctx->dev, s);
     if (ctx->verbose)

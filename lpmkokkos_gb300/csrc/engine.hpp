@@ -77,10 +77,14 @@ struct SolveStage {
 
 // Launch-shape of the FP32C pair kernel.
 struct PairShape {
-  int threads;   // CTA size
-  int k;         // targets per thread
-  int srcTile;   // sources staged in shared memory per step
+  int threads;    // CTA size
+  int k;          // targets per thread
+  int srcTile;    // sources staged in shared memory per step
+  int minBlocks;  // resident CTAs per SM the register budget is sized for (1 = compiler's choice)
   int tileSize() const { return threads * k; }
+  bool operator==(const PairShape& o) const {
+    return threads == o.threads && k == o.k && srcTile == o.srcTile && minBlocks == o.minBlocks;
+  }
 };
 
 enum class Precision { FP64 = 0, FP32C = 1 };

@@ -154,8 +154,9 @@ __device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const f
 //   are formed from hi/lo float pairs, accurate to ~1e-7 relative.  19 FMA-pipe ops per pair.
 // NEWTON = false skips the Newton refinement of the hardware reciprocal (11 FMA-pipe ops per
 //   pair in the fast formulation); selected by LPM_BVE_RCP_APPROX.
-template <int NTH, int K, int ST, bool PSI, bool PRECISE, bool NEWTON>
-__global__ void __launch_bounds__(NTH) pairFP32C(const SolveDev* __restrict__ solves,
+// MINB: minimum resident CTAs per SM the register allocation must allow (__launch_bounds__).
+template <int NTH, int K, int ST, int MINB, bool PSI, bool PRECISE, bool NEWTON>
+__global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restrict__ solves,
                                                  const WorkItem* __restrict__ items, int nitems,
                                                  int* __restrict__ counter) {
   static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
@@ -328,24 +329,25 @@ __global__ void __launch_bounds__(kFP64Threads) pairFP64(const SolveDev* __restr
 // Instantiated launch shapes (the autotuner chooses among these).  Variants per shape:
 // [0] fast, [1] precise (hi/lo), [2] fast without the Newton step; each without / with psi.
 struct ShapeFn {
-  int threads, k, srcTile;
+  int threads, k, srcTile, minBlocks;
   void* fn[3][2];
 };
-#define LPM_SHAPE(T, K, S)                                                                                        \
-  {T, K, S, {{(void*)pairFP32C<T, K, S, false, false, true>, (void*)pairFP32C<T, K, S, true, false, true>},        \
-             {(void*)pairFP32C<T, K, S, false, true, true>, (void*)pairFP32C<T, K, S, true, true, true>},          \
-             {(void*)pairFP32C<T, K, S, false, false, false>, (void*)pairFP32C<T, K, S, true, false, false>}}}
+#define LPM_SHAPE(T, K, S, B)                                                                                        \
+  {T, K, S, B, {{(void*)pairFP32C<T, K, S, B, false, false, true>, (void*)pairFP32C<T, K, S, B, true, false, true>},   \
+                {(void*)pairFP32C<T, K, S, B, false, true, true>, (void*)pairFP32C<T, K, S, B, true, true, true>},     \
+                {(void*)pairFP32C<T, K, S, B, false, false, false>, (void*)pairFP32C<T, K, S, B, true, false, false>}}}
 const ShapeFn kShapes[] = {
-  LPM_SHAPE(128, 4, 256),
-  LPM_SHAPE(128, 8, 256),
-  LPM_SHAPE(256, 2, 256),
-  LPM_SHAPE(256, 4, 256),
+  LPM_SHAPE(128, 4, 256, 1),
+  LPM_SHAPE(128, 4, 256, 6),
+  LPM_SHAPE(128, 8, 256, 1),
+  LPM_SHAPE(256, 2, 256, 1),
+  LPM_SHAPE(256, 4, 256, 1),
 };
 #undef LPM_SHAPE
 
 const ShapeFn* findShape(const PairShape& s) {
   for (const auto& e : kShapes)
-    if (e.threads == s.threads && e.k == s.k && e.srcTile == s.srcTile) return &e;
+    if (e.threads == s.threads && e.k == s.k && e.srcTile == s.srcTile && e.minBlocks == s.minBlocks) return &e;
   return nullptr;
 }
 
@@ -365,10 +367,13 @@ void* kernelFor(Precision prec, const PairShape& shape, bool psi, bool precise, 
 
 int pairShapeCount() { return (int)(sizeof(kShapes) / sizeof(kShapes[0])); }
 
-PairShape pairShapeAt(int i) { return PairShape{kShapes[i].threads, kShapes[i].k, kShapes[i].srcTile}; }
+PairShape pairShapeAt(int i) {
+  return PairShape{kShapes[i].threads, kShapes[i].k, kShapes[i].srcTile, kShapes[i].minBlocks};
+}
 
 bool pairShapeSupported(Precision prec, const PairShape& shape) {
-  if (prec == Precision::FP64) return shape.threads == kFP64Threads && shape.k == 1 && shape.srcTile == kFP64Tile;
+  if (prec == Precision::FP64)
+    return shape.threads == kFP64Threads && shape.k == 1 && shape.srcTile == kFP64Tile && shape.minBlocks == 1;
   return findShape(shape) != nullptr;
 }
 

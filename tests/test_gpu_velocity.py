@@ -194,3 +194,15 @@ def test_nan_targets_do_not_contaminate(ctx, flags):
     assert np.isfinite(g).all()
     tol = FP64_TOL if flags == P.FP64 else FP32C_TOL
     assert _l2rel(g, r) <= tol
+
+
+def test_autotuned_context_stays_within_tolerance(oracle):
+    """With the autotuner on, whichever launch shape wins gives results within the FP32C bar."""
+    from lpmkokkos_gb300 import bve
+    ctx = bve.Context(0, autotune=True)
+    m, zf = _problem(0, 5)
+    uv, uf, pv, pf = _gpu_velocity(ctx, m, zf, P.FP32C)
+    ruv, ruf, rpv, rpf = oracle.velocity(m["vx"], m["fx"], zf, m["farea"], m["fmask"], psi=True)
+    leaf = m["fmask"] == 0
+    assert _l2rel(np.concatenate([uv, uf[leaf]]), np.concatenate([ruv, ruf[leaf]])) <= FP32C_TOL
+    ctx.close()
