@@ -11,6 +11,7 @@
 #include "lpm_bve.h"
 #include "lpm_bve_ensemble.h"
 #include "engine.hpp"
+#include "engine_core.hpp"
 
 #include <algorithm>
 #include <array>
@@ -26,64 +27,6 @@
 
 namespace lpm {
 
-// ---------------------------------------------------------------------------------------
-// small utilities
-// ---------------------------------------------------------------------------------------
-struct Error {
-  int code;
-  std::string msg;
-};
-
-#define LPM_CUDA(call)                                                                          \
-  do {                                                                                          \
-    cudaError_t e_ = (call);                                                                    \
-    if (e_ != cudaSuccess)                                                                      \
-      throw Error{LPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};            \
-  } while (0)
-
-[[noreturn]] void fail(int code, const char* fmt, ...) {
-  char buf[512];
-  va_list ap;
-  va_start(ap, fmt);
-  std::vsnprintf(buf, sizeof(buf), fmt, ap);
-  va_end(ap);
-  throw Error{code, buf};
-}
-
-class DeviceArena {  // owns a set of cudaMalloc'd buffers
- public:
-  ~DeviceArena() { release(); }
-  template <typename T>
-  T* alloc(size_t count) {
-    if (count == 0) count = 1;
-    void* p = nullptr;
-    const cudaError_t e = cudaMalloc(&p, count * sizeof(T));
-    if (e != cudaSuccess) {
-      (void)cudaGetLastError();
-      fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "cudaMalloc(%zu bytes): %s",
-           count * sizeof(T), cudaGetErrorString(e));
-    }
-    ptrs_.push_back(p);
-    bytes_ += count * sizeof(T);
-    return static_cast<T*>(p);
-  }
-  void release() {
-    for (void* p : ptrs_) cudaFree(p);
-    ptrs_.clear();
-    bytes_ = 0;
-  }
-  size_t bytes() const { return bytes_; }
-
- private:
-  std::vector<void*> ptrs_;
-  size_t bytes_ = 0;
-};
-
-template <typename T>
-void upload(T* dst, const std::vector<T>& src, cudaStream_t s) {
-  if (!src.empty()) LPM_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
-}
-
 // Copy n strided 3-vectors from the device to a host row-major array (synchronises s).
 std::vector<double> fetchPoints(const double* p, int64_t n, int64_t si, int64_t sc, cudaStream_t s) {
   std::vector<double> out(3 * (size_t)n);
@@ -97,25 +40,6 @@ std::vector<double> fetchPoints(const double* p, int64_t n, int64_t si, int64_t 
   return out;
 }
 
-inline uint32_t spread3(uint32_t x) {  // 10-bit value -> every third bit
-  x &= 0x3ffu;
-  x = (x | (x << 16)) & 0x030000ffu;
-  x = (x | (x << 8)) & 0x0300f00fu;
-  x = (x | (x << 4)) & 0x030c30c3u;
-  x = (x | (x << 2)) & 0x09249249u;
-  return x;
-}
-inline uint32_t mortonKey(const double* x) {
-  uint32_t q[3];
-  for (int c = 0; c < 3; ++c) {
-    double t = (x[c] + 1.05) * (1024.0 / 2.1);
-    if (!(t >= 0.0)) t = 0.0;  // also catches NaN
-    if (t > 1023.0) t = 1023.0;
-    q[c] = (uint32_t)t;
-  }
-  return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
-}
-
 void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc) {
   if (n < 0) fail(LPM_ERR_INVALID_ARGUMENT, "%s: negative count", name);
   if (n > 0 && !p) fail(LPM_ERR_INVALID_ARGUMENT, "%s: null pointer with n = %lld", name, (long long)n);
@@ -124,114 +48,30 @@ void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc
   if (n > (int64_t)INT_MAX / 4) fail(LPM_ERR_NOT_SUPPORTED, "%s: %lld points exceed the supported size", name, (long long)n);
 }
 
-// ---------------------------------------------------------------------------------------
-// plans
-// ---------------------------------------------------------------------------------------
-enum class Mode { Distinct = 0, Collocated = 1, RK4 = 2 };
-
-// Launch shape used when the autotuner is off (measured best on GB300 among the
-// instantiated shapes; the autotuner may choose another one per problem size).
-constexpr PairShape kDefaultFP32C{128, 4, 256, 1};
-constexpr PairShape kFP64Shape{128, 1, 128, 1};
-
-struct SolvePlan {
-  Mode mode = Mode::Distinct;
-  Precision prec = Precision::FP64;
-  ParticleIO io;
-  const uint8_t* mask = nullptr;
-  bool skipMasked = false, sorted = true;
-  int nslots = 0, ns = 0, ntiles = 0, nchunks = 1, tileSize = 1, chunkLen = 0;
-  double eps2 = 0.0;
-  std::vector<int2> tileSelfHost;
-  DeviceArena mem;
-  SolveStage stage{};
-  SolveDev dev{};
-};
-
-// CUDA-event timing of the pair-kernel launches (enabled by lpm_bve_ctx_set_timing).
-struct PairTimer {
-  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
-  std::vector<cudaEvent_t> pool;
-  double totalMs = 0.0;
-  int64_t launches = 0;
-  cudaEvent_t get() {
-    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
-    cudaEvent_t e = nullptr;
-    LPM_CUDA(cudaEventCreate(&e));
-    return e;
-  }
-  void collect() {
-    for (auto& pr : pending) {
-      LPM_CUDA(cudaEventSynchronize(pr.second));
-      float ms = 0.f;
-      LPM_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
-      totalMs += ms;
-      launches += 1;
-      pool.push_back(pr.first);
-      pool.push_back(pr.second);
-    }
-    pending.clear();
-  }
-  ~PairTimer() {
-    for (auto& pr : pending) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
-    for (auto e : pool) cudaEventDestroy(e);
-  }
-};
-
-struct Batch {
-  PairTimer* timer = nullptr;  // non-null: bracket each pair launch with events (direct launches only)
-  std::vector<std::unique_ptr<SolvePlan>> solves;
-  Precision prec = Precision::FP64;
-  PairShape shape = kFP64Shape;
-  bool rk4 = false;
-  bool precise = false;    // FP32C hi/lo differences (arbitrary distinct targets)
-  bool rcpApprox = false;  // FP32C without the Newton step (LPM_BVE_RCP_APPROX)
-  int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
-  std::vector<double> itemPairs;  // target-source pairs of each work item (host, launch order)
-  DeviceArena mem;
-  WorkItem* items = nullptr;
-  SolveDev* solveDev = nullptr;
-  SolveStage* stageDev = nullptr;
-  int4* prepMap = nullptr;
-  int4* slotMap = nullptr;
-  int* counter = nullptr;
-  // captured RK4 step
-  cudaGraphExec_t graph = nullptr;
-  bool graphQuirk = false, graphRenorm = false, graphRcp = false;
-  ~Batch() {
-    if (graph) cudaGraphExecDestroy(graph);
-  }
-};
-
-struct DeviceInfo {
-  int device = 0, sms = 0;
-};
-
-// Shape-independent part of a plan, computed on the host: target slot order, compacted
-// source list, and the maps between them.
-struct HostPlan {
-  int64_t na = 0, nb = 0;
-  std::vector<uint8_t> hmask;
-  std::vector<int> ids, srcFace, self, srcSlot;
-};
-
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
                      cudaStream_t s) {
-  HostPlan H;
-  const int64_t na = io.na, nb = io.nb;
-  H.na = na;
-  H.nb = nb;
-  std::vector<uint8_t>& hmask = H.hmask;
-  hmask.assign((size_t)nb, 0);
-  if (mask && nb > 0) {
-    LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)nb, cudaMemcpyDeviceToHost, s));
+  std::vector<uint8_t> hmask((size_t)io.nb, 0);
+  if (mask && io.nb > 0) {
+    LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)io.nb, cudaMemcpyDeviceToHost, s));
     LPM_CUDA(cudaStreamSynchronize(s));
   }
   std::vector<double> ha, hb;
   if (sort) {
-    if (mode != Mode::Collocated) ha = fetchPoints(io.ax.p, na, io.ax.si, io.ax.sc, s);
-    hb = fetchPoints(io.bx.p, nb, io.bx.si, io.bx.sc, s);
+    if (mode != Mode::Collocated) ha = fetchPoints(io.ax.p, io.na, io.ax.si, io.ax.sc, s);
+    hb = fetchPoints(io.bx.p, io.nb, io.bx.si, io.bx.sc, s);
   }
+  return prepareHostFromHost(mode, io.na, io.nb, ha.empty() ? nullptr : ha.data(), hb.empty() ? nullptr : hb.data(),
+                             hmask.data(), skipMasked, sort);
+}
+
+HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
+                             const uint8_t* hmaskIn, bool skipMasked, bool sort) {
+  HostPlan H;
+  H.na = na;
+  H.nb = nb;
+  std::vector<uint8_t>& hmask = H.hmask;
+  hmask.assign((size_t)nb, 0);
+  if (hmaskIn && nb > 0) std::copy(hmaskIn, hmaskIn + nb, hmask.begin());
 
   // Target slots: particle ids (a: id = i; face f: id = na + f).
   std::vector<int> ids;
@@ -399,10 +239,13 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
     const int chunkLen = chunkLength(P.ns, srcTile);
     P.chunkLen = chunkLen;
     P.nchunks = P.ns > 0 ? (P.ns + chunkLen - 1) / chunkLen : 1;
-    double* partial = P.mem.alloc<double>((size_t)P.nchunks * ncomp * std::max(1, P.nslots));
-    P.stage.partial = partial;
+    if (!P.partialReady) {
+      double* partial = P.mem.alloc<double>((size_t)P.nchunks * ncomp * std::max(1, P.nslots));
+      P.stage.partial = partial;
+      P.dev.partial = partial;
+      P.partialReady = true;
+    }
     P.stage.nchunks = P.nchunks;
-    P.dev.partial = partial;
     P.dev.nchunks = P.nchunks;
     for (int t = 0; t < P.ntiles; ++t)
       for (int c = 0; c < P.nchunks; ++c) {
@@ -584,7 +427,8 @@ std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, c
     B->shape = autotune(ctx, mode, prec, io, mask, skipMasked, sort, eps, precise, H, s);
   B->rk4 = (mode == Mode::RK4);
   B->precise = precise;
-  B->solves.emplace_back(new SolvePlan());
+  B->owned.emplace_back(new SolvePlan());
+  B->solves.push_back(B->owned.back().get());
   buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), H, s);
   finalizeBatch(*B, ctx->dev, s);
   if (ctx->verbose)
@@ -618,7 +462,8 @@ PairShape autotune(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO
       T.prec = prec;
       T.shape = sh;
       T.precise = precise;
-      T.solves.emplace_back(new SolvePlan());
+      T.owned.emplace_back(new SolvePlan());
+      T.solves.push_back(T.owned.back().get());
       buildSolve(*T.solves[0], mode, prec, io, mask, skipMasked, sort, eps, sh.tileSize(), H, s);
       finalizeBatch(T, ctx->dev, s);
       // A bounded trial: a few waves of work items are enough to rank shapes.
@@ -1044,7 +889,8 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
       io.bu = DVec{st->fvel, st->fvel_stride_i, st->fvel_stride_c};
       io.bzeta = st->fzeta;
       io.barea = st->farea;
-      B.solves.emplace_back(new SolvePlan());
+      B.owned.emplace_back(new SolvePlan());
+      B.solves.push_back(B.owned.back().get());
       const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s);
       buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), H, s);
     }

@@ -1,0 +1,209 @@
+// engine_core.hpp -- internals of the host engine shared by engine.cpp and server.cpp:
+// error handling, device arenas, per-solve plans and batches, and the functions that build
+// plans and queue one evaluation or one RK4 step of a batch.
+#pragma once
+
+#include "lpm_bve.h"
+#include "engine.hpp"
+
+#include <algorithm>
+#include <climits>
+#include <cstdarg>
+#include <cstdio>
+#include <memory>
+#include <string>
+#include <vector>
+
+namespace lpm {
+
+// ---------------------------------------------------------------------------------------
+// small utilities
+// ---------------------------------------------------------------------------------------
+struct Error {
+  int code;
+  std::string msg;
+};
+
+#define LPM_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw Error{LPM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)};            \
+  } while (0)
+
+[[noreturn]] inline void fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  throw Error{code, buf};
+}
+
+class DeviceArena {  // owns a set of cudaMalloc'd buffers
+ public:
+  ~DeviceArena() { release(); }
+  template <typename T>
+  T* alloc(size_t count) {
+    if (count == 0) count = 1;
+    void* p = nullptr;
+    const cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "cudaMalloc(%zu bytes): %s",
+           count * sizeof(T), cudaGetErrorString(e));
+    }
+    ptrs_.push_back(p);
+    bytes_ += count * sizeof(T);
+    return static_cast<T*>(p);
+  }
+  void release() {
+    for (void* p : ptrs_) cudaFree(p);
+    ptrs_.clear();
+    bytes_ = 0;
+  }
+  size_t bytes() const { return bytes_; }
+
+ private:
+  std::vector<void*> ptrs_;
+  size_t bytes_ = 0;
+};
+
+template <typename T>
+inline void upload(T* dst, const std::vector<T>& src, cudaStream_t s) {
+  if (!src.empty()) LPM_CUDA(cudaMemcpyAsync(dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+}
+
+// Copy n strided 3-vectors from the device to a host row-major array (synchronises s).
+std::vector<double> fetchPoints(const double* p, int64_t n, int64_t si, int64_t sc, cudaStream_t s);
+
+inline uint32_t spread3(uint32_t x) {  // 10-bit value -> every third bit
+  x &= 0x3ffu;
+  x = (x | (x << 16)) & 0x030000ffu;
+  x = (x | (x << 8)) & 0x0300f00fu;
+  x = (x | (x << 4)) & 0x030c30c3u;
+  x = (x | (x << 2)) & 0x09249249u;
+  return x;
+}
+inline uint32_t mortonKey(const double* x) {
+  uint32_t q[3];
+  for (int c = 0; c < 3; ++c) {
+    double t = (x[c] + 1.05) * (1024.0 / 2.1);
+    if (!(t >= 0.0)) t = 0.0;  // also catches NaN
+    if (t > 1023.0) t = 1023.0;
+    q[c] = (uint32_t)t;
+  }
+  return spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+}
+
+void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc);
+
+// ---------------------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------------------
+enum class Mode { Distinct = 0, Collocated = 1, RK4 = 2 };
+
+// Launch shape used when the autotuner is off (measured best on GB300 among the
+// instantiated shapes; the autotuner may choose another one per problem size).
+inline constexpr PairShape kDefaultFP32C{128, 4, 256, 1};
+inline constexpr PairShape kFP64Shape{128, 1, 128, 1};
+
+struct SolvePlan {
+  Mode mode = Mode::Distinct;
+  Precision prec = Precision::FP64;
+  ParticleIO io;
+  const uint8_t* mask = nullptr;
+  bool skipMasked = false, sorted = true;
+  int nslots = 0, ns = 0, ntiles = 0, nchunks = 1, tileSize = 1, chunkLen = 0;
+  double eps2 = 0.0;
+  std::vector<int2> tileSelfHost;
+  DeviceArena mem;
+  bool partialReady = false;  // partial-sum buffer allocated (once per plan)
+  SolveStage stage{};
+  SolveDev dev{};
+};
+
+// CUDA-event timing of the pair-kernel launches (enabled by lpm_bve_ctx_set_timing).
+struct PairTimer {
+  std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+  std::vector<cudaEvent_t> pool;
+  double totalMs = 0.0;
+  int64_t launches = 0;
+  cudaEvent_t get() {
+    if (!pool.empty()) { cudaEvent_t e = pool.back(); pool.pop_back(); return e; }
+    cudaEvent_t e = nullptr;
+    LPM_CUDA(cudaEventCreate(&e));
+    return e;
+  }
+  void collect() {
+    for (auto& pr : pending) {
+      LPM_CUDA(cudaEventSynchronize(pr.second));
+      float ms = 0.f;
+      LPM_CUDA(cudaEventElapsedTime(&ms, pr.first, pr.second));
+      totalMs += ms;
+      launches += 1;
+      pool.push_back(pr.first);
+      pool.push_back(pr.second);
+    }
+    pending.clear();
+  }
+  ~PairTimer() {
+    for (auto& pr : pending) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto e : pool) cudaEventDestroy(e);
+  }
+};
+
+struct Batch {
+  PairTimer* timer = nullptr;  // non-null: bracket each pair launch with events (direct launches only)
+  std::vector<std::unique_ptr<SolvePlan>> owned;  // plans owned by this batch (single solves, ensembles)
+  std::vector<SolvePlan*> solves;                 // the batch's solves in solve-index order (not owned)
+  Precision prec = Precision::FP64;
+  PairShape shape = kFP64Shape;
+  bool rk4 = false;
+  bool precise = false;    // FP32C hi/lo differences (arbitrary distinct targets)
+  bool rcpApprox = false;  // FP32C without the Newton step (LPM_BVE_RCP_APPROX)
+  int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
+  std::vector<double> itemPairs;  // target-source pairs of each work item (host, launch order)
+  DeviceArena mem;
+  WorkItem* items = nullptr;
+  SolveDev* solveDev = nullptr;
+  SolveStage* stageDev = nullptr;
+  int4* prepMap = nullptr;
+  int4* slotMap = nullptr;
+  int* counter = nullptr;
+  // captured RK4 step
+  cudaGraphExec_t graph = nullptr;
+  bool graphQuirk = false, graphRenorm = false, graphRcp = false;
+  ~Batch() {
+    if (graph) cudaGraphExecDestroy(graph);
+  }
+};
+
+struct DeviceInfo {
+  int device = 0, sms = 0;
+};
+
+
+// Shape-independent part of a plan, computed on the host: target slot order, compacted
+// source list, and the maps between them.
+struct HostPlan {
+  int64_t na = 0, nb = 0;
+  std::vector<uint8_t> hmask;
+  std::vector<int> ids, srcFace, self, srcSlot;
+};
+
+HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
+                     cudaStream_t s);
+// Same from host arrays: ha (na x 3) and hb (nb x 3) row-major positions, hmask (nb bytes).
+HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
+                             const uint8_t* hmask, bool skipMasked, bool sort);
+void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
+                bool sort, double eps, int tileSize, const HostPlan& H, cudaStream_t s);
+int chunkLength(int ns, int srcTile);
+// Allocates a plan's partial buffer on first use; builds items, block maps and device tables.
+void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s);
+void refreshTables(Batch& B, cudaStream_t s);
+void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s);
+void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
+
+}  // namespace lpm
