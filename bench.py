@@ -4,9 +4,9 @@
 Workload (the single-solve configuration the headline metric is quoted on): icosahedral
 level 7 (163,842 vertices; 436,900 faces of which 327,680 leaves are the sources), RH54
 relative vorticity plus 3 seeded Gaussian vortices (amplitude U(-2,2), width 0.1 rad),
-Omega = 2 pi, eps = 0, dt = 0.01.  A step is one RK4 step (four direct-sum evaluations
-over every vertex and face target).  Synthetic data generated on the host; nothing is
-downloaded.
+Omega = 2 pi, eps = 0, dt = 0.00125 (0.01 at level 4, halved per level).  A step is one
+RK4 step (four direct-sum evaluations over every vertex and face target).  Synthetic data
+generated on the host; nothing is downloaded.
 
 Printed JSON line (rank 0):
   value      RK4 steps/s, whole job, device-resident inputs, graph-replayed steps
@@ -61,9 +61,13 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
-    ap.add_argument("--config", choices=["c2", "c3", "c5"], default="c2",
+    ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
                     help="c2: single solve icos L7 (default, the headline); c3: 64-solve uneven ensemble; "
+                         "c4: continuous-batching server under Poisson arrivals; "
                          "c5: icos L8, eps 0.01, 8 vortices, then the stream function at all targets")
+    ap.add_argument("--requests", type=int, default=96, help="c4: number of requests")
+    ap.add_argument("--rate", type=float, default=8.0, help="c4: mean arrivals per second")
+    ap.add_argument("--req-steps", type=int, default=10, help="c4: RK4 steps per request")
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     return ap.parse_args()
 
@@ -534,6 +538,100 @@ def run_large(args, rank, world, local_rank):
     ctx.close()
 
 
+def run_server(args, rank, world, local_rank):
+    """Config 4: the continuous-batching server under Poisson arrivals.  Requests draw a mesh
+    uniformly from icosahedral / cubed-sphere and a level from 3-7 (weights .3 .3 .2 .15 .05),
+    RH54 + 3 seeded Gaussian vortices, dt at the level-4 Courant number, --req-steps RK4 steps
+    each.  Latency is submit-to-result on the host clock: host preparation, upload, queueing,
+    the steps and the copy back are all inside it."""
+    import threading
+
+    import numpy as np
+    import torch
+
+    import lpmkokkos_gb300 as P
+    from lpmkokkos_gb300 import bve
+    P.build()
+    torch.cuda.set_device(local_rank)
+    rng = np.random.default_rng(SEED_BASE + 4)
+    levels, weights = [3, 4, 5, 6, 7], [0.3, 0.3, 0.2, 0.15, 0.05]
+    n = args.requests
+    kinds = rng.integers(0, 2, size=n)
+    lvls = rng.choice(levels, size=n, p=weights)
+    gaps = rng.exponential(1.0 / args.rate, size=n)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    specs = [dict(seed=int(k), level=int(lv), dt=courant_dt(int(k), int(lv)), nsteps=args.req_steps,
+                  ic_seed=SEED_BASE + 4 + i) for i, (k, lv) in enumerate(zip(kinds, lvls))]
+    srv = bve.Server(local_rank, flags=P.FP32C)
+    # warm-up: one zero-step request per mesh (fills the host mesh/plan cache, loads kernels)
+    warm = [srv.submit(seed=k, level=lv, dt=0.01, nsteps=0) for k in (0, 1) for lv in levels]
+    warm += [srv.submit(seed=0, level=4, dt=0.005, nsteps=2, ic_seed=s) for s in range(max(1, args.warmup))]
+    for rid in warm:
+        assert srv.wait(rid, 600.0)
+        srv.release(rid)
+    base = srv.stats()
+    ids = [None] * n
+
+    def feeder():
+        t0 = time.perf_counter()
+        for i, sp in enumerate(specs):
+            delay = arrivals[i] - (time.perf_counter() - t0)
+            if delay > 0:
+                time.sleep(delay)
+            ids[i] = srv.submit(**sp)
+
+    sampler = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or None)
+    t_start = time.perf_counter()
+    th = threading.Thread(target=feeder)
+    th.start()
+    th.join()
+    for rid in ids:
+        assert srv.wait(rid, 1800.0)
+    wall = time.perf_counter() - t_start
+    clocks = sampler.stop()
+    st = srv.stats()
+    lat = np.array([srv.timing(r)["total_s"] for r in ids])
+    waits = np.array([srv.timing(r)["wait_s"] for r in ids])
+    by_level = {}
+    for lv in levels:
+        sel = lat[lvls == lv]
+        if sel.size:
+            by_level[str(lv)] = {"n": int(sel.size), "p50_s": float(np.percentile(sel, 50)),
+                                 "max_s": float(sel.max())}
+    # the same request alone gives the same bits as in the mix
+    check = [i for i in range(n) if specs[i]["level"] <= 5][:2]
+    mixed = [srv.result(ids[i]) for i in check]
+    srv.close()
+    same = True
+    with bve.Server(local_rank, flags=P.FP32C) as alone:
+        for i, got in zip(check, mixed):
+            rid = alone.submit(**specs[i])
+            assert alone.wait(rid, 600.0)
+            ref = alone.result(rid)
+            same &= all(np.array_equal(got[k], ref[k], equal_nan=True) for k in ref)
+    solve_steps = st["solve_steps"] - base["solve_steps"]
+    pairs = st["pairs"] - base["pairs"]
+    nearest = lambda q: float(np.sort(lat)[max(0, math.ceil(q * n) - 1)])  # noqa: E731
+    out = {
+        "metric": "server requests/s", "value": n / wall, "unit": "requests/s", "n_gpus": 1,
+        "steps": args.req_steps, "warmup": len(warm), "ms_per_step": None, "higher_is_better": True,
+        "scaling": "replicas only", "vs_baseline": None, "dtype": "f32c",
+        "data": "synthetic (seeded RH54 + Gaussian vortices on generated meshes, Poisson arrivals)",
+        "config": {"workload": f"{n} requests, Poisson arrivals at {args.rate}/s, icosahedral or cubed sphere "
+                               f"levels 3-7 (weights .3 .3 .2 .15 .05), {args.req_steps} RK4 steps each, "
+                               f"dt at the level-4 Courant number, FP32C (seed {SEED_BASE + 4})",
+                   "levels": {str(lv): int((lvls == lv).sum()) for lv in levels}},
+        "latency_s": {"p50": nearest(0.5), "p99": nearest(0.99), "max": float(lat.max()),
+                      "mean_wait": float(waits.mean())},
+        "latency_by_level": by_level,
+        "solve_steps_per_s": solve_steps / wall, "computed_pairs_per_s": pairs / wall,
+        "server_iterations": st["steps_run"] - base["steps_run"], "max_running": st["max_running_seen"],
+        "wall_s": wall, "mix_equals_alone": bool(same), "clocks": clocks,
+        "e2e": {"value": n / wall, "unit": "requests/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
+    }
+    print(json.dumps(out), flush=True)
+
+
 # ------------------------------------------------------------------------------------------
 # reference arm: the reference path's CPU implementation (oracle port) on the host cores
 # ------------------------------------------------------------------------------------------
@@ -599,7 +697,7 @@ def main():
             torch.cuda.set_device(local_rank)
         dist.init_process_group(backend=backend)
     try:
-        {"c2": run_ours, "c3": run_ensemble, "c5": run_large}[args.config](args, rank, world, local_rank)
+        {"c2": run_ours, "c3": run_ensemble, "c4": run_server, "c5": run_large}[args.config](args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

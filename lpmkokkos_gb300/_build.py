@@ -22,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
 CU_SOURCES = ["pair_kernels.cu", "stage_kernels.cu", "probe.cu", "noalloc.cu"]
-CXX_SOURCES = ["engine.cpp", "mesh.cpp"]
+CXX_SOURCES = ["engine.cpp", "mesh.cpp", "server.cpp"]
 
 
 def _nvcc() -> str:
@@ -65,7 +65,8 @@ def build(verbose: bool = False) -> str:
         o = os.path.join(OUT, src + ".o")
         objs.append(o)
         if _stale(o, s, headers):
-            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", *incs, "-c", s, "-o", o]
+            cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-Wall", *incs, "-c", s, "-o",
+                   o]
             jobs.append((src, cmd))
     procs = [(src, cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))
              for src, cmd in jobs]
@@ -80,7 +81,7 @@ def build(verbose: bool = False) -> str:
         raise RuntimeError("native build failed:\n" + "\n".join(errors))
     if jobs or not os.path.exists(LIB) or any(os.path.getmtime(o) > os.path.getmtime(LIB) for o in objs):
         cmd = [_nvcc(), *ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs,
-               f"-L{os.path.join(CUDA_HOME, 'lib64')}", "-lcudart"]
+               f"-L{os.path.join(CUDA_HOME, 'lib64')}", "-lcudart", "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + res.stdout + res.stderr)

@@ -64,6 +64,26 @@ class State(ctypes.Structure):
     ]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int),
+                ("flags", ctypes.c_uint), ("eps", ctypes.c_double)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("seed", ctypes.c_int), ("level", ctypes.c_int), ("ic_seed", ctypes.c_uint64),
+                ("n_gaussians", ctypes.c_int), ("gauss_width", ctypes.c_double), ("dt", ctypes.c_double),
+                ("omega", ctypes.c_double), ("nsteps", ctypes.c_int)]
+
+
+class ServerCounters(ctypes.Structure):
+    _fields_ = [("submitted", c_i64), ("completed", c_i64), ("failed", c_i64), ("cancelled", c_i64),
+                ("running", c_i64), ("queued", c_i64), ("steps_run", c_i64), ("solve_steps", c_i64),
+                ("pairs", ctypes.c_double), ("busy_s", ctypes.c_double), ("reserved_bytes", ctypes.c_size_t),
+                ("budget_bytes", ctypes.c_size_t), ("max_running_seen", ctypes.c_int)]
+
+
+REQ_QUEUED, REQ_PREPARING, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, -1, -2
+
 _lib = None
 
 
@@ -105,6 +125,22 @@ def _declare(L):
     L.lpm_ic_gaussians_add.argtypes = [vp, c_i64, vp, vp, ctypes.c_int, ctypes.c_double, vp]
     L.lpm_probe_fp32_fma.argtypes = [ctypes.c_int, ctypes.c_int, c_dp, c_dp]
     L.lpm_ic_gaussian_params.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
+    L.lpm_bve_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
+    L.lpm_bve_server_estimate.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(Request),
+                                          ctypes.POINTER(ctypes.c_size_t)]
+    L.lpm_bve_server_submit.argtypes = [vp, ctypes.POINTER(Request), ctypes.POINTER(c_i64)]
+    L.lpm_bve_server_wait.argtypes = [vp, c_i64, ctypes.c_double]
+    L.lpm_bve_server_status.argtypes = [vp, c_i64, ctypes.POINTER(ctypes.c_int)]
+    L.lpm_bve_server_cancel.argtypes = [vp, c_i64]
+    L.lpm_bve_server_result.argtypes = [vp, c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), vp, vp, vp, vp, vp,
+                                        vp]
+    L.lpm_bve_server_release.argtypes = [vp, c_i64]
+    L.lpm_bve_server_timing.argtypes = [vp, c_i64, c_dp, c_dp, c_dp]
+    L.lpm_bve_server_latency.argtypes = [vp, c_dp, ctypes.c_int, c_dp]
+    L.lpm_bve_server_stats.argtypes = [vp, ctypes.POINTER(ServerCounters)]
+    L.lpm_bve_server_last_error.argtypes = [vp]
+    L.lpm_bve_server_last_error.restype = ctypes.c_char_p
+    L.lpm_bve_server_destroy.argtypes = [vp]
 
 
 def lib(build_if_missing: bool = False):

@@ -271,6 +271,113 @@ class Ensemble:
             pass
 
 
+def server_estimate(seed: int, level: int, flags: int = L.FP32C, nsteps: int = 1, dt: float = 0.01) -> int:
+    """Device bytes a server with these flags reserves for one request on this mesh (host-only)."""
+    opts = L.ServerOpts(0, 0, 0, flags, 0.0)
+    req = L.Request(seed, level, 0, 0, 0.1, dt, 2 * PI, nsteps)
+    n = ctypes.c_size_t()
+    L.check(L.lib().lpm_bve_server_estimate(ctypes.byref(opts), ctypes.byref(req), ctypes.byref(n)))
+    return n.value
+
+
+class Server:
+    """Continuous-batching solve server on one GPU (include/lpm_bve_server.h).
+
+    ``submit`` queues a request (mesh seed/level, RH54 + seeded Gaussian vortices, dt, Omega,
+    step count) and returns its id at once; the server admits requests while their device
+    footprint fits the HBM budget and advances every running solve by one RK4 step per
+    iteration.  ``result`` returns the final state as host arrays.
+    """
+
+    def __init__(self, device: Optional[int] = None, budget_bytes: int = 0, max_active: int = 0,
+                 flags: int = L.FP32C, eps: float = 0.0):
+        self._lib = L.lib()
+        dev = torch.cuda.current_device() if device is None else device
+        opts = L.ServerOpts(dev, budget_bytes, max_active, flags, eps)
+        h = ctypes.c_void_p()
+        rc = self._lib.lpm_bve_server_create(ctypes.byref(opts), ctypes.byref(h))
+        if rc != L.LPM_OK:
+            raise L.LpmError(rc, "server creation failed (see stderr)")
+        self.handle = h
+
+    def _check(self, rc):
+        if rc != L.LPM_OK:
+            raise L.LpmError(rc, self._lib.lpm_bve_server_last_error(self.handle).decode())
+        return rc
+
+    def submit(self, seed: int, level: int, dt: float, nsteps: int, omega: float = 2 * PI, ic_seed: int = 0,
+               n_gaussians: int = 3, gauss_width: float = 0.1) -> int:
+        req = L.Request(seed, level, ic_seed, n_gaussians, gauss_width, dt, omega, nsteps)
+        rid = L.c_i64()
+        self._check(self._lib.lpm_bve_server_submit(self.handle, ctypes.byref(req), ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout: Optional[float] = None) -> bool:
+        """True when the request is done; False on timeout; raises if it failed or was cancelled."""
+        rc = self._lib.lpm_bve_server_wait(self.handle, rid, -1.0 if timeout is None else float(timeout))
+        if rc == L.LPM_ERR_TIMEOUT:
+            return False
+        self._check(rc)
+        return True
+
+    def status(self, rid: int) -> int:
+        st = ctypes.c_int()
+        self._check(self._lib.lpm_bve_server_status(self.handle, rid, ctypes.byref(st)))
+        return st.value
+
+    def cancel(self, rid: int):
+        self._check(self._lib.lpm_bve_server_cancel(self.handle, rid))
+
+    def result(self, rid: int) -> dict:
+        nv, nf = L.c_i64(), L.c_i64()
+        self._check(self._lib.lpm_bve_server_result(self.handle, rid, ctypes.byref(nv), ctypes.byref(nf),
+                                                    None, None, None, None, None, None))
+        nv, nf = nv.value, nf.value
+        out = dict(vx=np.zeros((nv, 3)), vzeta=np.zeros(nv), vvel=np.zeros((nv, 3)),
+                   fx=np.zeros((nf, 3)), fzeta=np.zeros(nf), fvel=np.zeros((nf, 3)))
+        p = [_np_ptr(out[k]) for k in ("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")]
+        self._check(self._lib.lpm_bve_server_result(self.handle, rid, None, None, *p))
+        return out
+
+    def release(self, rid: int):
+        self._check(self._lib.lpm_bve_server_release(self.handle, rid))
+
+    def timing(self, rid: int) -> dict:
+        t, w, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        self._check(self._lib.lpm_bve_server_timing(self.handle, rid, ctypes.byref(t), ctypes.byref(w),
+                                                    ctypes.byref(r)))
+        return dict(total_s=t.value, wait_s=w.value, run_s=r.value)
+
+    def latency(self, quantiles=(0.5, 0.99)) -> list:
+        q = np.asarray(quantiles, dtype=np.float64)
+        out = np.zeros_like(q)
+        self._check(self._lib.lpm_bve_server_latency(self.handle, q.ctypes.data_as(L.c_dp), q.size,
+                                                     out.ctypes.data_as(L.c_dp)))
+        return out.tolist()
+
+    def stats(self) -> dict:
+        c = L.ServerCounters()
+        self._check(self._lib.lpm_bve_server_stats(self.handle, ctypes.byref(c)))
+        return {name: getattr(c, name) for name, _ in L.ServerCounters._fields_}
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.lpm_bve_server_destroy(self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 # ----------------------------------------------------------------------------------------
 # reference-shaped containers
 # ----------------------------------------------------------------------------------------

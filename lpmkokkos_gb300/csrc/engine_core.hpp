@@ -40,17 +40,27 @@ struct Error {
   throw Error{code, buf};
 }
 
-class DeviceArena {  // owns a set of cudaMalloc'd buffers
+// Owns a set of device buffers.  By default they come from cudaMalloc/cudaFree; after
+// streamOrdered(a, f, pool) they come from `pool` in stream order on `a` and are freed in
+// stream order on `f` (the stream of their last use), so neither call waits for work in flight.
+class DeviceArena {
  public:
   ~DeviceArena() { release(); }
+  void streamOrdered(cudaStream_t allocStream, cudaStream_t freeStream, cudaMemPool_t pool) {
+    async_ = true;
+    allocS_ = allocStream;
+    freeS_ = freeStream;
+    pool_ = pool;
+  }
   template <typename T>
   T* alloc(size_t count) {
     if (count == 0) count = 1;
     void* p = nullptr;
-    const cudaError_t e = cudaMalloc(&p, count * sizeof(T));
+    const cudaError_t e =
+        async_ ? cudaMallocFromPoolAsync(&p, count * sizeof(T), pool_, allocS_) : cudaMalloc(&p, count * sizeof(T));
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
-      fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "cudaMalloc(%zu bytes): %s",
+      fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "device allocation (%zu bytes): %s",
            count * sizeof(T), cudaGetErrorString(e));
     }
     ptrs_.push_back(p);
@@ -58,7 +68,10 @@ class DeviceArena {  // owns a set of cudaMalloc'd buffers
     return static_cast<T*>(p);
   }
   void release() {
-    for (void* p : ptrs_) cudaFree(p);
+    for (void* p : ptrs_) {
+      if (async_) cudaFreeAsync(p, freeS_);
+      else cudaFree(p);
+    }
     ptrs_.clear();
     bytes_ = 0;
   }
@@ -67,6 +80,9 @@ class DeviceArena {  // owns a set of cudaMalloc'd buffers
  private:
   std::vector<void*> ptrs_;
   size_t bytes_ = 0;
+  bool async_ = false;
+  cudaStream_t allocS_ = nullptr, freeS_ = nullptr;
+  cudaMemPool_t pool_ = nullptr;
 };
 
 template <typename T>

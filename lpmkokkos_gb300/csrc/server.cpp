@@ -1,0 +1,907 @@
+// server.cpp -- continuous-batching BVE solve server (include/lpm_bve_server.h).
+//
+// Three host threads share one GPU:
+//   prep       admits queued requests first-come first-served while their estimated device
+//              footprint fits the HBM budget, then builds the mesh (cached per seed/level/
+//              flags together with its target/source plan), evaluates the initial vorticity and
+//              writes the initial state into a pinned host buffer.
+//   gpu        owns every device object.  Each iteration it uploads the requests that became
+//              ready (upload stream, stream-ordered allocation from a private pool), evaluates
+//              their initial velocity, and advances every running solve.  Running solves are
+//              grouped in size classes (log4 of pairs per evaluation); a class is one batch
+//              whose RK4 step is one CUDA graph of 13 launches, each of the four evaluations one
+//              persistent pair-kernel launch over all the class's solves.  The most expensive
+//              class takes one step per iteration, cheaper classes several (a measured time
+//              share), so small requests do not wait one large step per step of their own.  A
+//              class's batch (work items, tables, graph) is rebuilt only when its membership
+//              changes.  A solve that has taken its steps is copied back into its pinned
+//              buffer and its device memory is freed in stream order; nothing waits for the
+//              GPU except the pacing wait that keeps the host at most two iterations ahead.
+//   completion waits on each finished solve's copy event, marks it done, returns its budget
+//              reservation and wakes waiters and the admission loop.
+// A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
+// summation order depend on nothing but its own mesh and the launch shape, fixed per server.
+
+#include "lpm_bve_server.h"
+#include "engine_core.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <thread>
+#include <tuple>
+
+namespace lpm {
+namespace server {
+
+using Clock = std::chrono::steady_clock;
+
+// One mesh on the host with its RK4 plan (slot order, compacted sources), shared by every
+// request on the same (seed, level, skip-masked) key.
+struct MeshHost {
+  int64_t nv = 0, nf = 0, nl = 0;
+  std::vector<double> vx, fx, farea;
+  std::vector<uint8_t> fmask;
+  HostPlan plan;
+};
+
+// Per-request state layout, identical on the host (pinned) and on the device: doubles
+// [vx 3nv | vvel 3nv | vzeta nv | fx 3nf | fvel 3nf | fzeta nf | farea nf], then nf mask bytes.
+// Vectors are row-major (stride 3, 1), the LayoutRight views of the reference.
+struct Layout {
+  size_t vx, vvel, vzeta, fx, fvel, fzeta, farea, ndoubles, maskByte, bytes;
+  Layout(int64_t nv, int64_t nf) {
+    vx = 0;
+    vvel = 3 * (size_t)nv;
+    vzeta = 6 * (size_t)nv;
+    fx = 7 * (size_t)nv;
+    fvel = fx + 3 * (size_t)nf;
+    fzeta = fvel + 3 * (size_t)nf;
+    farea = fzeta + (size_t)nf;
+    ndoubles = farea + (size_t)nf;
+    maskByte = ndoubles * sizeof(double);
+    bytes = (maskByte + (size_t)nf + 255) / 256 * 256;
+  }
+};
+
+struct Req {
+  int64_t id = 0;
+  lpm_bve_request r{};
+  int state = LPM_REQ_QUEUED;
+  std::string err;
+  Clock::time_point tSubmit, tStart, tDone;
+  size_t est = 0;
+  int64_t nv = 0, nf = 0, nl = 0;
+  std::shared_ptr<const MeshHost> mesh;  // held from preparation until the upload
+  char* host = nullptr;                  // pinned state buffer (Layout)
+  // owned by the gpu thread while running
+  std::unique_ptr<SolvePlan> plan;
+  DeviceArena mem;
+  char* dev = nullptr;
+  int stepsDone = 0;
+  double pairsPerEval = 0.0;
+  cudaEvent_t done = nullptr;
+};
+
+}  // namespace server
+}  // namespace lpm
+
+using namespace lpm;
+using namespace lpm::server;
+
+struct lpm_bve_server {
+  DeviceInfo dev;
+  unsigned flags = 0;
+  Precision prec = Precision::FP32C;
+  PairShape shape = kDefaultFP32C;
+  double eps = 0.0;
+  bool skip = false, quirk = true, renorm = false, rcp = false;
+  size_t budget = 0;
+  int maxActive = 0;
+  cudaStream_t up = nullptr, compute = nullptr, cap = nullptr;
+  cudaMemPool_t pool = nullptr;
+
+  std::mutex mu;
+  std::condition_variable cvPrep, cvGpu, cvComp, cvDone;
+  bool stop = false, compStop = false;
+  std::string fatal;  // non-empty once a CUDA error made the server unusable
+  std::string err;    // last error of an API call
+  int64_t nextId = 1;
+  std::map<int64_t, std::unique_ptr<Req>> reqs;
+  std::deque<Req*> queued, prepared, completing;
+  size_t reserved = 0;
+  int inflight = 0;  // admitted and not finished
+  lpm_bve_server_counters st{};
+  std::vector<double> latencies;
+  std::map<std::tuple<int, int, int>, std::shared_ptr<const MeshHost>> meshes;  // prep thread only
+  std::deque<std::tuple<int, int, int>> meshOrder;
+  std::thread prepT, gpuT, compT;
+};
+
+namespace lpm {
+namespace server {
+namespace {
+
+double seconds(Clock::time_point a, Clock::time_point b) { return std::chrono::duration<double>(b - a).count(); }
+
+constexpr size_t kMeshCache = 16;
+
+// Device bytes of one request: state, plan (targets, sources, RK4 increments, partial sums)
+// and its share of the batch tables; 5 % + 1 MiB for pool granularity.
+size_t estimateBytes(Precision prec, const PairShape& shape, bool skip, int64_t nv, int64_t nf, int64_t nl) {
+  const Layout L(nv, nf);
+  const size_t nslots = (size_t)nv + (size_t)(skip ? nl : nf), ns = (size_t)nl;
+  const size_t ts = (size_t)shape.tileSize(), ntiles = (nslots + ts - 1) / ts;
+  const int chunk = chunkLength((int)ns, shape.srcTile);
+  const size_t nchunks = ns > 0 ? (ns + chunk - 1) / chunk : 1;
+  const size_t ncomp = (size_t)pairNumComponents(prec, true);
+  size_t plan = 8 * nslots + 12 * ntiles + 8 * ns + 24 * nslots + (prec == Precision::FP32C ? 64 : 32) * ns +
+                4 * 32 * nslots + 8 * nchunks * ncomp * nslots;
+  const size_t bs = (size_t)stageBlockSize();
+  size_t tables = 2 * (ntiles * nchunks * sizeof(WorkItem) + (2 * nslots / bs + ns / bs + 4) * sizeof(int4) +
+                       sizeof(SolveDev) + sizeof(SolveStage));
+  const size_t raw = L.bytes + plan + tables;
+  return raw + raw / 20 + (1u << 20);
+}
+
+// Empty when the request is well formed, else the reason.
+std::string validate(const lpm_bve_request& q) {
+  if ((q.seed != LPM_SEED_ICOS_TRI && q.seed != LPM_SEED_CUBED) || q.level < 0 || q.level > 10)
+    return "seed must be LPM_SEED_ICOS_TRI/CUBED and level 0..10";
+  if (q.nsteps < 0 || !std::isfinite(q.dt) || !std::isfinite(q.omega)) return "nsteps must be >= 0 and dt, omega finite";
+  if (q.n_gaussians < 0 || q.n_gaussians > 4096 || (q.n_gaussians > 0 && !(q.gauss_width > 0.0)))
+    return "0..4096 Gaussians with a positive width";
+  return std::string();
+}
+
+int setErr(lpm_bve_server* S, int code, const std::string& msg) {
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->err = msg;
+  return code;
+}
+
+// Marks a request failed and returns its reservation (caller holds the lock).
+void failLocked(lpm_bve_server* S, Req* r, const std::string& msg) {
+  if (r->state == LPM_REQ_DONE || r->state == LPM_REQ_FAILED || r->state == LPM_REQ_CANCELLED) return;
+  const bool admitted = r->state != LPM_REQ_QUEUED;
+  r->state = LPM_REQ_FAILED;
+  r->err = msg;
+  r->tDone = Clock::now();
+  if (admitted) {
+    S->reserved -= r->est;
+    S->inflight -= 1;
+  }
+  S->st.failed += 1;
+  S->cvDone.notify_all();
+  S->cvPrep.notify_all();
+}
+
+std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) {
+  const auto key = std::make_tuple(seed, level, S->skip ? 1 : 0);
+  auto it = S->meshes.find(key);
+  if (it != S->meshes.end()) return it->second;
+  auto M = std::make_shared<MeshHost>();
+  if (lpm_mesh_counts(seed, level, &M->nv, &M->nf, &M->nl) != LPM_OK)
+    fail(LPM_ERR_INVALID_ARGUMENT, "mesh seed %d level %d", seed, level);
+  M->vx.resize(3 * (size_t)M->nv);
+  M->fx.resize(3 * (size_t)M->nf);
+  M->farea.resize((size_t)M->nf);
+  M->fmask.resize((size_t)M->nf);
+  if (lpm_mesh_build(seed, level, M->vx.data(), M->fx.data(), M->farea.data(), M->fmask.data()) != LPM_OK)
+    fail(LPM_ERR_INVALID_ARGUMENT, "mesh seed %d level %d", seed, level);
+  M->plan = prepareHostFromHost(Mode::RK4, M->nv, M->nf, M->vx.data(), M->fx.data(), M->fmask.data(), S->skip, true);
+  S->meshes[key] = M;
+  S->meshOrder.push_back(key);
+  if (S->meshOrder.size() > kMeshCache) {
+    S->meshes.erase(S->meshOrder.front());
+    S->meshOrder.pop_front();
+  }
+  return M;
+}
+
+// Host side of a request: mesh, initial vorticity (RH54 + seeded Gaussian vortices, as
+// BVESphere::init_vorticity evaluates an initial condition at vertices and faces), zero
+// velocity (computed on the GPU before the first step), pinned buffer.
+void prepare(lpm_bve_server* S, Req* r) {
+  r->mesh = meshFor(S, r->r.seed, r->r.level);
+  const MeshHost& M = *r->mesh;
+  const Layout L(M.nv, M.nf);
+  void* p = nullptr;
+  const cudaError_t e = cudaHostAlloc(&p, L.bytes, cudaHostAllocDefault);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    fail(LPM_ERR_OUT_OF_MEMORY, "pinned host buffer (%zu bytes): %s", L.bytes, cudaGetErrorString(e));
+  }
+  r->host = static_cast<char*>(p);
+  double* d = reinterpret_cast<double*>(r->host);
+  std::memcpy(d + L.vx, M.vx.data(), sizeof(double) * M.vx.size());
+  std::memcpy(d + L.fx, M.fx.data(), sizeof(double) * M.fx.size());
+  std::memcpy(d + L.farea, M.farea.data(), sizeof(double) * M.farea.size());
+  std::memcpy(r->host + L.maskByte, M.fmask.data(), M.fmask.size());
+  std::fill(d + L.vvel, d + L.vvel + 3 * M.nv, 0.0);
+  std::fill(d + L.fvel, d + L.fvel + 3 * M.nf, 0.0);
+  lpm_ic_rh54(d + L.vx, M.nv, d + L.vzeta);
+  lpm_ic_rh54(d + L.fx, M.nf, d + L.fzeta);
+  const int ng = r->r.n_gaussians;
+  if (ng > 0) {
+    std::vector<double> c(3 * (size_t)ng), a((size_t)ng);
+    lpm_ic_gaussian_params(r->r.ic_seed, ng, -2.0, 2.0, c.data(), a.data());
+    lpm_ic_gaussians_add(d + L.vx, M.nv, c.data(), a.data(), ng, r->r.gauss_width, d + L.vzeta);
+    lpm_ic_gaussians_add(d + L.fx, M.nf, c.data(), a.data(), ng, r->r.gauss_width, d + L.fzeta);
+  }
+}
+
+void prepLoop(lpm_bve_server* S) {
+  cudaSetDevice(S->dev.device);
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cvPrep.wait(lk, [&] {
+        if (S->stop) return true;
+        if (S->queued.empty() || !S->fatal.empty()) return false;
+        const Req* h = S->queued.front();
+        return S->reserved + h->est <= S->budget && (S->maxActive <= 0 || S->inflight < S->maxActive);
+      });
+      if (S->stop) return;
+      r = S->queued.front();
+      S->queued.pop_front();
+      r->state = LPM_REQ_PREPARING;
+      S->reserved += r->est;
+      S->inflight += 1;
+    }
+    try {
+      prepare(S, r);
+      std::lock_guard<std::mutex> lk(S->mu);
+      if (!S->fatal.empty()) {
+        r->mesh.reset();
+        failLocked(S, r, "server stopped after a device error: " + S->fatal);
+        continue;
+      }
+      S->prepared.push_back(r);
+      S->cvGpu.notify_one();
+    } catch (const Error& e) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      r->mesh.reset();
+      failLocked(S, r, e.msg);
+    } catch (const std::bad_alloc&) {
+      std::lock_guard<std::mutex> lk(S->mu);
+      r->mesh.reset();
+      failLocked(S, r, "host memory exhausted while preparing the request");
+    }
+  }
+}
+
+// Uploads a prepared request and builds its plan (upload stream; stream-ordered allocation).
+void setupSolve(lpm_bve_server* S, Req* r) {
+  const MeshHost& M = *r->mesh;
+  r->nv = M.nv;
+  r->nf = M.nf;
+  const Layout L(M.nv, M.nf);
+  r->mem.streamOrdered(S->up, S->compute, S->pool);
+  r->dev = r->mem.alloc<char>(L.bytes);
+  LPM_CUDA(cudaMemcpyAsync(r->dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, S->up));
+  double* d = reinterpret_cast<double*>(r->dev);
+  ParticleIO io;
+  io.na = M.nv;
+  io.nb = M.nf;
+  io.ax = DVec{d + L.vx, 3, 1};
+  io.au = DVec{d + L.vvel, 3, 1};
+  io.azeta = d + L.vzeta;
+  io.bx = DVec{d + L.fx, 3, 1};
+  io.bu = DVec{d + L.fvel, 3, 1};
+  io.bzeta = d + L.fzeta;
+  io.barea = d + L.farea;
+  const uint8_t* mask = reinterpret_cast<const uint8_t*>(r->dev + L.maskByte);
+  r->plan.reset(new SolvePlan());
+  r->plan->mem.streamOrdered(S->up, S->compute, S->pool);
+  buildSolve(*r->plan, Mode::RK4, S->prec, io, mask, S->skip, true, S->eps, S->shape.tileSize(), M.plan, S->up);
+  r->plan->stage.dt = r->r.dt;
+  r->plan->stage.omega = r->r.omega;
+  r->pairsPerEval = (double)r->plan->nslots * r->plan->ns;
+}
+
+std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs) {
+  auto B = std::make_unique<Batch>();
+  B->prec = S->prec;
+  B->shape = S->shape;
+  B->rk4 = true;
+  B->rcpApprox = S->rcp;
+  B->mem.streamOrdered(S->up, S->compute, S->pool);
+  for (Req* r : rs) B->solves.push_back(r->plan.get());
+  finalizeBatch(*B, S->dev, S->up);
+  return B;
+}
+
+void captureStep(lpm_bve_server* S, Batch& B) {
+  cudaGraph_t g = nullptr;
+  LPM_CUDA(cudaStreamBeginCapture(S->cap, cudaStreamCaptureModeThreadLocal));
+  try {
+    enqueueStep(B, S->quirk, S->renorm, S->cap);
+  } catch (...) {
+    cudaStreamEndCapture(S->cap, &g);
+    if (g) cudaGraphDestroy(g);
+    throw;
+  }
+  LPM_CUDA(cudaStreamEndCapture(S->cap, &g));
+  const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
+  cudaGraphDestroy(g);
+  LPM_CUDA(ie);
+}
+
+// Queues the copy of a finished solve's state into its pinned buffer, frees its device memory
+// in stream order and hands it to the completion thread.
+void finish(lpm_bve_server* S, Req* r) {
+  const Layout L(r->nv, r->nf);
+  LPM_CUDA(cudaMemcpyAsync(r->host, r->dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, S->compute));
+  LPM_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming | cudaEventBlockingSync));
+  LPM_CUDA(cudaEventRecord(r->done, S->compute));
+  r->plan.reset();
+  r->mem.release();
+  r->dev = nullptr;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->completing.push_back(r);
+  S->cvComp.notify_one();
+}
+
+// Size classes.  Solves are grouped by cost (log4 of target-source pairs per evaluation);
+// each class is one batch with its own captured step.  Per iteration the most expensive
+// class takes one step and every other class takes as many steps as fit in a share of that
+// step's time (measured per class, moving average), capped by the fewest steps any of its
+// solves has left.  A small request therefore finishes within one or two iterations of a
+// large one instead of one step per large-solve step, and the large solve's iteration grows by
+// at most kSmallShare of its step time.
+constexpr double kSmallShare = 1.0;
+constexpr int kMaxStepsPerIteration = 256;
+
+struct SizeClass {
+  std::vector<Req*> solves;
+  std::unique_ptr<Batch> batch;
+  bool changed = false;
+  double msPerStep = -1.0;  // moving average of measured step time (-1: not measured yet)
+  double pairsPerStep = 0.0;
+};
+
+struct StepTiming {  // events around one class's launches in one iteration
+  int cls;
+  int64_t iter;
+  int steps;
+  cudaEvent_t e0, e1;
+};
+
+int costClass(double pairsPerEval) {
+  int c = 0;
+  while (pairsPerEval >= 4.0 && c < 40) {
+    pairsPerEval /= 4.0;
+    ++c;
+  }
+  return c;
+}
+
+// Step time of a class before it has been measured: 4 evaluations at a nominal pair rate plus
+// the 13 launches of a graph-replayed step.
+double modelMs(const lpm_bve_server* S, double pairsPerStep) {
+  const double rate = S->prec == Precision::FP32C ? 1.6e12 : 1.2e10;
+  return pairsPerStep / rate * 1e3 + 0.06;
+}
+
+void gpuLoop(lpm_bve_server* S) {
+  cudaSetDevice(S->dev.device);
+  std::map<int, SizeClass> classes;  // key: cost class
+  int nActive = 0;
+  cudaEvent_t stepEv[2] = {nullptr, nullptr};
+  cudaEvent_t upEv = nullptr;
+  std::vector<cudaEvent_t> evPool;
+  std::deque<StepTiming> timings;
+  int64_t iter = 0;
+  Clock::time_point tick = Clock::now();
+  auto getEvent = [&]() {
+    if (!evPool.empty()) {
+      cudaEvent_t e = evPool.back();
+      evPool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    LPM_CUDA(cudaEventCreate(&e));
+    return e;
+  };
+  auto allActive = [&]() {
+    std::vector<Req*> v;
+    for (auto& kv : classes) v.insert(v.end(), kv.second.solves.begin(), kv.second.solves.end());
+    return v;
+  };
+  try {
+    for (auto& e : stepEv) LPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
+    LPM_CUDA(cudaEventCreateWithFlags(&upEv, cudaEventDisableTiming));
+    for (;;) {
+      std::vector<Req*> joiners;
+      {
+        std::unique_lock<std::mutex> lk(S->mu);
+        if (nActive == 0) S->cvGpu.wait(lk, [&] { return S->stop || !S->prepared.empty(); });
+        if (S->stop) break;
+        joiners.assign(S->prepared.begin(), S->prepared.end());
+        S->prepared.clear();
+        const Clock::time_point now = Clock::now();
+        if (nActive > 0) S->st.busy_s += seconds(tick, now);
+        tick = now;
+      }
+      // 1. upload the newcomers (a failure that leaves the context usable fails the request only)
+      std::vector<Req*> ok;
+      for (Req* r : joiners) {
+        try {
+          setupSolve(S, r);
+          ok.push_back(r);
+        } catch (const Error& e) {
+          if (e.code == LPM_ERR_CUDA) throw;
+          cudaStreamSynchronize(S->up);  // copies into the request's memory may be queued
+          r->plan.reset();
+          r->mem.release();
+          std::lock_guard<std::mutex> lk(S->mu);
+          failLocked(S, r, e.msg);
+        }
+        r->mesh.reset();
+      }
+      std::unique_ptr<Batch> init;
+      if (!ok.empty()) init = makeBatch(S, ok);  // initial velocity of the newcomers
+      std::vector<Req*> noSteps;
+      for (Req* r : ok) {
+        if (r->r.nsteps > 0) {
+          SizeClass& C = classes[costClass(r->pairsPerEval)];
+          C.solves.push_back(r);
+          C.changed = true;
+          ++nActive;
+        } else {
+          noSteps.push_back(r);
+        }
+      }
+      for (auto it = classes.begin(); it != classes.end();) {
+        SizeClass& C = it->second;
+        if (C.changed) {
+          C.batch.reset();  // an in-flight graph is freed when it completes; tables in stream order
+          C.pairsPerStep = 0.0;
+          for (Req* r : C.solves) C.pairsPerStep += 4.0 * r->pairsPerEval;
+          if (!C.solves.empty()) {
+            C.batch = makeBatch(S, C.solves);
+            captureStep(S, *C.batch);
+          }
+          C.changed = false;
+        }
+        if (C.solves.empty()) it = classes.erase(it);
+        else ++it;
+      }
+      LPM_CUDA(cudaEventRecord(upEv, S->up));
+      LPM_CUDA(cudaStreamWaitEvent(S->compute, upEv, 0));
+      if (init) {
+        enqueueEval(*init, 0, 0, false, true, S->compute);
+        init.reset();
+      }
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        const Clock::time_point now = Clock::now();
+        for (Req* r : ok) {
+          r->state = LPM_REQ_RUNNING;
+          r->tStart = now;
+          S->st.pairs += r->pairsPerEval;
+        }
+        S->st.max_running_seen = std::max<int>(S->st.max_running_seen, nActive);
+      }
+      for (Req* r : noSteps) finish(S, r);
+      // 2. RK4 steps: the dominant class one, the others as many as their share allows
+      if (!classes.empty()) {
+        auto est = [&](const SizeClass& C) { return C.msPerStep > 0 ? C.msPerStep : modelMs(S, C.pairsPerStep); };
+        int dom = classes.begin()->first;
+        for (auto& kv : classes)
+          if (est(kv.second) > est(classes[dom])) dom = kv.first;
+        const double domMs = est(classes[dom]);
+        const int others = (int)classes.size() - 1;
+        double pairs = 0.0;
+        int64_t solveSteps = 0;
+        for (auto it = classes.begin(); it != classes.end(); ++it) {  // cheapest first: small results leave early
+          SizeClass& C = it->second;
+          int left = INT_MAX;
+          for (Req* r : C.solves) left = std::min(left, r->r.nsteps - r->stepsDone);
+          int k = 1;
+          if (it->first != dom && others > 0)
+            k = (int)std::floor(kSmallShare * domMs / (others * est(C)));
+          k = std::max(1, std::min({k, left, kMaxStepsPerIteration}));
+          StepTiming T{it->first, iter, k, getEvent(), getEvent()};
+          LPM_CUDA(cudaEventRecord(T.e0, S->compute));
+          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(C.batch->graph, S->compute));
+          LPM_CUDA(cudaEventRecord(T.e1, S->compute));
+          timings.push_back(T);
+          std::vector<Req*> still;
+          for (Req* r : C.solves) {
+            r->stepsDone += k;
+            pairs += 4.0 * k * r->pairsPerEval;
+            solveSteps += k;
+            if (r->stepsDone >= r->r.nsteps) {
+              finish(S, r);
+              C.changed = true;
+              --nActive;
+            } else {
+              still.push_back(r);
+            }
+          }
+          C.solves.swap(still);
+          if (C.changed) C.batch.reset();
+        }
+        std::lock_guard<std::mutex> lk(S->mu);
+        S->st.steps_run += 1;
+        S->st.solve_steps += solveSteps;
+        S->st.pairs += pairs;
+      }
+      // 3. pacing: at most two iterations in flight; then fold in the finished iterations' timings
+      LPM_CUDA(cudaEventRecord(stepEv[iter & 1], S->compute));
+      if (iter > 0) LPM_CUDA(cudaEventSynchronize(stepEv[(iter - 1) & 1]));
+      while (!timings.empty() && timings.front().iter < iter) {
+        StepTiming T = timings.front();
+        timings.pop_front();
+        float ms = 0.f;
+        LPM_CUDA(cudaEventElapsedTime(&ms, T.e0, T.e1));
+        auto it = classes.find(T.cls);
+        if (it != classes.end()) {
+          const double per = ms / T.steps;
+          it->second.msPerStep = it->second.msPerStep > 0 ? 0.5 * (it->second.msPerStep + per) : per;
+        }
+        evPool.push_back(T.e0);
+        evPool.push_back(T.e1);
+      }
+      ++iter;
+    }
+  } catch (const Error& e) {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->fatal = e.msg;
+    for (Req* r : allActive()) failLocked(S, r, "server stopped: " + e.msg);
+    for (Req* r : S->prepared) failLocked(S, r, "server stopped: " + e.msg);
+    for (Req* r : S->queued) failLocked(S, r, "server stopped: " + e.msg);
+    S->prepared.clear();
+    S->queued.clear();
+    S->cvDone.notify_all();
+  }
+  const std::vector<Req*> active = allActive();
+  for (auto& kv : classes) kv.second.batch.reset();
+  cudaStreamSynchronize(S->compute);
+  cudaStreamSynchronize(S->up);
+  for (Req* r : active) {  // abandoned at shutdown
+    r->plan.reset();
+    r->mem.release();
+  }
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    for (Req* r : active) failLocked(S, r, "server destroyed while the request was running");
+  }
+  for (auto& T : timings) {
+    cudaEventDestroy(T.e0);
+    cudaEventDestroy(T.e1);
+  }
+  for (cudaEvent_t e : evPool) cudaEventDestroy(e);
+  for (auto& e : stepEv)
+    if (e) cudaEventDestroy(e);
+  if (upEv) cudaEventDestroy(upEv);
+}
+
+void completionLoop(lpm_bve_server* S) {
+  cudaSetDevice(S->dev.device);
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cvComp.wait(lk, [&] { return S->compStop || !S->completing.empty(); });
+      if (S->completing.empty()) return;
+      r = S->completing.front();
+      S->completing.pop_front();
+    }
+    const cudaError_t e = cudaEventSynchronize(r->done);
+    cudaEventDestroy(r->done);
+    r->done = nullptr;
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (e != cudaSuccess) {
+      if (S->fatal.empty()) S->fatal = cudaGetErrorString(e);
+      failLocked(S, r, std::string("device error: ") + cudaGetErrorString(e));
+      continue;
+    }
+    r->state = LPM_REQ_DONE;
+    r->tDone = Clock::now();
+    S->reserved -= r->est;
+    S->inflight -= 1;
+    S->st.completed += 1;
+    S->latencies.push_back(seconds(r->tSubmit, r->tDone));
+    S->cvDone.notify_all();
+    S->cvPrep.notify_all();
+  }
+}
+
+Req* findLocked(lpm_bve_server* S, int64_t id) {
+  auto it = S->reqs.find(id);
+  return it == S->reqs.end() ? nullptr : it->second.get();
+}
+
+}  // namespace
+}  // namespace server
+}  // namespace lpm
+
+extern "C" {
+
+int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out) {
+  if (!out) return LPM_ERR_INVALID_ARGUMENT;
+  *out = nullptr;
+  auto S = std::make_unique<lpm_bve_server>();
+  try {
+    int dev = opts ? opts->device : -1;
+    if (dev < 0) LPM_CUDA(cudaGetDevice(&dev));
+    LPM_CUDA(cudaSetDevice(dev));
+    S->dev.device = dev;
+    LPM_CUDA(cudaDeviceGetAttribute(&S->dev.sms, cudaDevAttrMultiProcessorCount, dev));
+    int major = 0, minor = 0;
+    LPM_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
+    LPM_CUDA(cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev));
+    if (major != 10 || minor != 3)
+      fail(LPM_ERR_NOT_SUPPORTED, "device %d is sm_%d%d; this library is built for sm_103a (GB300) only", dev, major,
+           minor);
+    const unsigned flags = opts ? opts->flags : LPM_BVE_FP32C;
+    const double eps = opts ? opts->eps : 0.0;
+    if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "server: eps must be finite and >= 0");
+    S->flags = flags;
+    S->prec = (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64;
+    S->shape = S->prec == Precision::FP32C ? kDefaultFP32C : kFP64Shape;
+    S->eps = eps;
+    S->skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
+    S->quirk = !(flags & LPM_BVE_RK4_FIX_QUIRK);
+    S->renorm = flags & LPM_BVE_RENORM;
+    S->rcp = flags & LPM_BVE_RCP_APPROX;
+    S->maxActive = opts ? opts->max_active : 0;
+    size_t freeB = 0, totalB = 0;
+    LPM_CUDA(cudaMemGetInfo(&freeB, &totalB));
+    S->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : freeB / 10 * 8;
+    S->st.budget_bytes = S->budget;
+    LPM_CUDA(cudaStreamCreateWithFlags(&S->up, cudaStreamNonBlocking));
+    LPM_CUDA(cudaStreamCreateWithFlags(&S->compute, cudaStreamNonBlocking));
+    LPM_CUDA(cudaStreamCreateWithFlags(&S->cap, cudaStreamNonBlocking));
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    LPM_CUDA(cudaMemPoolCreate(&S->pool, &props));
+    uint64_t keep = UINT64_MAX;  // keep freed blocks for the next requests
+    LPM_CUDA(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  } catch (const Error& e) {
+    std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.msg.c_str());
+    if (S->pool) cudaMemPoolDestroy(S->pool);
+    for (cudaStream_t s : {S->up, S->compute, S->cap})
+      if (s) cudaStreamDestroy(s);
+    return e.code;
+  }
+  lpm_bve_server* raw = S.release();
+  raw->prepT = std::thread(prepLoop, raw);
+  raw->gpuT = std::thread(gpuLoop, raw);
+  raw->compT = std::thread(completionLoop, raw);
+  *out = raw;
+  return LPM_OK;
+}
+
+int lpm_bve_server_submit(lpm_bve_server* S, const lpm_bve_request* req, int64_t* id) {
+  if (!S || !req) return LPM_ERR_INVALID_ARGUMENT;
+  const lpm_bve_request& q = *req;
+  const std::string bad = validate(q);
+  if (!bad.empty()) return setErr(S, LPM_ERR_INVALID_ARGUMENT, "submit: " + bad);
+  int64_t nv = 0, nf = 0, nl = 0;
+  lpm_mesh_counts(q.seed, q.level, &nv, &nf, &nl);
+  auto r = std::make_unique<Req>();
+  r->r = q;
+  r->nv = nv;
+  r->nf = nf;
+  r->nl = nl;
+  r->est = estimateBytes(S->prec, S->shape, S->skip, nv, nf, nl);
+  r->tSubmit = Clock::now();
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (!S->fatal.empty()) {
+    S->err = "server stopped after a device error: " + S->fatal;
+    return LPM_ERR_CUDA;
+  }
+  if (r->est > S->budget) {
+    char buf[192];
+    std::snprintf(buf, sizeof(buf), "submit: request needs about %zu bytes, the HBM budget is %zu", r->est, S->budget);
+    S->err = buf;
+    return LPM_ERR_ADMISSION;
+  }
+  r->id = S->nextId++;
+  if (id) *id = r->id;
+  S->queued.push_back(r.get());
+  S->reqs[r->id] = std::move(r);
+  S->st.submitted += 1;
+  S->cvPrep.notify_one();
+  return LPM_OK;
+}
+
+int lpm_bve_server_estimate(const lpm_bve_server_opts* opts, const lpm_bve_request* req, size_t* bytes) {
+  if (!req || !bytes) return LPM_ERR_INVALID_ARGUMENT;
+  if (!validate(*req).empty()) return LPM_ERR_INVALID_ARGUMENT;
+  const unsigned flags = opts ? opts->flags : LPM_BVE_FP32C;
+  const Precision prec = (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64;
+  int64_t nv = 0, nf = 0, nl = 0;
+  lpm_mesh_counts(req->seed, req->level, &nv, &nf, &nl);
+  *bytes = estimateBytes(prec, prec == Precision::FP32C ? kDefaultFP32C : kFP64Shape,
+                         flags & LPM_BVE_SKIP_MASKED_TARGETS, nv, nf, nl);
+  return LPM_OK;
+}
+
+int lpm_bve_server_wait(lpm_bve_server* S, int64_t id, double timeout_s) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  std::unique_lock<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r) {
+    S->err = "wait: unknown request id";
+    return LPM_ERR_STATE;
+  }
+  auto finished = [&] { return r->state == LPM_REQ_DONE || r->state == LPM_REQ_FAILED || r->state == LPM_REQ_CANCELLED; };
+  if (timeout_s < 0) {
+    S->cvDone.wait(lk, finished);
+  } else if (!S->cvDone.wait_for(lk, std::chrono::duration<double>(timeout_s), finished)) {
+    return LPM_ERR_TIMEOUT;
+  }
+  if (r->state != LPM_REQ_DONE) {
+    S->err = r->state == LPM_REQ_CANCELLED ? "request was cancelled" : "request failed: " + r->err;
+    return LPM_ERR_STATE;
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_server_status(lpm_bve_server* S, int64_t id, int* state) {
+  if (!S || !state) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r) return LPM_ERR_STATE;
+  *state = r->state;
+  return LPM_OK;
+}
+
+int lpm_bve_server_cancel(lpm_bve_server* S, int64_t id) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r || r->state != LPM_REQ_QUEUED) {
+    S->err = "cancel: only a request still waiting for admission can be cancelled";
+    return LPM_ERR_STATE;
+  }
+  S->queued.erase(std::find(S->queued.begin(), S->queued.end(), r));
+  r->state = LPM_REQ_CANCELLED;
+  r->tDone = Clock::now();
+  S->st.cancelled += 1;
+  S->cvDone.notify_all();
+  S->cvPrep.notify_all();
+  return LPM_OK;
+}
+
+int lpm_bve_server_result(lpm_bve_server* S, int64_t id, int64_t* nverts, int64_t* nfaces, double* vx, double* vzeta,
+                          double* vvel, double* fx, double* fzeta, double* fvel) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r) {
+    S->err = "result: unknown request id";
+    return LPM_ERR_STATE;
+  }
+  if (nverts) *nverts = r->nv;
+  if (nfaces) *nfaces = r->nf;
+  if (!vx && !vzeta && !vvel && !fx && !fzeta && !fvel) return LPM_OK;
+  if (r->state != LPM_REQ_DONE || !r->host) {
+    S->err = "result: request has not finished (or was released)";
+    return LPM_ERR_STATE;
+  }
+  const Layout L(r->nv, r->nf);
+  const double* d = reinterpret_cast<const double*>(r->host);
+  auto put = [](double* dst, const double* src, size_t n) {
+    if (dst) std::memcpy(dst, src, n * sizeof(double));
+  };
+  put(vx, d + L.vx, 3 * (size_t)r->nv);
+  put(vvel, d + L.vvel, 3 * (size_t)r->nv);
+  put(vzeta, d + L.vzeta, (size_t)r->nv);
+  put(fx, d + L.fx, 3 * (size_t)r->nf);
+  put(fvel, d + L.fvel, 3 * (size_t)r->nf);
+  put(fzeta, d + L.fzeta, (size_t)r->nf);
+  return LPM_OK;
+}
+
+int lpm_bve_server_release(lpm_bve_server* S, int64_t id) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  std::unique_ptr<Req> r;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    auto it = S->reqs.find(id);
+    if (it == S->reqs.end()) return LPM_ERR_STATE;
+    const int st = it->second->state;
+    if (st != LPM_REQ_DONE && st != LPM_REQ_FAILED && st != LPM_REQ_CANCELLED) {
+      S->err = "release: request has not finished";
+      return LPM_ERR_STATE;
+    }
+    r = std::move(it->second);
+    S->reqs.erase(it);
+  }
+  if (r->host) cudaFreeHost(r->host);
+  return LPM_OK;
+}
+
+int lpm_bve_server_timing(lpm_bve_server* S, int64_t id, double* total_s, double* wait_s, double* run_s) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r || r->state != LPM_REQ_DONE) return LPM_ERR_STATE;
+  if (total_s) *total_s = seconds(r->tSubmit, r->tDone);
+  if (wait_s) *wait_s = seconds(r->tSubmit, r->tStart);
+  if (run_s) *run_s = seconds(r->tStart, r->tDone);
+  return LPM_OK;
+}
+
+int lpm_bve_server_latency(lpm_bve_server* S, const double* q, int nq, double* out) {
+  if (!S || (nq > 0 && (!q || !out))) return LPM_ERR_INVALID_ARGUMENT;
+  std::vector<double> v;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    v = S->latencies;
+  }
+  if (v.empty()) return LPM_ERR_STATE;
+  std::sort(v.begin(), v.end());
+  for (int i = 0; i < nq; ++i) {  // nearest-rank quantile
+    if (!(q[i] >= 0.0 && q[i] <= 1.0)) return LPM_ERR_INVALID_ARGUMENT;
+    const size_t k = (size_t)std::ceil(q[i] * (double)v.size());
+    out[i] = v[k == 0 ? 0 : k - 1];
+  }
+  return LPM_OK;
+}
+
+int lpm_bve_server_stats(lpm_bve_server* S, lpm_bve_server_counters* out) {
+  if (!S || !out) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  *out = S->st;
+  out->queued = (int64_t)S->queued.size();
+  int64_t running = 0;
+  for (auto& kv : S->reqs) running += kv.second->state == LPM_REQ_RUNNING;
+  out->running = running;
+  out->reserved_bytes = S->reserved;
+  out->budget_bytes = S->budget;
+  return LPM_OK;
+}
+
+const char* lpm_bve_server_last_error(lpm_bve_server* S) { return S ? S->err.c_str() : "null server"; }
+
+int lpm_bve_server_destroy(lpm_bve_server* S) {
+  if (!S) return LPM_ERR_INVALID_ARGUMENT;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->stop = true;
+  }
+  S->cvPrep.notify_all();
+  S->cvGpu.notify_all();
+  if (S->prepT.joinable()) S->prepT.join();
+  if (S->gpuT.joinable()) S->gpuT.join();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->compStop = true;
+  }
+  S->cvComp.notify_all();
+  if (S->compT.joinable()) S->compT.join();
+  cudaSetDevice(S->dev.device);
+  cudaStreamSynchronize(S->compute);
+  cudaStreamSynchronize(S->up);
+  for (auto& kv : S->reqs) {
+    kv.second->plan.reset();
+    kv.second->mem.release();
+  }
+  cudaStreamSynchronize(S->compute);
+  for (auto& kv : S->reqs)
+    if (kv.second->host) cudaFreeHost(kv.second->host);
+  S->reqs.clear();
+  cudaMemPoolDestroy(S->pool);
+  cudaStreamDestroy(S->up);
+  cudaStreamDestroy(S->compute);
+  cudaStreamDestroy(S->cap);
+  delete S;
+  return LPM_OK;
+}
+
+}  // extern "C"

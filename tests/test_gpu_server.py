@@ -1,0 +1,137 @@
+"""Continuous-batching server (include/lpm_bve_server.h) through the C ABI.
+
+  * a request's final state is bitwise the same run alone and run in a mix of requests of
+    other sizes that arrive while it runs (per-solve summation order is fixed);
+  * in FP64 the server's result is bitwise the single-solve path's: BVESphere initial
+    condition + velocity, then lpm_bve_rk4_step (itself pinned to the oracle at 1e-12);
+  * a request with zero steps returns the initial state with its velocity;
+  * the HBM budget admits one request at a time when only one fits, rejects a request that
+    can never fit, and a queued request can be cancelled;
+  * invalid requests are rejected; stats and latency quantiles are consistent.
+"""
+import math
+import time
+
+import numpy as np
+import pytest
+import torch
+
+import lpmkokkos_gb300 as P
+from lpmkokkos_gb300 import _lib as L
+from lpmkokkos_gb300 import bve
+
+pytestmark = pytest.mark.gpu
+
+OMEGA = 2 * math.pi
+KEYS = ("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")
+WAIT = 600.0
+
+
+def _same(a, b):
+    return np.array_equal(a, b, equal_nan=True)
+
+
+def _alone(flags, spec):
+    with bve.Server(0, flags=flags) as srv:
+        rid = srv.submit(**spec)
+        assert srv.wait(rid, WAIT)
+        return srv.result(rid)
+
+
+@pytest.mark.parametrize("flags", [P.FP32C, P.FP64])
+def test_same_result_alone_and_in_the_mix(flags):
+    torch.cuda.set_device(0)
+    a_spec = dict(seed=0, level=4, dt=0.005, nsteps=5, ic_seed=7)
+    b_spec = dict(seed=1, level=5, dt=0.0025, nsteps=3, ic_seed=8)
+    alone_a, alone_b = _alone(flags, a_spec), _alone(flags, b_spec)
+    long_level = 6 if flags == P.FP32C else 5  # FP64 pairs run at 1/64 of the FP32 rate
+    with bve.Server(0, flags=flags) as srv:
+        long_run = srv.submit(seed=0, level=long_level, dt=0.0025, nsteps=12, ic_seed=1)
+        small = [srv.submit(seed=1, level=3, dt=0.01, nsteps=2 + s, ic_seed=s) for s in range(4)]
+        time.sleep(0.05)
+        a = srv.submit(**a_spec)
+        time.sleep(0.02)
+        b = srv.submit(**b_spec)
+        late = [srv.submit(seed=0, level=5, dt=0.005, nsteps=2, ic_seed=10 + s) for s in range(3)]
+        for rid in (long_run, a, b, *small, *late):
+            assert srv.wait(rid, WAIT)
+        st = srv.stats()
+        got_a, got_b = srv.result(a), srv.result(b)
+        # size classes: the small requests step several times per step of the long one
+        small_done = max(srv.timing(r)["total_s"] for r in small)
+        long_done = srv.timing(long_run)["total_s"]
+    assert st["completed"] == 10 and st["failed"] == 0
+    assert small_done < long_done, (small_done, long_done)
+    assert st["max_running_seen"] >= 3, st  # the requests really shared launches
+    for k in KEYS:
+        assert _same(got_a[k], alone_a[k]), k
+        assert _same(got_b[k], alone_b[k]), k
+    leaf = bve.build_mesh(0, 4)["fmask"] == 0
+    assert np.isfinite(got_a["fx"][leaf]).all() and np.isfinite(got_a["vvel"]).all()
+
+
+def test_fp64_server_matches_single_solve_path(ctx):
+    torch.cuda.set_device(0)
+    seed, level, dt, nsteps, ic_seed, ng, width = 0, 3, 0.01, 3, 5, 3, 0.1
+    with bve.Server(0, flags=P.FP64) as srv:
+        r0 = srv.submit(seed, level, dt, 0, ic_seed=ic_seed, n_gaussians=ng, gauss_width=width)
+        r3 = srv.submit(seed, level, dt, nsteps, ic_seed=ic_seed, n_gaussians=ng, gauss_width=width)
+        assert srv.wait(r0, WAIT) and srv.wait(r3, WAIT)
+        init, got = srv.result(r0), srv.result(r3)
+    s = bve.BVESphere(seed, level)
+    s.init_vorticity(bve.rh54_gaussians(ic_seed, ng, width), ctx, flags=P.FP64)
+    torch.cuda.synchronize()
+    ref0 = dict(vx=s.physVerts, vzeta=s.relVortVerts, vvel=s.velocityVerts, fx=s.physFaces, fzeta=s.relVortFaces,
+                fvel=s.velocityFaces)
+    ref0 = {k: v.cpu().numpy() for k, v in ref0.items()}
+    for k in KEYS:
+        assert _same(init[k], ref0[k]), k
+    ctx.rk4_step(s.state(), dt, OMEGA, nsteps, flags=P.FP64)
+    torch.cuda.synchronize()
+    ref = dict(vx=s.physVerts, vzeta=s.relVortVerts, vvel=s.velocityVerts, fx=s.physFaces, fzeta=s.relVortFaces,
+               fvel=s.velocityFaces)
+    for k in KEYS:
+        assert _same(got[k], ref[k].cpu().numpy()), k
+
+
+def test_budget_admission_and_cancel():
+    torch.cuda.set_device(0)
+    one = bve.server_estimate(1, 4)
+    with bve.Server(0, budget_bytes=int(one * 1.5)) as srv:
+        with pytest.raises(L.LpmError) as e:
+            srv.submit(1, 6, 0.0025, 1)
+        assert e.value.code == L.LPM_ERR_ADMISSION
+        ids = [srv.submit(1, 4, 0.005, 4, ic_seed=s) for s in range(3)]
+        last = srv.submit(1, 4, 0.005, 4, ic_seed=99)
+        srv.cancel(last)
+        assert srv.status(last) == L.REQ_CANCELLED
+        with pytest.raises(L.LpmError):
+            srv.wait(last, 1.0)
+        for rid in ids:
+            assert srv.wait(rid, WAIT)
+        st = srv.stats()
+        assert st["completed"] == 3 and st["cancelled"] == 1 and st["max_running_seen"] == 1
+        assert st["reserved_bytes"] == 0
+        p50, p99 = srv.latency([0.5, 0.99])
+        assert 0 < p50 <= p99
+        t = srv.timing(ids[-1])
+        assert t["total_s"] >= t["run_s"] > 0 and t["wait_s"] >= 0
+        srv.release(ids[0])
+        with pytest.raises(L.LpmError):
+            srv.result(ids[0])
+
+
+def test_invalid_requests_rejected():
+    torch.cuda.set_device(0)
+    with bve.Server(0) as srv:
+        for bad in (dict(seed=2, level=3, dt=0.01, nsteps=1), dict(seed=0, level=11, dt=0.01, nsteps=1),
+                    dict(seed=0, level=3, dt=float("nan"), nsteps=1), dict(seed=0, level=3, dt=0.01, nsteps=-1),
+                    dict(seed=0, level=3, dt=0.01, nsteps=1, n_gaussians=2, gauss_width=0.0)):
+            with pytest.raises(L.LpmError) as e:
+                srv.submit(**bad)
+            assert e.value.code == L.LPM_ERR_INVALID_ARGUMENT
+        with pytest.raises(L.LpmError):
+            srv.wait(12345, 0.1)
+        rid = srv.submit(0, 3, 0.01, 1)
+        assert srv.wait(rid, WAIT)
+        assert srv.stats()["submitted"] == 1

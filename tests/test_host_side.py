@@ -86,3 +86,31 @@ def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError):
         _lib.lib()
+
+
+def test_server_footprint_estimate(native):
+    """The server's admission figure (host-only): grows ~4x per level, FP64 stores one packed
+    source record instead of two, invalid requests are rejected."""
+    from lpmkokkos_gb300 import _lib as L
+    from lpmkokkos_gb300 import bve
+    est = [bve.server_estimate(0, lv) for lv in range(4, 9)]
+    ratios = [b / a for a, b in zip(est, est[1:])]
+    assert all(3.5 < r < 4.5 for r in ratios), ratios
+    nv, nf, nl = bve.mesh_counts(0, 7)
+    state = 8 * (7 * nv + 8 * nf) + nf
+    assert state < est[3] < 16 * state  # plan: chunk partials and RK4 increments per target slot
+    assert bve.server_estimate(0, 7, flags=L.FP64) < est[3]
+    with pytest.raises(L.LpmError):
+        bve.server_estimate(0, 11)
+
+
+def test_server_create_fails_cleanly_without_gpu(native):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from lpmkokkos_gb300 import _lib as L
+    lib = L.lib()
+    h = ctypes.c_void_p()
+    opts = L.ServerOpts(0, 0, 0, L.FP32C, 0.0)
+    assert lib.lpm_bve_server_create(ctypes.byref(opts), ctypes.byref(h)) != L.LPM_OK
+    assert not h.value
