@@ -49,6 +49,19 @@ def time_step(level: int) -> float:
 OPS_PER_PAIR = 13  # FP32 FMA-pipe lane operations per velocity pair in the FP32C kernel
 
 
+def fma_peak(P, device):
+    """Achievable FP32 FMA-pipe rate in lane-ops/s at the current clock: the larger of the
+    scalar-FFMA and paired-FFMA (f32x2) probes, with both figures."""
+    import ctypes
+    rates = {}
+    for name in ("lpm_probe_fp32_fma", "lpm_probe_fp32_fma2"):
+        r, ms = ctypes.c_double(), ctypes.c_double()
+        P._lib.check(getattr(P.lib(), name)(device, 200000, ctypes.byref(r), ctypes.byref(ms)))
+        rates[name] = r.value
+    return max(rates.values()), {"ffma_lane_ops_per_s": rates["lpm_probe_fp32_fma"],
+                                 "ffma2_lane_ops_per_s": rates["lpm_probe_fp32_fma2"]}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -58,6 +71,9 @@ def parse():
     ap.add_argument("--level", type=int, default=WORKLOAD["level"])
     ap.add_argument("--prec", choices=["fp32c", "fp64"], default="fp32c")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--err-steps", type=int, default=0,
+                    help="c2: also advance an FP64 trajectory beside an FP32C one for this many steps and report "
+                         "the per-step velocity/vorticity errors (device norms; FP64 is ~150x slower)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
@@ -66,8 +82,13 @@ def parse():
                          "c4: continuous-batching server under Poisson arrivals; "
                          "c5: icos L8, eps 0.01, 8 vortices, then the stream function at all targets")
     ap.add_argument("--requests", type=int, default=96, help="c4: number of requests")
-    ap.add_argument("--rate", type=float, default=8.0, help="c4: mean arrivals per second")
+    ap.add_argument("--rate", type=float, default=8.0, help="c4: mean arrivals per second (0: set by --util)")
+    ap.add_argument("--util", type=float, default=0.7, help="c4 with --rate 0: target device utilisation")
     ap.add_argument("--req-steps", type=int, default=10, help="c4: RK4 steps per request")
+    ap.add_argument("--levels", default="3-7", help="c4: mesh levels, e.g. 3-8")
+    ap.add_argument("--level-weights", default=".3,.3,.2,.15,.05",
+                    help="c4: comma-separated weights per level (empty: uniform)")
+    ap.add_argument("--kinds", choices=["both", "icos"], default="both", help="c4: mesh seeds")
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     return ap.parse_args()
 
@@ -185,10 +206,7 @@ def run_ours(args, rank, world, local_rank):
         return max_over_ranks(x, world, dev)
 
     # FP32 FMA-pipe peak at the current clock (roofline denominator)
-    import ctypes
-    r, ms = ctypes.c_double(), ctypes.c_double()
-    P._lib.check(P.lib().lpm_probe_fp32_fma(local_rank, 200000, ctypes.byref(r), ctypes.byref(ms)))
-    fma_peak_lane_ops = r.value
+    fma_peak_lane_ops, probes = fma_peak(P, local_rank)
 
     # warm-up: builds the plan and captures the step graph
     t0 = time.time()
@@ -298,7 +316,9 @@ def run_ours(args, rank, world, local_rank):
             "peak": peak_at_probe,
             "unit": "Gpair/s",
             "frac": achieved / peak_at_probe,
-            "peak_source": "FP32 FMA-pipe probe (independent FFMA chains, this run) / 13 lane-ops per pair",
+            "peak_source": "FP32 FMA-pipe probe (independent FFMA / FFMA2 chains, the larger, this run) "
+                           "/ 13 lane-ops per pair",
+            "probes": probes,
             "peak_nominal_2070MHz": peak_nominal,
             "frac_of_nominal": achieved / peak_nominal,
             "pair_launch_ms_avg": pair_avg_ms,
@@ -321,9 +341,47 @@ def run_ours(args, rank, world, local_rank):
     # 5) CPU baseline (rank 0, single GPU only)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
         out["cpu_baseline"] = cpu_baseline(sphere.state(), sphere, w, args, pairs_done)
+    # 6) per-step error of the FP32C trajectory against the FP64 one
+    if args.err_steps > 0 and rank == 0:
+        out["per_step_error"] = per_step_error(ctx, w, args.level, args.err_steps, dev, P, bve, torch)
     if rank == 0:
         print(json.dumps(out), flush=True)
     ctx.close()
+
+
+def per_step_error(ctx, w, level, nsteps, dev, P, bve, torch):
+    """FP64 and FP32C trajectories from the same initial state; after every RK4 step the
+    relative l2/linf of the FP32C velocity (vertices; leaf faces, area-weighted), relative
+    vorticity and face positions against FP64, reduced on the device (lpm_errnorms)."""
+    ic = bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"])
+    mesh = bve.build_mesh(w["seed_kind"], level)
+    runs = {}
+    for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C)):
+        s = bve.BVESphere(w["seed_kind"], level, omega=w["omega"], device=dev, mesh=mesh)
+        s.init_vorticity(ic, ctx, flags=flags, eps=w["eps"])
+        runs[name] = s
+    a, b = runs["fp64"], runs["fp32c"]
+    area, parents = a.faces_area, a.faces_mask
+
+    def norms():
+        uv = ctx.errnorms(b.velocityVerts, a.velocityVerts)
+        uf = ctx.errnorms(b.velocityFaces, a.velocityFaces, area, parents)
+        zf = ctx.errnorms(b.relVortFaces, a.relVortFaces, area, parents, abs_linf=True)
+        xf = ctx.errnorms(b.physFaces, a.physFaces, area, parents)
+        return {"u_verts_l2": uv[1], "u_verts_linf": uv[2], "u_faces_l2": uf[1], "u_faces_linf": uf[2],
+                "zeta_faces_l2": zf[1], "zeta_faces_linf": zf[2], "x_faces_l2": xf[1]}
+
+    rows = [dict(step=0, **norms())]
+    t0 = time.time()
+    for k in range(1, nsteps + 1):
+        ctx.rk4_step(a.state(), w["dt"], w["omega"], 1, flags=P.FP64, eps=w["eps"])
+        ctx.rk4_step(b.state(), w["dt"], w["omega"], 1, flags=P.FP32C, eps=w["eps"])
+        torch.cuda.synchronize()
+        rows.append(dict(step=k, **norms()))
+    return {"steps": nsteps, "seconds": time.time() - t0, "rows": rows,
+            "max_u_l2": max(max(r["u_verts_l2"], r["u_faces_l2"]) for r in rows),
+            "max_zeta_l2": max(r["zeta_faces_l2"] for r in rows),
+            "note": "leaf faces area-weighted, masked parent faces skipped; vertices unweighted"}
 
 
 def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step, eps=0.0):
@@ -510,12 +568,10 @@ def run_large(args, rank, world, local_rank):
     e1.record(stream)
     torch.cuda.synchronize()
     psi_ms = e0.elapsed_time(e1)
-    r, ms = __import__("ctypes").c_double(), __import__("ctypes").c_double()
-    P._lib.check(P.lib().lpm_probe_fp32_fma(local_rank, 200000, __import__("ctypes").byref(r),
-                                            __import__("ctypes").byref(ms)))
+    lane_ops, probes = fma_peak(P, local_rank)
     pairs_alg = (nv + nl) * nl
     achieved = pairs_alg / (pair_ms / pair_n * 1e-3) / 1e9
-    peak = r.value / OPS_PER_PAIR / 1e9
+    peak = lane_ops / OPS_PER_PAIR / 1e9
     fp64 = fp64_sample(ctx, s, dict(WORKLOAD, level=level, dt=dt), P, torch, np, (nv + nall) * nl,
                        el / args.steps, eps=eps)
     out = {
@@ -530,7 +586,8 @@ def run_large(args, rank, world, local_rank):
         "psi_and_velocity_all_targets_ms": psi_ms,
         "roofline": {"bound": "fp32_fma_pipe", "kernel": "pairFP32C", "achieved": achieved, "peak": peak,
                      "unit": "Gpair/s", "frac": achieved / peak, "pair_launch_ms_avg": pair_ms / pair_n,
-                     "peak_source": "FP32 FMA-pipe probe / 13 lane-ops per pair", "traffic": None},
+                     "peak_source": "FP32 FMA-pipe probe (FFMA / FFMA2, the larger) / 13 lane-ops per pair",
+                     "probes": probes, "traffic": None},
         "fp64_gpu": fp64, "init_s": t_init,
     }
     if rank == 0:
@@ -538,12 +595,26 @@ def run_large(args, rank, world, local_rank):
     ctx.close()
 
 
+COMPUTED_PAIR_RATE = 2.2e12  # FP32C pairs/s incl. masked-parent targets (measured, icos L7)
+
+
+def computed_pairs(seed_kind: int, level: int) -> int:
+    """Target-source pairs one evaluation computes: (vertices + all faces) x leaf faces."""
+    f0, v0 = (20, 10) if seed_kind == 0 else (6, 6)
+    nv = 2 + v0 * 4 ** level
+    nall = f0 * (4 ** (level + 1) - 1) // 3
+    return (nv + nall) * f0 * 4 ** level
+
+
 def run_server(args, rank, world, local_rank):
-    """Config 4: the continuous-batching server under Poisson arrivals.  Requests draw a mesh
-    uniformly from icosahedral / cubed-sphere and a level from 3-7 (weights .3 .3 .2 .15 .05),
-    RH54 + 3 seeded Gaussian vortices, dt at the level-4 Courant number, --req-steps RK4 steps
-    each.  Latency is submit-to-result on the host clock: host preparation, upload, queueing,
-    the steps and the copy back are all inside it."""
+    """Config 4: the continuous-batching server under Poisson arrivals.  Each request draws a
+    mesh seed (icosahedral, or icosahedral/cubed sphere with equal odds) and a level from
+    --levels (--level-weights), RH54 + 3 seeded Gaussian vortices, dt at the level-4 Courant
+    number, --req-steps RK4 steps.  The arrival rate is --rate, or with --rate 0 the rate that
+    loads the device to --util by the expected service time.  Latency is submit-to-result on the
+    host clock: host preparation, upload, queueing, the steps and the copy back are all inside.
+    Beside it: the same requests served one at a time by the plain FP64 GPU path, extrapolated
+    from its pair rate measured in this run."""
     import threading
 
     import numpy as np
@@ -554,17 +625,27 @@ def run_server(args, rank, world, local_rank):
     P.build()
     torch.cuda.set_device(local_rank)
     rng = np.random.default_rng(SEED_BASE + 4)
-    levels, weights = [3, 4, 5, 6, 7], [0.3, 0.3, 0.2, 0.15, 0.05]
+    lo, hi = (int(v) for v in args.levels.split("-"))
+    levels = list(range(lo, hi + 1))
+    weights = [float(v) for v in args.level_weights.split(",")] if args.level_weights else []
+    if len(weights) != len(levels):
+        weights = [1.0] * len(levels)
+    weights = np.asarray(weights) / np.sum(weights)
     n = args.requests
-    kinds = rng.integers(0, 2, size=n)
+    kinds = np.zeros(n, dtype=int) if args.kinds == "icos" else rng.integers(0, 2, size=n)
     lvls = rng.choice(levels, size=n, p=weights)
-    gaps = rng.exponential(1.0 / args.rate, size=n)
+    exp_service = sum(wt * args.req_steps * 4 * np.mean([computed_pairs(k, lv) for k in
+                                                          ((0,) if args.kinds == "icos" else (0, 1))])
+                      for lv, wt in zip(levels, weights)) / COMPUTED_PAIR_RATE
+    rate = args.rate if args.rate > 0 else args.util / exp_service
+    gaps = rng.exponential(1.0 / rate, size=n)
     arrivals = np.cumsum(gaps) - gaps[0]
     specs = [dict(seed=int(k), level=int(lv), dt=courant_dt(int(k), int(lv)), nsteps=args.req_steps,
                   ic_seed=SEED_BASE + 4 + i) for i, (k, lv) in enumerate(zip(kinds, lvls))]
     srv = bve.Server(local_rank, flags=P.FP32C)
     # warm-up: one zero-step request per mesh (fills the host mesh/plan cache, loads kernels)
-    warm = [srv.submit(seed=k, level=lv, dt=0.01, nsteps=0) for k in (0, 1) for lv in levels]
+    meshes = sorted({(s["seed"], s["level"]) for s in specs})
+    warm = [srv.submit(seed=k, level=lv, dt=0.01, nsteps=0) for k, lv in meshes]
     warm += [srv.submit(seed=0, level=4, dt=0.005, nsteps=2, ic_seed=s) for s in range(max(1, args.warmup))]
     for rid in warm:
         assert srv.wait(rid, 600.0)
@@ -586,7 +667,7 @@ def run_server(args, rank, world, local_rank):
     th.start()
     th.join()
     for rid in ids:
-        assert srv.wait(rid, 1800.0)
+        assert srv.wait(rid, 7200.0)
     wall = time.perf_counter() - t_start
     clocks = sampler.stop()
     st = srv.stats()
@@ -609,24 +690,47 @@ def run_server(args, rank, world, local_rank):
             assert alone.wait(rid, 600.0)
             ref = alone.result(rid)
             same &= all(np.array_equal(got[k], ref[k], equal_nan=True) for k in ref)
+    # plain FP64 GPU path, one request after another: its pair rate on a level-6 sample
+    ctx = bve.Context(local_rank)
+    s6 = bve.BVESphere(0, 6)
+    s6.init_vorticity(bve.rh54_gaussians(SEED_BASE + 4, 3), ctx, flags=P.FP32C)
+    tgt = s6.physVerts[:8192].contiguous()
+    src = (s6.physFaces, s6.relVortFaces, s6.faces_area, s6.faces_mask)
+    ctx.velocity(tgt, *src, flags=P.FP64)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    ctx.velocity(tgt, *src, flags=P.FP64)
+    e1.record()
+    torch.cuda.synchronize()
+    r64 = 8192 * int((s6.mesh["fmask"] == 0).sum()) / (e0.elapsed_time(e1) * 1e-3)
+    ctx.close()
+    serial64 = sum((sp["nsteps"] * 4 + 1) * computed_pairs(sp["seed"], sp["level"]) for sp in specs) / r64
     solve_steps = st["solve_steps"] - base["solve_steps"]
     pairs = st["pairs"] - base["pairs"]
     nearest = lambda q: float(np.sort(lat)[max(0, math.ceil(q * n) - 1)])  # noqa: E731
+    kinds_desc = "icosahedral" if args.kinds == "icos" else "icosahedral or cubed sphere"
     out = {
         "metric": "server requests/s", "value": n / wall, "unit": "requests/s", "n_gpus": 1,
         "steps": args.req_steps, "warmup": len(warm), "ms_per_step": None, "higher_is_better": True,
         "scaling": "replicas only", "vs_baseline": None, "dtype": "f32c",
         "data": "synthetic (seeded RH54 + Gaussian vortices on generated meshes, Poisson arrivals)",
-        "config": {"workload": f"{n} requests, Poisson arrivals at {args.rate}/s, icosahedral or cubed sphere "
-                               f"levels 3-7 (weights .3 .3 .2 .15 .05), {args.req_steps} RK4 steps each, "
-                               f"dt at the level-4 Courant number, FP32C (seed {SEED_BASE + 4})",
-                   "levels": {str(lv): int((lvls == lv).sum()) for lv in levels}},
+        "config": {"workload": f"{n} requests, Poisson arrivals at {rate:.4g}/s, {kinds_desc} levels "
+                               f"{lo}-{hi} (weights {', '.join(f'{v:.3g}' for v in weights)}), "
+                               f"{args.req_steps} RK4 steps each, dt at the level-4 Courant number, FP32C "
+                               f"(seed {SEED_BASE + 4})",
+                   "levels": {str(lv): int((lvls == lv).sum()) for lv in levels},
+                   "expected_service_s": exp_service, "offered_utilisation": rate * exp_service},
         "latency_s": {"p50": nearest(0.5), "p99": nearest(0.99), "max": float(lat.max()),
                       "mean_wait": float(waits.mean())},
         "latency_by_level": by_level,
         "solve_steps_per_s": solve_steps / wall, "computed_pairs_per_s": pairs / wall,
         "server_iterations": st["steps_run"] - base["steps_run"], "max_running": st["max_running_seen"],
         "wall_s": wall, "mix_equals_alone": bool(same), "clocks": clocks,
+        "serial_fp64_gpu": {"pairs_per_s": r64, "seconds": serial64, "requests_per_s": n / serial64,
+                            "speedup": (n / wall) / (n / serial64),
+                            "how": "each request alone on the plain FP64 GPU path: (4 evaluations per step + 1 "
+                                   "initial) x computed pairs / FP64 pair rate measured here (level 6)"},
         "e2e": {"value": n / wall, "unit": "requests/s", "h2d_bytes_per_step": None, "d2h_bytes_per_step": None},
     }
     print(json.dumps(out), flush=True)

@@ -169,6 +169,19 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
 int lpm_bve_rk4_increments(lpm_bve_ctx* ctx, int stage, double* vx_inc, double* vzeta_inc, double* fx_inc,
                            double* fzeta_inc, lpm_stream_t stream);
 
+/* Relative error norms of ErrNorms::compute (src/LpmErrorNorms.cpp:26-70) between two DEVICE
+ * arrays of n entries: ncomp = 3 for vectors (strides as above; magnitudes of the difference and
+ * of `exact`), ncomp = 1 for scalars (component strides ignored).  out = {l1, l2, linf} on the
+ * host: l1 = sum |e| w / sum |x| w, l2 = sqrt(sum |e|^2 w / sum |x|^2 w), linf = max |e| / max |x|.
+ * wt: optional weights (e.g. face areas; NULL = 1); skip: optional byte mask, entries with
+ * skip[i] != 0 are left out (e.g. masked parent faces).  For scalars the reference's linf takes
+ * the largest signed error and exact value; LPM_NORMS_ABS_LINF uses magnitudes instead.  The sums
+ * are reduced in a fixed order (bitwise reproducible).  Synchronises the stream. */
+#define LPM_NORMS_ABS_LINF (1u << 0)
+int lpm_errnorms(lpm_bve_ctx* ctx, const double* appx, int64_t a_si, int64_t a_sc, const double* exact,
+                 int64_t e_si, int64_t e_sc, const double* wt, const uint8_t* skip, int64_t n, int ncomp,
+                 unsigned flags, double out[3], lpm_stream_t stream);
+
 /* ---- host-side mesh and initial conditions ------------------------------------------ */
 #define LPM_SEED_ICOS_TRI 0 /* IcosTriSphereSeed  (src/LpmMeshSeed.hpp:134-152) */
 #define LPM_SEED_CUBED    1 /* CubedSphereSeed    (src/LpmMeshSeed.hpp:113-128) */

@@ -12,6 +12,9 @@ extern "C" {
 #endif
 
 int lpm_probe_fp32_fma(int device, int iters, double* lane_ops_per_s, double* ms);
+/* The same with paired FP32 FMAs (f32x2, two FMA lanes per issued instruction); the rate is
+ * still counted in single FMA lane operations per second. */
+int lpm_probe_fp32_fma2(int device, int iters, double* lane_ops_per_s, double* ms);
 
 #ifdef __cplusplus
 }

@@ -82,6 +82,8 @@ class ServerCounters(ctypes.Structure):
                 ("budget_bytes", ctypes.c_size_t), ("max_running_seen", ctypes.c_int)]
 
 
+NORMS_ABS_LINF = 1 << 0
+
 REQ_QUEUED, REQ_PREPARING, REQ_RUNNING, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, -1, -2
 
 _lib = None
@@ -124,7 +126,10 @@ def _declare(L):
         getattr(L, n).argtypes = [vp, c_i64, vp]
     L.lpm_ic_gaussians_add.argtypes = [vp, c_i64, vp, vp, ctypes.c_int, ctypes.c_double, vp]
     L.lpm_probe_fp32_fma.argtypes = [ctypes.c_int, ctypes.c_int, c_dp, c_dp]
+    L.lpm_probe_fp32_fma2.argtypes = [ctypes.c_int, ctypes.c_int, c_dp, c_dp]
     L.lpm_ic_gaussian_params.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
+    L.lpm_errnorms.argtypes = [vp, vp, c_i64, c_i64, vp, c_i64, c_i64, vp, vp, c_i64, ctypes.c_int, ctypes.c_uint,
+                               c_dp, vp]
     L.lpm_bve_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
     L.lpm_bve_server_estimate.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(Request),
                                           ctypes.POINTER(ctypes.c_size_t)]

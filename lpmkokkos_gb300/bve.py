@@ -227,6 +227,28 @@ class Context:
                                                  _np_ptr(fz), _stream(stream)), self.handle)
         return vx, vz, fx, fz
 
+    def errnorms(self, appx: torch.Tensor, exact: torch.Tensor, wt: Optional[torch.Tensor] = None,
+                 skip: Optional[torch.Tensor] = None, abs_linf: bool = False, stream=None):
+        """Relative (l1, l2, linf) of appx against exact on the device (ErrNorms::compute,
+        src/LpmErrorNorms.cpp:26-70): float64 (n, 3) vectors or (n,) scalars, optional float64
+        weights and a byte mask of entries to leave out."""
+        assert appx.dtype == torch.float64 and exact.dtype == torch.float64 and appx.shape == exact.shape
+        ncomp = 3 if appx.dim() == 2 else 1
+        if ncomp == 3:
+            assert appx.shape[1] == 3
+            a_sc, e_sc = appx.stride(1), exact.stride(1)
+        else:
+            a_sc = e_sc = 0
+        if wt is not None:
+            assert wt.dtype == torch.float64 and wt.is_contiguous() and wt.shape[0] == appx.shape[0]
+        if skip is not None:
+            assert skip.dtype in (torch.uint8, torch.bool) and skip.is_contiguous()
+        out = (ctypes.c_double * 3)()
+        L.check(self._lib.lpm_errnorms(self.handle, appx.data_ptr(), appx.stride(0), a_sc, exact.data_ptr(),
+                                       exact.stride(0), e_sc, _vp(wt), _vp(skip), appx.shape[0], ncomp,
+                                       L.NORMS_ABS_LINF if abs_linf else 0, out, _stream(stream)), self.handle)
+        return tuple(out)
+
     def ensemble(self, states: Sequence[BVEState], flags: int = 0, eps: float = 0.0, stream=None) -> "Ensemble":
         return Ensemble(self, states, flags, eps, stream)
 

@@ -369,6 +369,8 @@ struct lpm_bve_ctx {
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
   lpm::PairShape forced{0, 0, 0, 0};       // FP32C launch shape chosen by the caller (threads 0 = none)
   std::map<std::array<int, 5>, lpm::PairShape> tuned;  // autotuner results per size bucket
+  double* normScratch = nullptr;  // device: block partials + result of lpm_errnorms
+  double* normHost = nullptr;     // pinned: result of lpm_errnorms
 };
 
 struct lpm_bve_ensemble {
@@ -559,6 +561,8 @@ int lpm_bve_ctx_destroy(lpm_bve_ctx* ctx) {
   ctx->velBatch.reset();
   ctx->rkBatch.reset();
   if (ctx->capture) cudaStreamDestroy(ctx->capture);
+  if (ctx->normScratch) cudaFree(ctx->normScratch);
+  if (ctx->normHost) cudaFreeHost(ctx->normHost);
   delete ctx;
   return LPM_OK;
 }
@@ -820,6 +824,42 @@ int lpm_bve_rk4_increments(lpm_bve_ctx* ctx, int stage, double* vx_inc, double* 
         for (int c = 0; c < 3; ++c) X[3 * q + c] = kx[(size_t)c * n + t];
       if (Z) Z[q] = kz[t];
     }
+  } catch (const Error& e) {
+    return handle(ctx, e);
+  }
+  return LPM_OK;
+}
+
+int lpm_errnorms(lpm_bve_ctx* ctx, const double* appx, int64_t a_si, int64_t a_sc, const double* exact,
+                 int64_t e_si, int64_t e_sc, const double* wt, const uint8_t* skip, int64_t n, int ncomp,
+                 unsigned flags, double out[3], lpm_stream_t stream) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  try {
+    setDevice(ctx);
+    cudaStream_t s = (cudaStream_t)stream;
+    if (!out) fail(LPM_ERR_INVALID_ARGUMENT, "errnorms: null output");
+    if (ncomp != 1 && ncomp != 3) fail(LPM_ERR_INVALID_ARGUMENT, "errnorms: ncomp must be 1 or 3");
+    if (ncomp == 1) a_sc = e_sc = 0;
+    checkVec("appx", appx, n, a_si, ncomp == 3 ? a_sc : 0);
+    checkVec("exact", exact, n, e_si, ncomp == 3 ? e_sc : 0);
+    if (n == 0) fail(LPM_ERR_INVALID_ARGUMENT, "errnorms: no entries");
+    const int nblocks = normBlocks(ctx->dev.sms);
+    if (!ctx->normScratch) {
+      void* p = nullptr;
+      LPM_CUDA(cudaMalloc(&p, sizeof(double) * (6 * (size_t)nblocks + 3)));
+      ctx->normScratch = static_cast<double*>(p);
+    }
+    if (!ctx->normHost) {
+      void* p = nullptr;
+      LPM_CUDA(cudaMallocHost(&p, sizeof(double) * 3));
+      ctx->normHost = static_cast<double*>(p);
+    }
+    NormArgs a{appx, a_si, a_sc, exact, e_si, e_sc, wt, skip, n, ncomp, (flags & LPM_NORMS_ABS_LINF) ? 0 : 1};
+    double* dOut = ctx->normScratch + 6 * (size_t)nblocks;
+    LPM_CUDA(launchNorms(a, ctx->normScratch, nblocks, dOut, s));
+    LPM_CUDA(cudaMemcpyAsync(ctx->normHost, dOut, sizeof(double) * 3, cudaMemcpyDeviceToHost, s));
+    LPM_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < 3; ++k) out[k] = ctx->normHost[k];
   } catch (const Error& e) {
     return handle(ctx, e);
   }

@@ -109,6 +109,22 @@ cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool pr
 int pairShapeCount();              // FP32C launch shapes compiled in
 PairShape pairShapeAt(int i);
 int stageBlockSize();
+
+// Relative error norms (norms.cu): appx/exact strided arrays of n entries of ncomp (1 or 3)
+// components, optional weights and skip mask; out (device) = {l1, l2, linf}.
+struct NormArgs {
+  const double* appx;
+  int64_t a_si, a_sc;
+  const double* exact;
+  int64_t e_si, e_sc;
+  const double* wt;
+  const uint8_t* skip;
+  int64_t n;
+  int ncomp;
+  int signedLinf;
+};
+int normBlocks(int sms);
+cudaError_t launchNorms(const NormArgs& a, double* partial, int nblocks, double* out, cudaStream_t s);
 int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi);
 bool pairShapeSupported(Precision prec, const PairShape& shape);
 int pairNumComponents(Precision prec, bool psi);  // partial-sum components per (chunk, slot)

@@ -119,9 +119,11 @@ void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc
 // ---------------------------------------------------------------------------------------
 enum class Mode { Distinct = 0, Collocated = 1, RK4 = 2 };
 
-// Launch shape used when the autotuner is off (measured best on GB300 among the
-// instantiated shapes; the autotuner may choose another one per problem size).
-inline constexpr PairShape kDefaultFP32C{128, 4, 256, 1};
+// Launch shape used when the autotuner is off: 128 threads x 8 targets (four target pairs per
+// thread), 256-source tiles, 2 resident CTAs per SM -- the fastest instantiated shape on GB300
+// at icosahedral levels 6 and 7 (RK4 pair launches: 76.7 ms at level 7 against 77.1-80.8 ms for
+// the others).  The autotuner may choose another one per problem size.
+inline constexpr PairShape kDefaultFP32C{128, 8, 256, 1};
 inline constexpr PairShape kFP64Shape{128, 1, 128, 1};
 
 struct SolvePlan {

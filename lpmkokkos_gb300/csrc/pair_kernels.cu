@@ -15,8 +15,9 @@
 //    D = 1 - |x|^2.  Coordinates are FP64 hi/lo float pairs; each CTA subtracts the centre
 //    of its target tile once per staged source, so every FP32 difference is taken between
 //    nearby small numbers.  Per pair: 13 FP32 FMA-pipe ops + one MUFU.RCP
-//    (3 FADD d, 1 FADD + 3 FFMA for 2q, 2 FFMA Newton step, 1 FMUL, 3 FFMA accumulate).
-//    Each 32-source sub-block is summed in FP32 and added to a Kahan-compensated FP32
+//    (3 FADD d, 1 FADD + 3 FFMA for 2q, 1 FMUL + 1 FFMA + 1 FMUL for w r and the Newton
+//    step, 3 FFMA accumulate), issued as paired f32x2 instructions over two targets.
+//    Each 64-source sub-block is summed in FP32 and added to a Kahan-compensated FP32
 //    accumulator; partials leave the kernel in FP64 and the epilogue forms the FP64 cross
 //    product.  Stream function: + MUFU.LG2, 1 FFMA, 1 FADD per pair.
 //
@@ -85,64 +86,117 @@ __device__ __forceinline__ void tileCentre(const double* __restrict__ tx, int n,
   cx = tx[tile0 + c]; cy = tx[n + tile0 + c]; cz = tx[2 * n + tile0 + c];
 }
 
-// Shared-memory record of one staged source: A = (x, y, z, w) and B = (x_lo, y_lo, z_lo, D).
-// Fast formulation: A.xyz = x_j - c relative to the tile centre c, B.w = D_j (B.xyz unused).
-// Precise formulation: A.xyz = hi(x_j), B.xyz = lo(x_j) (x = hi + lo exactly to ~2^-48).
+// Paired FP32 arithmetic (f32x2): one instruction computes the same operation for two of a
+// thread's targets, so the 13 FMA-pipe lane-ops of a pair issue as 6.5 instructions and the
+// issue slots left over carry the reciprocal, the shared loads and the loop.  Each lane is
+// rounded exactly as the scalar instruction would be.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// Staged source tile, every value stored twice so that one shared load yields the pair operand
+// (both halves hold the same source): XY = (x, x, y, y), ZW = (z, z, w, w), D = (D, D).
+// Fast formulation: x, y, z relative to the tile origin; precise: hi parts, with the lo parts in
+// LXY = (x_lo, x_lo, y_lo, y_lo), LZ = (z_lo, z_lo).  w = -zeta A / 2 pi, D = 1 - |x|^2.
+template <bool PRECISE>
+struct SourceTile;
+template <>
+struct SourceTile<false> {
+  const float4* xy; const float4* zw; const float2* d;
+};
+template <>
+struct SourceTile<true> {
+  const float4* xy; const float4* zw; const float2* d; const float4* lxy; const float2* lz;
+};
+
+// One staged tile against the thread's K targets, held as K/2 target pairs with negated
+// coordinates (nx = -x_i, so x_j + nx = x_j - x_i) and C = D_i + 2 eps^2.  Per pair:
+//   d = x_j - x_i, 2q = D_j + C + |d|^2 (x, y, z in that order), r = rcp.approx(2q),
+//   NEWTON:   s' = (w r) (2q r - 2) = -s   (the Newton step r (2 - 2q r), negated so that no
+//             operand needs a sign flip), accumulated as v += s' d and folded with a minus sign;
+//   !NEWTON:  s  = w r, folded with a plus sign.
+// Each kSub-source block is summed in FP32, then added to the Kahan-compensated accumulators.
 template <int K, bool PSI, bool CHECKED, bool PRECISE, bool NEWTON>
-__device__ __forceinline__ void fp32cTile(const float4* __restrict__ sA, const float4* __restrict__ sB, int nsrc,
-                                          int jbase, const float (&ax)[K], const float (&ay)[K], const float (&az)[K],
-                                          const float (&lx)[K], const float (&ly)[K], const float (&lz)[K],
-                                          const float (&C)[K], const int (&self)[K],
+__device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc, int jbase,
+                                          const float2 (&nx)[K / 2], const float2 (&ny)[K / 2],
+                                          const float2 (&nz)[K / 2], const float2 (&nlx)[K / 2],
+                                          const float2 (&nly)[K / 2], const float2 (&nlz)[K / 2],
+                                          const float2 (&C)[K / 2], const int (&self)[K],
                                           float (&hx)[K], float (&hy)[K], float (&hz)[K],
                                           float (&cx)[K], float (&cy)[K], float (&cz)[K],
                                           float (&hp)[K], float (&cp)[K], float (&hw)[K], float (&cw)[K]) {
+  constexpr int P = K / 2;
+  constexpr float kSign = NEWTON ? -1.f : 1.f;
+  const float2 kMinusTwo = make_float2(-2.f, -2.f);
 #pragma unroll 1
   for (int j0 = 0; j0 < nsrc; j0 += kSub) {
-    float vx[K], vy[K], vz[K], vp[K], vw[K];
+    float2 vx[P], vy[P], vz[P], vp[P], vw[P];
 #pragma unroll
-    for (int k = 0; k < K; ++k) { vx[k] = 0.f; vy[k] = 0.f; vz[k] = 0.f; vp[k] = 0.f; vw[k] = 0.f; }
+    for (int m = 0; m < P; ++m) {
+      vx[m] = vy[m] = vz[m] = vp[m] = vw[m] = make_float2(0.f, 0.f);
+    }
 #pragma unroll 4
     for (int j = j0; j < j0 + kSub; ++j) {
-      const float4 A = sA[j];
-      const float4 B = sB[j];
+      const float4 xy = T.xy[j];
+      const float4 zw = T.zw[j];
+      const float2 dj = T.d[j];
+      const float2 X = make_float2(xy.x, xy.y), Y = make_float2(xy.z, xy.w), Z = make_float2(zw.x, zw.y);
+      const float2 W = make_float2(zw.z, zw.w);
+      float2 LX, LY, LZ;
+      if constexpr (PRECISE) {
+        const float4 lxy = T.lxy[j];
+        LX = make_float2(lxy.x, lxy.y);
+        LY = make_float2(lxy.z, lxy.w);
+        LZ = T.lz[j];
+      }
 #pragma unroll
-      for (int k = 0; k < K; ++k) {
-        float dx, dy, dz;
-        if (PRECISE) {  // hi parts subtract exactly when close; lo parts restore the rest
-          dx = (A.x - ax[k]) + (B.x - lx[k]);
-          dy = (A.y - ay[k]) + (B.y - ly[k]);
-          dz = (A.z - az[k]) + (B.z - lz[k]);
+      for (int m = 0; m < P; ++m) {
+        float2 dx, dy, dz;
+        if constexpr (PRECISE) {  // hi parts subtract exactly when close; lo parts restore the rest
+          dx = add2(add2(X, nx[m]), add2(LX, nlx[m]));
+          dy = add2(add2(Y, ny[m]), add2(LY, nly[m]));
+          dz = add2(add2(Z, nz[m]), add2(LZ, nlz[m]));
         } else {
-          dx = A.x - ax[k];
-          dy = A.y - ay[k];
-          dz = A.z - az[k];
+          dx = add2(X, nx[m]);
+          dy = add2(Y, ny[m]);
+          dz = add2(Z, nz[m]);
         }
-        const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, B.w + C[k])));
-        float r = rcpApprox(q2);
-        if (NEWTON) {  // one Newton step: r (2 - q2 r)
-          const float e = fmaf(-q2, r, 1.0f);
-          r = fmaf(r, e, r);
+        float2 q = add2(dj, C[m]);
+        q = fma2(dx, dx, q);
+        q = fma2(dy, dy, q);
+        q = fma2(dz, dz, q);
+        const float2 r = make_float2(rcpApprox(q.x), rcpApprox(q.y));
+        float2 sp = mul2(W, r);
+        if (NEWTON) sp = mul2(sp, fma2(q, r, kMinusTwo));
+        float2 lg, ww;
+        if (PSI) { lg = make_float2(lg2Approx(q.x), lg2Approx(q.y)); ww = W; }
+        if (CHECKED) {  // a self pair has q ~ 0: drop its (inf/NaN) terms after they are formed
+          if (jbase + j == self[2 * m]) { sp.x = 0.f; if (PSI) { lg.x = 0.f; ww.x = 0.f; } }
+          if (jbase + j == self[2 * m + 1]) { sp.y = 0.f; if (PSI) { lg.y = 0.f; ww.y = 0.f; } }
         }
-        float s = A.w * r;
-        float wl = 0.f, ww = 0.f;
-        if (PSI) { wl = A.w * lg2Approx(q2); ww = A.w; }
-        if (CHECKED) {
-          const bool me = (jbase + j) == self[k];
-          s = me ? 0.f : s;
-          if (PSI) { wl = me ? 0.f : wl; ww = me ? 0.f : ww; }
+        vx[m] = fma2(sp, dx, vx[m]);
+        vy[m] = fma2(sp, dy, vy[m]);
+        vz[m] = fma2(sp, dz, vz[m]);
+        if (PSI) {
+          vp[m] = fma2(W, lg, vp[m]);
+          vw[m] = add2(vw[m], ww);
         }
-        vx[k] = fmaf(s, dx, vx[k]);
-        vy[k] = fmaf(s, dy, vy[k]);
-        vz[k] = fmaf(s, dz, vz[k]);
-        if (PSI) { vp[k] += wl; vw[k] += ww; }
       }
     }
 #pragma unroll
-    for (int k = 0; k < K; ++k) {
-      kahanAdd(hx[k], cx[k], vx[k]);
-      kahanAdd(hy[k], cy[k], vy[k]);
-      kahanAdd(hz[k], cz[k], vz[k]);
-      if (PSI) { kahanAdd(hp[k], cp[k], vp[k]); kahanAdd(hw[k], cw[k], vw[k]); }
+    for (int m = 0; m < P; ++m) {
+      kahanAdd(hx[2 * m], cx[2 * m], kSign * vx[m].x);
+      kahanAdd(hx[2 * m + 1], cx[2 * m + 1], kSign * vx[m].y);
+      kahanAdd(hy[2 * m], cy[2 * m], kSign * vy[m].x);
+      kahanAdd(hy[2 * m + 1], cy[2 * m + 1], kSign * vy[m].y);
+      kahanAdd(hz[2 * m], cz[2 * m], kSign * vz[m].x);
+      kahanAdd(hz[2 * m + 1], cz[2 * m + 1], kSign * vz[m].y);
+      if (PSI) {
+        kahanAdd(hp[2 * m], cp[2 * m], vp[m].x);
+        kahanAdd(hp[2 * m + 1], cp[2 * m + 1], vp[m].y);
+        kahanAdd(hw[2 * m], cw[2 * m], vw[m].x);
+        kahanAdd(hw[2 * m + 1], cw[2 * m + 1], vw[m].y);
+      }
     }
   }
 }
@@ -160,10 +214,18 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
                                                  const WorkItem* __restrict__ items, int nitems,
                                                  int* __restrict__ counter) {
   static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
-  __shared__ float4 sA[ST];
-  __shared__ float4 sB[ST];
+  static_assert(K % 2 == 0, "targets are processed in pairs");
+  constexpr int P = K / 2;
+  __shared__ float4 sXY[ST];
+  __shared__ float4 sZW[ST];
+  __shared__ float2 sD[ST];
+  __shared__ float4 sLXY[PRECISE ? ST : 1];
+  __shared__ float2 sLZ[PRECISE ? ST : 1];
   __shared__ int sItem;
   __shared__ int sCentre;
+  SourceTile<PRECISE> T;
+  T.xy = sXY; T.zw = sZW; T.d = sD;
+  if constexpr (PRECISE) { T.lxy = sLXY; T.lz = sLZ; }
 
   for (;;) {
     if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
@@ -190,7 +252,8 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
       clz = __double2float_rn(czd - (double)chz);
     }
 
-    float ax[K], ay[K], az[K], lx[K], ly[K], lz[K], C[K];
+    // Targets k = 2m, 2m+1 of this thread form pair m (slots tile0 + threadIdx.x + k NTH).
+    float ax[K], ay[K], az[K], lx[K], ly[K], lz[K], Ck[K];
     int self[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -208,11 +271,22 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
           az[k] = relCoord(hz, ez, chz, clz);
           lx[k] = ly[k] = lz[k] = 0.f;
         }
-        C[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * S.eps2);
+        Ck[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * S.eps2);
         self[k] = S.self[slot];
       } else {
-        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; lx[k] = ly[k] = lz[k] = 0.f; C[k] = 1.f; self[k] = -1;
+        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; lx[k] = ly[k] = lz[k] = 0.f; Ck[k] = 1.f; self[k] = -1;
       }
+    }
+    float2 nx[P], ny[P], nz[P], nlx[P], nly[P], nlz[P], C[P];
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+      nx[m] = make_float2(-ax[2 * m], -ax[2 * m + 1]);
+      ny[m] = make_float2(-ay[2 * m], -ay[2 * m + 1]);
+      nz[m] = make_float2(-az[2 * m], -az[2 * m + 1]);
+      nlx[m] = make_float2(-lx[2 * m], -lx[2 * m + 1]);
+      nly[m] = make_float2(-ly[2 * m], -ly[2 * m + 1]);
+      nlz[m] = make_float2(-lz[2 * m], -lz[2 * m + 1]);
+      C[m] = make_float2(Ck[2 * m], Ck[2 * m + 1]);
     }
     float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
 #pragma unroll
@@ -226,30 +300,36 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
       // Stage ST sources; padding (w = 0, D = 1) adds exactly 0.
       for (int j = threadIdx.x; j < ST; j += NTH) {
         const int s = b0 + j;
-        if (s < w.s1) {
+        float x = 0.f, y = 0.f, z = 0.f, wj = 0.f, dj = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+        if (s < w.s1) {  // else: at the centre (fast) or the origin (precise), finite q, zero weight
           const float4 p0 = S.sp0[s];
           const float4 p1 = S.sp1[s];
           if (PRECISE) {
-            sA[j] = p0;
-            sB[j] = p1;
+            x = p0.x; y = p0.y; z = p0.z; ux = p1.x; uy = p1.y; uz = p1.z;
           } else {
-            sA[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
-                                relCoord(p0.z, p1.z, chz, clz), p0.w);
-            sB[j] = make_float4(0.f, 0.f, 0.f, p1.w);
+            x = relCoord(p0.x, p1.x, chx, clx);
+            y = relCoord(p0.y, p1.y, chy, cly);
+            z = relCoord(p0.z, p1.z, chz, clz);
           }
-        } else {  // at the centre (fast) or at the origin (precise): finite q, zero weight
-          sA[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-          sB[j] = make_float4(0.f, 0.f, 0.f, 1.f);
+          wj = p0.w;
+          dj = p1.w;
+        }
+        sXY[j] = make_float4(x, x, y, y);
+        sZW[j] = make_float4(z, z, wj, wj);
+        sD[j] = make_float2(dj, dj);
+        if (PRECISE) {
+          sLXY[j] = make_float4(ux, ux, uy, uy);
+          sLZ[j] = make_float2(uz, uz);
         }
       }
       __syncthreads();
       const bool checked = (ts.x <= b0 + ST - 1) && (ts.y >= b0);
       if (checked)
-        fp32cTile<K, PSI, true, PRECISE, NEWTON>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
-                                         hp, cp, hw, cw);
+        fp32cTile<K, PSI, true, PRECISE, NEWTON>(T, ST, b0, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz, cx, cy,
+                                                 cz, hp, cp, hw, cw);
       else
-        fp32cTile<K, PSI, false, PRECISE, NEWTON>(sA, sB, ST, b0, ax, ay, az, lx, ly, lz, C, self, hx, hy, hz, cx, cy, cz,
-                                          hp, cp, hw, cw);
+        fp32cTile<K, PSI, false, PRECISE, NEWTON>(T, ST, b0, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz, cx, cy,
+                                                  cz, hp, cp, hw, cw);
       __syncthreads();
     }
 
@@ -336,12 +416,17 @@ struct ShapeFn {
   {T, K, S, B, {{(void*)pairFP32C<T, K, S, B, false, false, true>, (void*)pairFP32C<T, K, S, B, true, false, true>},   \
                 {(void*)pairFP32C<T, K, S, B, false, true, true>, (void*)pairFP32C<T, K, S, B, true, true, true>},     \
                 {(void*)pairFP32C<T, K, S, B, false, false, false>, (void*)pairFP32C<T, K, S, B, true, false, false>}}}
+// Register use of the RK4 velocity kernel (ptxas, sm_103a, paired arithmetic) sets the
+// resident CTAs per SM: 128x4 unbounded 154 regs -> 3/SM, min-blocks 4: 124 -> 4/SM;
+// 128x6 min-blocks 3: 163 -> 3/SM; 128x8 233 -> 2/SM; 64x8 min-blocks 4: 233 -> 4/SM;
+// 256x4 min-blocks 2: 125 -> 2/SM.  None of these spills.
 const ShapeFn kShapes[] = {
   LPM_SHAPE(128, 4, 256, 1),
-  LPM_SHAPE(128, 4, 256, 6),
+  LPM_SHAPE(128, 4, 256, 4),
+  LPM_SHAPE(128, 6, 256, 3),
   LPM_SHAPE(128, 8, 256, 1),
-  LPM_SHAPE(256, 2, 256, 1),
-  LPM_SHAPE(256, 4, 256, 1),
+  LPM_SHAPE(64, 8, 256, 4),
+  LPM_SHAPE(256, 4, 256, 2),
 };
 #undef LPM_SHAPE
 

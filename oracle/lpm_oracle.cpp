@@ -20,6 +20,7 @@
 //
 // Build: oracle/Makefile (g++ -O2 -fopenmp -ffp-contract=off -shared -fPIC).
 
+#include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstdlib>
@@ -625,6 +626,21 @@ void oracle_errnorms_vec(const double* appx, const double* exact, const double* 
     l1n += em*wt[i]; l1d += xm*wt[i]; l2n += em*em*wt[i]; l2d += xm*xm*wt[i];
     if (em > lin) lin = em;
     if (xm > lid) lid = xm;
+  }
+  out[0] = l1n/l1d; out[1] = std::sqrt(l2n/l2d); out[2] = lin/lid;
+}
+
+// ErrNorms::compute for scalars (src/LpmErrorNorms.cpp:47-70): l1/l2 of |e| and |exact|; linf is
+// the largest SIGNED error over the largest signed exact value, starting from the max-reduction
+// identity (the lowest double), as the reference's lambda writes it.
+void oracle_errnorms_scalar(const double* appx, const double* exact, const double* wt, long n, double* out) {
+  Real l1n = 0, l1d = 0, l2n = 0, l2d = 0, lin = -DBL_MAX, lid = -DBL_MAX;
+  for (long i = 0; i < n; ++i) {
+    const Real e = appx[i] - exact[i], x = exact[i];
+    l1n += std::abs(e)*wt[i]; l1d += std::abs(x)*wt[i];
+    l2n += e*e*wt[i]; l2d += x*x*wt[i];
+    lin = e > lin ? e : lin;
+    lid = x > lid ? x : lid;
   }
   out[0] = l1n/l1d; out[1] = std::sqrt(l2n/l2d); out[2] = lin/lid;
 }

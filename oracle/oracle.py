@@ -78,6 +78,7 @@ def _setup(L):
     L.oracle_ic_gaussians_add.argtypes = [D, ctypes.c_long, D, D, ctypes.c_int, ctypes.c_double, D]
     L.oracle_gaussian_params.argtypes = [ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D]
     L.oracle_errnorms_vec.argtypes = [D, D, D, ctypes.c_long, D]
+    L.oracle_errnorms_scalar.argtypes = [D, D, D, ctypes.c_long, D]
     L.oracle_poisson.argtypes = [ctypes.c_int, ctypes.c_int, D]
     L.oracle_poisson.restype = ctypes.c_int
     L.oracle_tri_area.argtypes = [D, D, D]
@@ -201,6 +202,15 @@ def errnorms_vec(appx, exact, wt):
     wt = np.ascontiguousarray(wt, dtype=np.float64)
     out = np.zeros(3)
     lib().oracle_errnorms_vec(_dp(appx), _dp(exact), _dp(wt), appx.shape[0], _dp(out))
+    return dict(l1=out[0], l2=out[1], linf=out[2])
+
+
+def errnorms_scalar(appx, exact, wt):
+    appx = np.ascontiguousarray(appx, dtype=np.float64)
+    exact = np.ascontiguousarray(exact, dtype=np.float64)
+    wt = np.ascontiguousarray(wt, dtype=np.float64)
+    out = np.zeros(3)
+    lib().oracle_errnorms_scalar(_dp(appx), _dp(exact), _dp(wt), appx.shape[0], _dp(out))
     return dict(l1=out[0], l2=out[1], linf=out[2])
 
 
