@@ -193,6 +193,11 @@ int lpm_mesh_counts(int seed, int level, int64_t* nverts, int64_t* nfaces, int64
  * farea (nfaces), fmask (nfaces).  Any pointer may be NULL. */
 int lpm_mesh_build(int seed, int level, double* vx, double* fx, double* farea, uint8_t* fmask);
 
+/* Face-to-vertex connectivity of the same mesh: face_verts (nfaces x verts_per_face, row-major;
+ * 3 for the icosahedral seed, 4 for the cubed sphere) in the order the divisions of
+ * src/LpmFaces.cpp:115-382 give the reference's Faces::verts.  Either pointer may be NULL. */
+int lpm_mesh_face_verts(int seed, int level, int32_t* face_verts, int* verts_per_face);
+
 /* Host initial conditions on row-major (n x 3) positions.
  * RH54: zeta = 30 cos(4 lambda) P_5^4(z) (src/LpmRossbyWaves.hpp:28-32).
  * Solid body: zeta = 2*(2 pi) z (src/LpmVorticityGallery.hpp:25-40).
@@ -202,6 +207,15 @@ int lpm_ic_rh54_velocity(const double* x, int64_t n, double* u);
 int lpm_ic_solid_body(const double* x, int64_t n, double* zeta);
 int lpm_ic_gaussians_add(const double* x, int64_t n, const double* centers, const double* amps, int ng,
                          double width, double* zeta);
+/* The same initial vorticity on the DEVICE: zeta[i] = RH54(x_i) + sum_g amps[g] exp(-(d(x_i,
+ * c_g)/width)^2) for n device points x (strides as above), written to the device array zeta,
+ * queued on `stream` with no allocation.  centers (ng x 3) and amps are HOST arrays, ng <=
+ * LPM_IC_MAX_GAUSSIANS.  Products and sums are rounded as in the host functions; cos, atan2 and
+ * exp come from CUDA's math library and agree with the host's to a few ulps. */
+#define LPM_IC_MAX_GAUSSIANS 64
+int lpm_ic_rh54_gaussians_device(const double* x, int64_t n, int64_t stride_i, int64_t stride_c,
+                                 const double* centers, const double* amps, int ng, double width, double* zeta,
+                                 lpm_stream_t stream);
 /* Seeded Gaussian-vortex parameters: centres uniform on the sphere (normalised normal
  * vectors), amplitudes U(amp_lo, amp_hi); std::mt19937_64 with a portable 53-bit uniform. */
 int lpm_ic_gaussian_params(uint64_t seed, int ng, double amp_lo, double amp_hi, double* centers, double* amps);

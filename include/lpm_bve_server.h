@@ -3,12 +3,12 @@
  * No counterpart in pbosler/lpmKokkos (one driver runs one BVESphere to completion).
  * Requests (a mesh, seeded RH54 + Gaussian-vortex initial data, dt, Omega, a step count) are
  * admitted first-come first-served while their estimated device footprint fits an HBM budget;
- * their particle state then stays on the device until they finish.  Every iteration of the
- * server advances every running solve by RK4 steps (src/LpmBVERK4_Impl.hpp:42-130); solves of
- * similar cost share a batch whose four evaluations per step are one persistent pair-kernel
- * launch each, the most expensive batch takes one step per iteration and cheaper ones several,
- * so a request that arrives while others run joins at the next iteration and leaves as soon
- * as its own steps are done.  A solve's result does not depend on which other solves shared
+ * their particle state then stays on the device until they finish.  Running solves advance by
+ * RK4 steps (src/LpmBVERK4_Impl.hpp:42-130); solves of similar cost share a batch whose four
+ * evaluations per step are one pair-kernel launch each, on a CUDA stream whose priority falls
+ * with the cost, so batches of different sizes run side by side and a small request is not held
+ * behind the steps of a large one.  A request that arrives while others run joins at once and
+ * leaves as soon as its own steps are done.  A solve's result does not depend on which other solves shared
  * its launches (per-solve summation order is fixed): bit-identical alone or in any mix.  Host
  * preparation (mesh, initial data, plan) runs on a separate thread.
  */
@@ -29,13 +29,16 @@ typedef struct {
   int max_active;          /* at most this many solves run together; 0 = no limit */
   unsigned flags;          /* LPM_BVE_FP32C or LPM_BVE_FP64, plus RK4 options of lpm_bve_rk4_step */
   double eps;              /* regularisation of the kernels (0 = reference) */
+  int host_ic;             /* 1: initial vorticity from the host functions (lpm_ic_rh54 +
+                              lpm_ic_gaussians_add, bitwise those of a BVESphere run); 0: on the
+                              GPU after the upload (lpm_ic_rh54_gaussians_device, a few ulps apart) */
 } lpm_bve_server_opts;
 
 typedef struct {
   int seed;            /* LPM_SEED_ICOS_TRI or LPM_SEED_CUBED */
   int level;           /* uniform refinement level, 0..10 */
   uint64_t ic_seed;    /* seed of the Gaussian-vortex parameters */
-  int n_gaussians;     /* RH54 plus this many Gaussian vortices, amplitudes U(-2, 2) */
+  int n_gaussians;     /* RH54 plus this many Gaussian vortices (<= LPM_IC_MAX_GAUSSIANS), U(-2, 2) */
   double gauss_width;  /* vortex width in radians */
   double dt, omega;    /* time step and rotation rate */
   int nsteps;          /* RK4 steps to run */
@@ -46,7 +49,7 @@ enum { LPM_REQ_QUEUED = 0, LPM_REQ_PREPARING = 1, LPM_REQ_RUNNING = 2, LPM_REQ_D
 
 typedef struct {
   int64_t submitted, completed, failed, cancelled, running, queued;
-  int64_t steps_run;          /* server iterations (each advances every running solve) */
+  int64_t steps_run;          /* RK4 steps launched over size classes (one step of one class) */
   int64_t solve_steps;        /* sum over solves of RK4 steps taken */
   double pairs;               /* target-source pairs evaluated (incl. masked-parent targets) */
   double busy_s;              /* wall time with at least one solve running */
@@ -71,6 +74,9 @@ int lpm_bve_server_cancel(lpm_bve_server* s, int64_t id);
  * array pointers NULL only the sizes are returned. */
 int lpm_bve_server_result(lpm_bve_server* s, int64_t id, int64_t* nverts, int64_t* nfaces, double* vx,
                           double* vzeta, double* vvel, double* fx, double* fzeta, double* fvel);
+/* Writes a finished request's final state as a snapshot file (include/lpm_bve_snapshot.h), with
+ * t = nsteps * dt; lpm_bve_snapshot_read restores it into device arrays to continue the run. */
+int lpm_bve_server_snapshot(lpm_bve_server* s, int64_t id, const char* path);
 /* Frees the host copy of a finished (done, failed or cancelled) request and forgets its id. */
 int lpm_bve_server_release(lpm_bve_server* s, int64_t id);
 /* Seconds from submit to done, spent queued/preparing before the first step, and running. */

@@ -66,7 +66,7 @@ class State(ctypes.Structure):
 
 class ServerOpts(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int), ("hbm_budget_bytes", ctypes.c_size_t), ("max_active", ctypes.c_int),
-                ("flags", ctypes.c_uint), ("eps", ctypes.c_double)]
+                ("flags", ctypes.c_uint), ("eps", ctypes.c_double), ("host_ic", ctypes.c_int)]
 
 
 class Request(ctypes.Structure):
@@ -128,6 +128,8 @@ def _declare(L):
     L.lpm_probe_fp32_fma.argtypes = [ctypes.c_int, ctypes.c_int, c_dp, c_dp]
     L.lpm_probe_fp32_fma2.argtypes = [ctypes.c_int, ctypes.c_int, c_dp, c_dp]
     L.lpm_ic_gaussian_params.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
+    L.lpm_ic_rh54_gaussians_device.argtypes = [vp, c_i64, c_i64, c_i64, vp, vp, ctypes.c_int, ctypes.c_double, vp,
+                                               vp]
     L.lpm_errnorms.argtypes = [vp, vp, c_i64, c_i64, vp, c_i64, c_i64, vp, vp, c_i64, ctypes.c_int, ctypes.c_uint,
                                c_dp, vp]
     L.lpm_bve_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]
@@ -140,6 +142,14 @@ def _declare(L):
     L.lpm_bve_server_result.argtypes = [vp, c_i64, ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), vp, vp, vp, vp, vp,
                                         vp]
     L.lpm_bve_server_release.argtypes = [vp, c_i64]
+    L.lpm_bve_server_snapshot.argtypes = [vp, c_i64, ctypes.c_char_p]
+    L.lpm_bve_snapshot_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(State), ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double, ctypes.c_double, ctypes.c_double, vp]
+    L.lpm_bve_snapshot_info.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                        ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), c_dp, c_dp, c_dp]
+    L.lpm_bve_snapshot_read.argtypes = [ctypes.c_char_p, ctypes.POINTER(State), c_dp, vp]
+    L.lpm_bve_vtk_write.argtypes = [ctypes.c_char_p, ctypes.POINTER(State), ctypes.c_int, ctypes.c_int, vp]
+    L.lpm_mesh_face_verts.argtypes = [ctypes.c_int, ctypes.c_int, vp, ctypes.POINTER(ctypes.c_int)]
     L.lpm_bve_server_timing.argtypes = [vp, c_i64, c_dp, c_dp, c_dp]
     L.lpm_bve_server_latency.argtypes = [vp, c_dp, ctypes.c_int, c_dp]
     L.lpm_bve_server_stats.argtypes = [vp, ctypes.POINTER(ServerCounters)]

@@ -108,6 +108,58 @@ def rh54_gaussians(seed: int, ng: int, width: float = 0.1) -> Callable[[np.ndarr
     return ic
 
 
+def ic_rh54_gaussians_device(x: torch.Tensor, seed: int, ng: int, width: float = 0.1, stream=None) -> torch.Tensor:
+    """rh54_gaussians(seed, ng, width) evaluated on the device at float64 (n, 3) device points."""
+    assert x.dtype == torch.float64 and x.dim() == 2 and x.shape[1] == 3 and x.is_cuda
+    c, a = gaussian_params(seed, ng)
+    z = torch.empty(x.shape[0], dtype=torch.float64, device=x.device)
+    L.check(L.lib().lpm_ic_rh54_gaussians_device(_vp(x), x.shape[0], x.stride(0), x.stride(1), _np_ptr(c),
+                                                 _np_ptr(a), ng, width, _vp(z), _stream(stream)))
+    return z
+
+
+def mesh_face_verts(seed: int, level: int) -> np.ndarray:
+    """Face-to-vertex connectivity (nfaces x 3 or 4) of build_mesh(seed, level)."""
+    _, nf, _ = mesh_counts(seed, level)
+    vpf = ctypes.c_int()
+    L.check(L.lib().lpm_mesh_face_verts(seed, level, None, ctypes.byref(vpf)))
+    fv = np.zeros((nf, vpf.value), dtype=np.int32)
+    L.check(L.lib().lpm_mesh_face_verts(seed, level, _np_ptr(fv), ctypes.byref(vpf)))
+    return fv
+
+
+# ----------------------------------------------------------------------------------------
+# snapshots and VTK output (include/lpm_bve_snapshot.h)
+# ----------------------------------------------------------------------------------------
+def snapshot_write(path: str, state: "BVEState", seed: int, level: int, t: float = 0.0, dt: float = 0.0,
+                   omega: float = 2 * PI, stream=None):
+    st = state.c_struct()
+    L.check(L.lib().lpm_bve_snapshot_write(path.encode(), ctypes.byref(st), seed, level, t, dt, omega,
+                                           _stream(stream)))
+
+
+def snapshot_info(path: str) -> dict:
+    sd, lv, nv, nf = ctypes.c_int(), ctypes.c_int(), L.c_i64(), L.c_i64()
+    t, dt, om = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    L.check(L.lib().lpm_bve_snapshot_info(path.encode(), ctypes.byref(sd), ctypes.byref(lv), ctypes.byref(nv),
+                                          ctypes.byref(nf), ctypes.byref(t), ctypes.byref(dt), ctypes.byref(om)))
+    return dict(seed=sd.value, level=lv.value, nverts=nv.value, nfaces=nf.value, t=t.value, dt=dt.value,
+                omega=om.value)
+
+
+def snapshot_read(path: str, state: "BVEState", stream=None) -> float:
+    """Restores positions, vorticity and velocity into `state`; returns the snapshot's time."""
+    st = state.c_struct()
+    t = ctypes.c_double()
+    L.check(L.lib().lpm_bve_snapshot_read(path.encode(), ctypes.byref(st), ctypes.byref(t), _stream(stream)))
+    return t.value
+
+
+def vtk_write(path: str, state: "BVEState", seed: int, level: int, stream=None):
+    st = state.c_struct()
+    L.check(L.lib().lpm_bve_vtk_write(path.encode(), ctypes.byref(st), seed, level, _stream(stream)))
+
+
 # ----------------------------------------------------------------------------------------
 # context
 # ----------------------------------------------------------------------------------------
@@ -295,7 +347,7 @@ class Ensemble:
 
 def server_estimate(seed: int, level: int, flags: int = L.FP32C, nsteps: int = 1, dt: float = 0.01) -> int:
     """Device bytes a server with these flags reserves for one request on this mesh (host-only)."""
-    opts = L.ServerOpts(0, 0, 0, flags, 0.0)
+    opts = L.ServerOpts(0, 0, 0, flags, 0.0, 0)
     req = L.Request(seed, level, 0, 0, 0.1, dt, 2 * PI, nsteps)
     n = ctypes.c_size_t()
     L.check(L.lib().lpm_bve_server_estimate(ctypes.byref(opts), ctypes.byref(req), ctypes.byref(n)))
@@ -312,10 +364,10 @@ class Server:
     """
 
     def __init__(self, device: Optional[int] = None, budget_bytes: int = 0, max_active: int = 0,
-                 flags: int = L.FP32C, eps: float = 0.0):
+                 flags: int = L.FP32C, eps: float = 0.0, host_ic: bool = False):
         self._lib = L.lib()
         dev = torch.cuda.current_device() if device is None else device
-        opts = L.ServerOpts(dev, budget_bytes, max_active, flags, eps)
+        opts = L.ServerOpts(dev, budget_bytes, max_active, flags, eps, int(host_ic))
         h = ctypes.c_void_p()
         rc = self._lib.lpm_bve_server_create(ctypes.byref(opts), ctypes.byref(h))
         if rc != L.LPM_OK:
@@ -363,6 +415,10 @@ class Server:
 
     def release(self, rid: int):
         self._check(self._lib.lpm_bve_server_release(self.handle, rid))
+
+    def snapshot(self, rid: int, path: str):
+        """Final state of a finished request as a snapshot file (restore with snapshot_read)."""
+        self._check(self._lib.lpm_bve_server_snapshot(self.handle, rid, path.encode()))
 
     def timing(self, rid: int) -> dict:
         t, w, r = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()

@@ -224,4 +224,9 @@ void refreshTables(Batch& B, cudaStream_t s);
 void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s);
 void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
 
+// Snapshot file of a state held in host row-major arrays (snapshot.cpp).
+void writeSnapshotHost(const char* path, int seed, int level, int vpf, int64_t nv, int64_t nf, double t, double dt,
+                       double omega, const double* vx, const double* vzeta, const double* vvel, const double* fx,
+                       const double* fzeta, const double* fvel, const double* farea, const uint8_t* fmask);
+
 }  // namespace lpm

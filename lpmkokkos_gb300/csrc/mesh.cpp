@@ -173,6 +173,8 @@ class TreeMesh {
   const std::vector<Vec3>& centres() const { return ctr_; }
   const std::vector<double>& areas() const { return area_; }
   const std::vector<uint8_t>& masks() const { return mask_; }
+  const std::vector<int>& faceVerts() const { return fv_; }  // n_ vertex indices per face
+  int vertsPerFace() const { return n_; }
 
  private:
   int n_;
@@ -305,6 +307,15 @@ int lpm_mesh_build(int seed, int level, double* vx, double* fx, double* farea, u
   for (size_t i = 0; fx && i < c.size(); ++i) { fx[3*i] = c[i].x; fx[3*i+1] = c[i].y; fx[3*i+2] = c[i].z; }
   if (farea) std::memcpy(farea, m.areas().data(), sizeof(double) * m.areas().size());
   if (fmask) std::memcpy(fmask, m.masks().data(), m.masks().size());
+  return LPM_OK;
+}
+
+int lpm_mesh_face_verts(int seed, int level, int32_t* face_verts, int* verts_per_face) {
+  if ((seed != LPM_SEED_ICOS_TRI && seed != LPM_SEED_CUBED) || level < 0 || level > 10) return LPM_ERR_INVALID_ARGUMENT;
+  lpm::TreeMesh m(lpm::kSeeds[seed]);
+  m.refine(level);
+  if (verts_per_face) *verts_per_face = m.vertsPerFace();
+  if (face_verts) std::memcpy(face_verts, m.faceVerts().data(), sizeof(int32_t) * m.faceVerts().size());
   return LPM_OK;
 }
 

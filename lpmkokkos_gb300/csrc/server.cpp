@@ -3,20 +3,20 @@
 // Three host threads share one GPU:
 //   prep       admits queued requests first-come first-served while their estimated device
 //              footprint fits the HBM budget, then builds the mesh (cached per seed/level/
-//              flags together with its target/source plan), evaluates the initial vorticity and
-//              writes the initial state into a pinned host buffer.
-//   gpu        owns every device object.  Each iteration it uploads the requests that became
-//              ready (upload stream, stream-ordered allocation from a private pool), evaluates
-//              their initial velocity, and advances every running solve.  Running solves are
+//              flags together with its target/source plan) and the pinned host buffer of the
+//              initial state (initial vorticity on the host only with the host_ic option).
+//   gpu        owns every device object.  It uploads the requests that became ready (upload
+//              stream, stream-ordered allocation from a private pool), evaluates their initial
+//              vorticity and velocity, and advances every running solve.  Running solves are
 //              grouped in size classes (log4 of pairs per evaluation); a class is one batch
 //              whose RK4 step is one CUDA graph of 13 launches, each of the four evaluations one
-//              persistent pair-kernel launch over all the class's solves.  The most expensive
-//              class takes one step per iteration, cheaper classes several (a measured time
-//              share), so small requests do not wait one large step per step of their own.  A
-//              class's batch (work items, tables, graph) is rebuilt only when its membership
-//              changes.  A solve that has taken its steps is copied back into its pinned
-//              buffer and its device memory is freed in stream order; nothing waits for the
-//              GPU except the pacing wait that keeps the host at most two iterations ahead.
+//              pair-kernel launch over all the class's solves, run on the class's lane -- a
+//              compute stream whose priority falls with the cost.  Classes advance at their own
+//              pace, so a small request does not wait for the steps of a large one.  A class's
+//              batch (work items, tables, graph) is rebuilt only when its membership changes.
+//              A solve that has taken its steps is copied back into its pinned buffer and its
+//              device memory is freed in stream order; the thread sleeps until a host function
+//              queued behind a burst of steps, or a new request, wakes it.
 //   completion waits on each finished solve's copy event, marks it done, returns its budget
 //              reservation and wakes waiters and the admission loop.
 // A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
@@ -79,7 +79,10 @@ struct Req {
   int64_t nv = 0, nf = 0, nl = 0;
   std::shared_ptr<const MeshHost> mesh;  // held from preparation until the upload
   char* host = nullptr;                  // pinned state buffer (Layout)
+  std::vector<double> gc, ga;            // Gaussian-vortex centres (ng x 3) and amplitudes
   // owned by the gpu thread while running
+  int cls = 0;                     // size class: log4 of pairs per evaluation
+  cudaStream_t lane = nullptr;     // compute stream of its size class
   std::unique_ptr<SolvePlan> plan;
   DeviceArena mem;
   char* dev = nullptr;
@@ -100,14 +103,19 @@ struct lpm_bve_server {
   Precision prec = Precision::FP32C;
   PairShape shape = kDefaultFP32C;
   double eps = 0.0;
-  bool skip = false, quirk = true, renorm = false, rcp = false;
+  bool skip = false, quirk = true, renorm = false, rcp = false, hostIc = false;
   size_t budget = 0;
   int maxActive = 0;
-  cudaStream_t up = nullptr, compute = nullptr, cap = nullptr;
+  cudaStream_t up = nullptr, cap = nullptr;
+  std::vector<cudaStream_t> lanes;  // compute streams, lanes[0] the highest priority
   cudaMemPool_t pool = nullptr;
+  // wake-ups of the gpu thread: new requests, finished bursts (host callbacks), stop
+  std::mutex wmu;
+  std::condition_variable cvWork;
+  uint64_t wakeups = 0;
 
   std::mutex mu;
-  std::condition_variable cvPrep, cvGpu, cvComp, cvDone;
+  std::condition_variable cvPrep, cvComp, cvDone;
   bool stop = false, compStop = false;
   std::string fatal;  // non-empty once a CUDA error made the server unusable
   std::string err;    // last error of an API call
@@ -154,8 +162,8 @@ std::string validate(const lpm_bve_request& q) {
   if ((q.seed != LPM_SEED_ICOS_TRI && q.seed != LPM_SEED_CUBED) || q.level < 0 || q.level > 10)
     return "seed must be LPM_SEED_ICOS_TRI/CUBED and level 0..10";
   if (q.nsteps < 0 || !std::isfinite(q.dt) || !std::isfinite(q.omega)) return "nsteps must be >= 0 and dt, omega finite";
-  if (q.n_gaussians < 0 || q.n_gaussians > 4096 || (q.n_gaussians > 0 && !(q.gauss_width > 0.0)))
-    return "0..4096 Gaussians with a positive width";
+  if (q.n_gaussians < 0 || q.n_gaussians > LPM_IC_MAX_GAUSSIANS || (q.n_gaussians > 0 && !(q.gauss_width > 0.0)))
+    return "0..LPM_IC_MAX_GAUSSIANS Gaussians with a positive width";
   return std::string();
 }
 
@@ -204,9 +212,11 @@ std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) 
   return M;
 }
 
-// Host side of a request: mesh, initial vorticity (RH54 + seeded Gaussian vortices, as
-// BVESphere::init_vorticity evaluates an initial condition at vertices and faces), zero
-// velocity (computed on the GPU before the first step), pinned buffer.
+// Host side of a request: mesh, pinned buffer, Gaussian-vortex parameters, and -- with the
+// host_ic option -- the initial vorticity (RH54 + seeded Gaussian vortices, as
+// BVESphere::init_vorticity evaluates an initial condition at vertices and faces); otherwise
+// the GPU evaluates it after the upload.  Velocity starts at zero and is computed on the GPU
+// before the first step.
 void prepare(lpm_bve_server* S, Req* r) {
   r->mesh = meshFor(S, r->r.seed, r->r.level);
   const MeshHost& M = *r->mesh;
@@ -225,16 +235,33 @@ void prepare(lpm_bve_server* S, Req* r) {
   std::memcpy(r->host + L.maskByte, M.fmask.data(), M.fmask.size());
   std::fill(d + L.vvel, d + L.vvel + 3 * M.nv, 0.0);
   std::fill(d + L.fvel, d + L.fvel + 3 * M.nf, 0.0);
-  lpm_ic_rh54(d + L.vx, M.nv, d + L.vzeta);
-  lpm_ic_rh54(d + L.fx, M.nf, d + L.fzeta);
   const int ng = r->r.n_gaussians;
-  if (ng > 0) {
-    std::vector<double> c(3 * (size_t)ng), a((size_t)ng);
-    lpm_ic_gaussian_params(r->r.ic_seed, ng, -2.0, 2.0, c.data(), a.data());
-    lpm_ic_gaussians_add(d + L.vx, M.nv, c.data(), a.data(), ng, r->r.gauss_width, d + L.vzeta);
-    lpm_ic_gaussians_add(d + L.fx, M.nf, c.data(), a.data(), ng, r->r.gauss_width, d + L.fzeta);
+  r->gc.assign(3 * (size_t)ng, 0.0);
+  r->ga.assign((size_t)ng, 0.0);
+  if (ng > 0) lpm_ic_gaussian_params(r->r.ic_seed, ng, -2.0, 2.0, r->gc.data(), r->ga.data());
+  if (S->hostIc) {
+    lpm_ic_rh54(d + L.vx, M.nv, d + L.vzeta);
+    lpm_ic_rh54(d + L.fx, M.nf, d + L.fzeta);
+    if (ng > 0) {
+      lpm_ic_gaussians_add(d + L.vx, M.nv, r->gc.data(), r->ga.data(), ng, r->r.gauss_width, d + L.vzeta);
+      lpm_ic_gaussians_add(d + L.fx, M.nf, r->gc.data(), r->ga.data(), ng, r->r.gauss_width, d + L.fzeta);
+    }
+  } else {
+    std::fill(d + L.vzeta, d + L.vzeta + M.nv, 0.0);
+    std::fill(d + L.fzeta, d + L.fzeta + M.nf, 0.0);
   }
 }
+
+// Wakes the gpu thread (new work, a finished burst, stop).  Also the host function queued
+// behind each burst: it takes only wmu, which no thread holds across a CUDA call.
+void wakeGpu(lpm_bve_server* S) {
+  {
+    std::lock_guard<std::mutex> lk(S->wmu);
+    S->wakeups += 1;
+  }
+  S->cvWork.notify_one();
+}
+void CUDART_CB burstDone(void* p) { wakeGpu(static_cast<lpm_bve_server*>(p)); }
 
 void prepLoop(lpm_bve_server* S) {
   cudaSetDevice(S->dev.device);
@@ -257,14 +284,16 @@ void prepLoop(lpm_bve_server* S) {
     }
     try {
       prepare(S, r);
-      std::lock_guard<std::mutex> lk(S->mu);
-      if (!S->fatal.empty()) {
-        r->mesh.reset();
-        failLocked(S, r, "server stopped after a device error: " + S->fatal);
-        continue;
+      {
+        std::lock_guard<std::mutex> lk(S->mu);
+        if (!S->fatal.empty()) {
+          r->mesh.reset();
+          failLocked(S, r, "server stopped after a device error: " + S->fatal);
+          continue;
+        }
+        S->prepared.push_back(r);
       }
-      S->prepared.push_back(r);
-      S->cvGpu.notify_one();
+      wakeGpu(S);
     } catch (const Error& e) {
       std::lock_guard<std::mutex> lk(S->mu);
       r->mesh.reset();
@@ -277,16 +306,45 @@ void prepLoop(lpm_bve_server* S) {
   }
 }
 
-// Uploads a prepared request and builds its plan (upload stream; stream-ordered allocation).
+int costClass(double pairsPerEval) {
+  int c = 0;
+  while (pairsPerEval >= 4.0 && c < 40) {
+    pairsPerEval /= 4.0;
+    ++c;
+  }
+  return c;
+}
+
+// Compute stream of a size class: two classes (a factor 16 in pairs, one mesh level) per
+// priority level, the cheapest classes (up to icosahedral level 4) on the highest priority.
+cudaStream_t laneOf(const lpm_bve_server* S, int cls) {
+  const int n = (int)S->lanes.size();
+  const int i = std::max(0, std::min(n - 1, (cls - 11) / 2));
+  return S->lanes[i];
+}
+
+// Uploads a prepared request and builds its plan (upload stream; stream-ordered allocation,
+// freed in order on the request's lane).
 void setupSolve(lpm_bve_server* S, Req* r) {
   const MeshHost& M = *r->mesh;
   r->nv = M.nv;
   r->nf = M.nf;
+  r->cls = costClass((double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl);
+  r->lane = laneOf(S, r->cls);
   const Layout L(M.nv, M.nf);
-  r->mem.streamOrdered(S->up, S->compute, S->pool);
+  r->mem.streamOrdered(S->up, r->lane, S->pool);
   r->dev = r->mem.alloc<char>(L.bytes);
   LPM_CUDA(cudaMemcpyAsync(r->dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, S->up));
   double* d = reinterpret_cast<double*>(r->dev);
+  if (!S->hostIc) {
+    const int ng = r->r.n_gaussians;
+    for (const auto& part : {std::make_pair(L.vx, L.vzeta), std::make_pair(L.fx, L.fzeta)}) {
+      const int64_t n = part.first == L.vx ? M.nv : M.nf;
+      const int rc = lpm_ic_rh54_gaussians_device(d + part.first, n, 3, 1, r->gc.data(), r->ga.data(), ng,
+                                                  r->r.gauss_width, d + part.second, (lpm_stream_t)S->up);
+      if (rc != LPM_OK) fail(rc, "initial vorticity on the device: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+  }
   ParticleIO io;
   io.na = M.nv;
   io.nb = M.nf;
@@ -299,22 +357,25 @@ void setupSolve(lpm_bve_server* S, Req* r) {
   io.barea = d + L.farea;
   const uint8_t* mask = reinterpret_cast<const uint8_t*>(r->dev + L.maskByte);
   r->plan.reset(new SolvePlan());
-  r->plan->mem.streamOrdered(S->up, S->compute, S->pool);
+  r->plan->mem.streamOrdered(S->up, r->lane, S->pool);
   buildSolve(*r->plan, Mode::RK4, S->prec, io, mask, S->skip, true, S->eps, S->shape.tileSize(), M.plan, S->up);
   r->plan->stage.dt = r->r.dt;
   r->plan->stage.omega = r->r.omega;
   r->pairsPerEval = (double)r->plan->nslots * r->plan->ns;
 }
 
-std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs) {
+// A batch over solves of one lane.  Its pair launches are not persistent: one CTA per work
+// item, so that kernels of higher-priority lanes are scheduled as soon as CTAs retire.
+std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs, cudaStream_t lane) {
   auto B = std::make_unique<Batch>();
   B->prec = S->prec;
   B->shape = S->shape;
   B->rk4 = true;
   B->rcpApprox = S->rcp;
-  B->mem.streamOrdered(S->up, S->compute, S->pool);
+  B->mem.streamOrdered(S->up, lane, S->pool);
   for (Req* r : rs) B->solves.push_back(r->plan.get());
   finalizeBatch(*B, S->dev, S->up);
+  B->grid = B->nitems;
   return B;
 }
 
@@ -338,9 +399,9 @@ void captureStep(lpm_bve_server* S, Batch& B) {
 // in stream order and hands it to the completion thread.
 void finish(lpm_bve_server* S, Req* r) {
   const Layout L(r->nv, r->nf);
-  LPM_CUDA(cudaMemcpyAsync(r->host, r->dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, S->compute));
+  LPM_CUDA(cudaMemcpyAsync(r->host, r->dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, r->lane));
   LPM_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming | cudaEventBlockingSync));
-  LPM_CUDA(cudaEventRecord(r->done, S->compute));
+  LPM_CUDA(cudaEventRecord(r->done, r->lane));
   r->plan.reset();
   r->mem.release();
   r->dev = nullptr;
@@ -349,56 +410,48 @@ void finish(lpm_bve_server* S, Req* r) {
   S->cvComp.notify_one();
 }
 
-// Size classes.  Solves are grouped by cost (log4 of target-source pairs per evaluation);
-// each class is one batch with its own captured step.  Per iteration the most expensive
-// class takes one step and every other class takes as many steps as fit in a share of that
-// step's time (measured per class, moving average), capped by the fewest steps any of its
-// solves has left.  A small request therefore finishes within one or two iterations of a
-// large one instead of one step per large-solve step, and the large solve's iteration grows by
-// at most kSmallShare of its step time.
-constexpr double kSmallShare = 1.0;
-constexpr int kMaxStepsPerIteration = 256;
+// Size classes and lanes.  Solves are grouped by cost (log4 of target-source pairs per
+// evaluation); a class is one batch whose RK4 step is one captured graph, launched on the
+// class's lane -- a compute stream whose priority falls with the cost.  Every class advances
+// at its own pace: up to kMaxInflight bursts in flight, a burst being as many steps as take
+// about kBurstMs (measured per class, moving average), capped by the fewest steps any of its
+// solves has left.  Pair launches of the server are not persistent, so the CTAs of a cheap
+// class's kernels start as soon as CTAs of an expensive one retire: a small request finishes
+// in milliseconds beside a level-8 solve instead of waiting out its seconds-long steps.  A
+// host function queued behind each burst wakes this thread when it completes.
+constexpr int kMaxInflight = 2;
+constexpr double kBurstMs = 10.0;
+constexpr int kMaxStepsPerBurst = 256;
+
+struct Burst {
+  cudaEvent_t e0, e1;
+  int steps;
+};
 
 struct SizeClass {
   std::vector<Req*> solves;
   std::unique_ptr<Batch> batch;
+  cudaStream_t lane = nullptr;
   bool changed = false;
   double msPerStep = -1.0;  // moving average of measured step time (-1: not measured yet)
   double pairsPerStep = 0.0;
+  std::deque<Burst> inflight;
 };
-
-struct StepTiming {  // events around one class's launches in one iteration
-  int cls;
-  int64_t iter;
-  int steps;
-  cudaEvent_t e0, e1;
-};
-
-int costClass(double pairsPerEval) {
-  int c = 0;
-  while (pairsPerEval >= 4.0 && c < 40) {
-    pairsPerEval /= 4.0;
-    ++c;
-  }
-  return c;
-}
 
 // Step time of a class before it has been measured: 4 evaluations at a nominal pair rate plus
 // the 13 launches of a graph-replayed step.
 double modelMs(const lpm_bve_server* S, double pairsPerStep) {
-  const double rate = S->prec == Precision::FP32C ? 1.6e12 : 1.2e10;
+  const double rate = S->prec == Precision::FP32C ? 2.2e12 : 1.2e10;
   return pairsPerStep / rate * 1e3 + 0.06;
 }
 
 void gpuLoop(lpm_bve_server* S) {
   cudaSetDevice(S->dev.device);
-  std::map<int, SizeClass> classes;  // key: cost class
+  std::map<int, SizeClass> classes;  // key: size class
   int nActive = 0;
-  cudaEvent_t stepEv[2] = {nullptr, nullptr};
   cudaEvent_t upEv = nullptr;
   std::vector<cudaEvent_t> evPool;
-  std::deque<StepTiming> timings;
-  int64_t iter = 0;
+  uint64_t seenWakeups = 0;
   Clock::time_point tick = Clock::now();
   auto getEvent = [&]() {
     if (!evPool.empty()) {
@@ -416,13 +469,11 @@ void gpuLoop(lpm_bve_server* S) {
     return v;
   };
   try {
-    for (auto& e : stepEv) LPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming | cudaEventBlockingSync));
     LPM_CUDA(cudaEventCreateWithFlags(&upEv, cudaEventDisableTiming));
     for (;;) {
       std::vector<Req*> joiners;
       {
-        std::unique_lock<std::mutex> lk(S->mu);
-        if (nActive == 0) S->cvGpu.wait(lk, [&] { return S->stop || !S->prepared.empty(); });
+        std::lock_guard<std::mutex> lk(S->mu);
         if (S->stop) break;
         joiners.assign(S->prepared.begin(), S->prepared.end());
         S->prepared.clear();
@@ -446,19 +497,27 @@ void gpuLoop(lpm_bve_server* S) {
         }
         r->mesh.reset();
       }
-      std::unique_ptr<Batch> init;
-      if (!ok.empty()) init = makeBatch(S, ok);  // initial velocity of the newcomers
+      std::map<int, std::vector<Req*>> byClass;
+      for (Req* r : ok) byClass[r->cls].push_back(r);
+      std::vector<std::pair<cudaStream_t, std::unique_ptr<Batch>>> inits;  // initial velocity per class
       std::vector<Req*> noSteps;
-      for (Req* r : ok) {
-        if (r->r.nsteps > 0) {
-          SizeClass& C = classes[costClass(r->pairsPerEval)];
-          C.solves.push_back(r);
-          C.changed = true;
-          ++nActive;
-        } else {
-          noSteps.push_back(r);
+      for (auto& kv : byClass) {
+        const cudaStream_t lane = kv.second.front()->lane;
+        inits.emplace_back(lane, makeBatch(S, kv.second, lane));
+        for (Req* r : kv.second) {
+          if (r->r.nsteps > 0) {
+            SizeClass& C = classes[kv.first];
+            C.lane = lane;
+            C.solves.push_back(r);
+            C.changed = true;
+            ++nActive;
+          } else {
+            noSteps.push_back(r);
+          }
         }
       }
+      // 2. rebuild the batches of classes whose membership changed
+      std::vector<cudaStream_t> waiting;
       for (auto it = classes.begin(); it != classes.end();) {
         SizeClass& C = it->second;
         if (C.changed) {
@@ -466,21 +525,30 @@ void gpuLoop(lpm_bve_server* S) {
           C.pairsPerStep = 0.0;
           for (Req* r : C.solves) C.pairsPerStep += 4.0 * r->pairsPerEval;
           if (!C.solves.empty()) {
-            C.batch = makeBatch(S, C.solves);
+            C.batch = makeBatch(S, C.solves, C.lane);
             captureStep(S, *C.batch);
+            waiting.push_back(C.lane);
           }
           C.changed = false;
         }
-        if (C.solves.empty()) it = classes.erase(it);
-        else ++it;
+        if (C.solves.empty() && C.inflight.empty()) {
+          it = classes.erase(it);
+        } else {
+          ++it;
+        }
       }
-      LPM_CUDA(cudaEventRecord(upEv, S->up));
-      LPM_CUDA(cudaStreamWaitEvent(S->compute, upEv, 0));
-      if (init) {
-        enqueueEval(*init, 0, 0, false, true, S->compute);
-        init.reset();
+      for (auto& in : inits) waiting.push_back(in.first);
+      if (!waiting.empty()) {
+        LPM_CUDA(cudaEventRecord(upEv, S->up));
+        std::sort(waiting.begin(), waiting.end());
+        waiting.erase(std::unique(waiting.begin(), waiting.end()), waiting.end());
+        for (cudaStream_t l : waiting) LPM_CUDA(cudaStreamWaitEvent(l, upEv, 0));
       }
-      {
+      for (auto& in : inits) {
+        enqueueEval(*in.second, 0, 0, false, true, in.first);
+        in.second.reset();
+      }
+      if (!ok.empty()) {
         std::lock_guard<std::mutex> lk(S->mu);
         const Clock::time_point now = Clock::now();
         for (Req* r : ok) {
@@ -491,29 +559,42 @@ void gpuLoop(lpm_bve_server* S) {
         S->st.max_running_seen = std::max<int>(S->st.max_running_seen, nActive);
       }
       for (Req* r : noSteps) finish(S, r);
-      // 2. RK4 steps: the dominant class one, the others as many as their share allows
-      if (!classes.empty()) {
-        auto est = [&](const SizeClass& C) { return C.msPerStep > 0 ? C.msPerStep : modelMs(S, C.pairsPerStep); };
-        int dom = classes.begin()->first;
-        for (auto& kv : classes)
-          if (est(kv.second) > est(classes[dom])) dom = kv.first;
-        const double domMs = est(classes[dom]);
-        const int others = (int)classes.size() - 1;
-        double pairs = 0.0;
-        int64_t solveSteps = 0;
-        for (auto it = classes.begin(); it != classes.end(); ++it) {  // cheapest first: small results leave early
-          SizeClass& C = it->second;
+      // 3. fold in the bursts that have completed
+      for (auto& kv : classes) {
+        SizeClass& C = kv.second;
+        while (!C.inflight.empty()) {
+          const cudaError_t q = cudaEventQuery(C.inflight.front().e1);
+          if (q == cudaErrorNotReady) break;
+          LPM_CUDA(q);
+          const Burst b = C.inflight.front();
+          C.inflight.pop_front();
+          float ms = 0.f;
+          LPM_CUDA(cudaEventElapsedTime(&ms, b.e0, b.e1));
+          const double per = ms / b.steps;
+          C.msPerStep = C.msPerStep > 0 ? 0.5 * (C.msPerStep + per) : per;
+          evPool.push_back(b.e0);
+          evPool.push_back(b.e1);
+        }
+      }
+      // 4. launch bursts on every lane that has room
+      bool launched = false;
+      double pairs = 0.0;
+      int64_t solveSteps = 0, classSteps = 0;
+      for (auto& kv : classes) {
+        SizeClass& C = kv.second;
+        while (C.batch && !C.solves.empty() && (int)C.inflight.size() < kMaxInflight) {
           int left = INT_MAX;
           for (Req* r : C.solves) left = std::min(left, r->r.nsteps - r->stepsDone);
-          int k = 1;
-          if (it->first != dom && others > 0)
-            k = (int)std::floor(kSmallShare * domMs / (others * est(C)));
-          k = std::max(1, std::min({k, left, kMaxStepsPerIteration}));
-          StepTiming T{it->first, iter, k, getEvent(), getEvent()};
-          LPM_CUDA(cudaEventRecord(T.e0, S->compute));
-          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(C.batch->graph, S->compute));
-          LPM_CUDA(cudaEventRecord(T.e1, S->compute));
-          timings.push_back(T);
+          const double est = C.msPerStep > 0 ? C.msPerStep : modelMs(S, C.pairsPerStep);
+          const int k = std::max(1, std::min({(int)(kBurstMs / est), left, kMaxStepsPerBurst}));
+          Burst b{getEvent(), getEvent(), k};
+          LPM_CUDA(cudaEventRecord(b.e0, C.lane));
+          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(C.batch->graph, C.lane));
+          LPM_CUDA(cudaEventRecord(b.e1, C.lane));
+          LPM_CUDA(cudaLaunchHostFunc(C.lane, burstDone, S));
+          C.inflight.push_back(b);
+          launched = true;
+          classSteps += k;
           std::vector<Req*> still;
           for (Req* r : C.solves) {
             r->stepsDone += k;
@@ -528,30 +609,26 @@ void gpuLoop(lpm_bve_server* S) {
             }
           }
           C.solves.swap(still);
-          if (C.changed) C.batch.reset();
+          if (C.changed) {
+            C.batch.reset();
+            break;  // rebuilt before its next burst
+          }
         }
+      }
+      if (launched) {
         std::lock_guard<std::mutex> lk(S->mu);
-        S->st.steps_run += 1;
+        S->st.steps_run += classSteps;
         S->st.solve_steps += solveSteps;
         S->st.pairs += pairs;
       }
-      // 3. pacing: at most two iterations in flight; then fold in the finished iterations' timings
-      LPM_CUDA(cudaEventRecord(stepEv[iter & 1], S->compute));
-      if (iter > 0) LPM_CUDA(cudaEventSynchronize(stepEv[(iter - 1) & 1]));
-      while (!timings.empty() && timings.front().iter < iter) {
-        StepTiming T = timings.front();
-        timings.pop_front();
-        float ms = 0.f;
-        LPM_CUDA(cudaEventElapsedTime(&ms, T.e0, T.e1));
-        auto it = classes.find(T.cls);
-        if (it != classes.end()) {
-          const double per = ms / T.steps;
-          it->second.msPerStep = it->second.msPerStep > 0 ? 0.5 * (it->second.msPerStep + per) : per;
-        }
-        evPool.push_back(T.e0);
-        evPool.push_back(T.e1);
-      }
-      ++iter;
+      bool rebuild = false;
+      for (auto& kv : classes) rebuild |= kv.second.changed;
+      if (launched || rebuild || !ok.empty()) continue;
+      // 5. nothing to launch: sleep until a burst completes or work arrives (bounded wait)
+      std::unique_lock<std::mutex> lk(S->wmu);
+      S->cvWork.wait_for(lk, std::chrono::milliseconds(nActive > 0 ? 50 : 500),
+                         [&] { return S->wakeups != seenWakeups; });
+      seenWakeups = S->wakeups;
     }
   } catch (const Error& e) {
     std::lock_guard<std::mutex> lk(S->mu);
@@ -565,7 +642,7 @@ void gpuLoop(lpm_bve_server* S) {
   }
   const std::vector<Req*> active = allActive();
   for (auto& kv : classes) kv.second.batch.reset();
-  cudaStreamSynchronize(S->compute);
+  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
   cudaStreamSynchronize(S->up);
   for (Req* r : active) {  // abandoned at shutdown
     r->plan.reset();
@@ -575,13 +652,12 @@ void gpuLoop(lpm_bve_server* S) {
     std::lock_guard<std::mutex> lk(S->mu);
     for (Req* r : active) failLocked(S, r, "server destroyed while the request was running");
   }
-  for (auto& T : timings) {
-    cudaEventDestroy(T.e0);
-    cudaEventDestroy(T.e1);
-  }
+  for (auto& kv : classes)
+    for (auto& b : kv.second.inflight) {
+      cudaEventDestroy(b.e0);
+      cudaEventDestroy(b.e1);
+    }
   for (cudaEvent_t e : evPool) cudaEventDestroy(e);
-  for (auto& e : stepEv)
-    if (e) cudaEventDestroy(e);
   if (upEv) cudaEventDestroy(upEv);
 }
 
@@ -654,13 +730,20 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     S->quirk = !(flags & LPM_BVE_RK4_FIX_QUIRK);
     S->renorm = flags & LPM_BVE_RENORM;
     S->rcp = flags & LPM_BVE_RCP_APPROX;
+    S->hostIc = opts && opts->host_ic;
     S->maxActive = opts ? opts->max_active : 0;
     size_t freeB = 0, totalB = 0;
     LPM_CUDA(cudaMemGetInfo(&freeB, &totalB));
     S->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : freeB / 10 * 8;
     S->st.budget_bytes = S->budget;
     LPM_CUDA(cudaStreamCreateWithFlags(&S->up, cudaStreamNonBlocking));
-    LPM_CUDA(cudaStreamCreateWithFlags(&S->compute, cudaStreamNonBlocking));
+    int least = 0, greatest = 0;  // lanes: one compute stream per priority level
+    LPM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    for (int p = greatest; p <= least; ++p) {
+      cudaStream_t l = nullptr;
+      LPM_CUDA(cudaStreamCreateWithPriority(&l, cudaStreamNonBlocking, p));
+      S->lanes.push_back(l);
+    }
     LPM_CUDA(cudaStreamCreateWithFlags(&S->cap, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -672,8 +755,9 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
   } catch (const Error& e) {
     std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.msg.c_str());
     if (S->pool) cudaMemPoolDestroy(S->pool);
-    for (cudaStream_t s : {S->up, S->compute, S->cap})
+    for (cudaStream_t s : {S->up, S->cap})
       if (s) cudaStreamDestroy(s);
+    for (cudaStream_t l : S->lanes) cudaStreamDestroy(l);
     return e.code;
   }
   lpm_bve_server* raw = S.release();
@@ -807,6 +891,29 @@ int lpm_bve_server_result(lpm_bve_server* S, int64_t id, int64_t* nverts, int64_
   return LPM_OK;
 }
 
+int lpm_bve_server_snapshot(lpm_bve_server* S, int64_t id, const char* path) {
+  if (!S || !path) return LPM_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> lk(S->mu);
+  Req* r = findLocked(S, id);
+  if (!r || r->state != LPM_REQ_DONE || !r->host) {
+    S->err = "snapshot: request has not finished (or was released)";
+    return LPM_ERR_STATE;
+  }
+  try {
+    const Layout L(r->nv, r->nf);
+    const double* d = reinterpret_cast<const double*>(r->host);
+    int vpf = 0;
+    lpm_mesh_face_verts(r->r.seed, r->r.level, nullptr, &vpf);
+    writeSnapshotHost(path, r->r.seed, r->r.level, vpf, r->nv, r->nf, r->r.nsteps * r->r.dt, r->r.dt, r->r.omega,
+                      d + L.vx, d + L.vzeta, d + L.vvel, d + L.fx, d + L.fzeta, d + L.fvel, d + L.farea,
+                      reinterpret_cast<const uint8_t*>(r->host + L.maskByte));
+  } catch (const Error& e) {
+    S->err = e.msg;
+    return e.code;
+  }
+  return LPM_OK;
+}
+
 int lpm_bve_server_release(lpm_bve_server* S, int64_t id) {
   if (!S) return LPM_ERR_INVALID_ARGUMENT;
   std::unique_ptr<Req> r;
@@ -876,7 +983,7 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
     S->stop = true;
   }
   S->cvPrep.notify_all();
-  S->cvGpu.notify_all();
+  wakeGpu(S);
   if (S->prepT.joinable()) S->prepT.join();
   if (S->gpuT.joinable()) S->gpuT.join();
   {
@@ -886,19 +993,19 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
   S->cvComp.notify_all();
   if (S->compT.joinable()) S->compT.join();
   cudaSetDevice(S->dev.device);
-  cudaStreamSynchronize(S->compute);
+  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
   cudaStreamSynchronize(S->up);
   for (auto& kv : S->reqs) {
     kv.second->plan.reset();
     kv.second->mem.release();
   }
-  cudaStreamSynchronize(S->compute);
+  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
   for (auto& kv : S->reqs)
     if (kv.second->host) cudaFreeHost(kv.second->host);
   S->reqs.clear();
   cudaMemPoolDestroy(S->pool);
   cudaStreamDestroy(S->up);
-  cudaStreamDestroy(S->compute);
+  for (cudaStream_t l : S->lanes) cudaStreamDestroy(l);
   cudaStreamDestroy(S->cap);
   delete S;
   return LPM_OK;

@@ -5,6 +5,8 @@
   * in FP64 the server's result is bitwise the single-solve path's: BVESphere initial
     condition + velocity, then lpm_bve_rk4_step (itself pinned to the oracle at 1e-12);
   * a request with zero steps returns the initial state with its velocity;
+  * the initial vorticity evaluated on the GPU (default) agrees with the host functions to
+    1e-13 relative, and the steps from it to 1e-10 (FP64);
   * the HBM budget admits one request at a time when only one fits, rejects a request that
     can never fit, and a queued request can be cancelled;
   * invalid requests are rejected; stats and latency quantiles are consistent.
@@ -73,7 +75,7 @@ def test_same_result_alone_and_in_the_mix(flags):
 def test_fp64_server_matches_single_solve_path(ctx):
     torch.cuda.set_device(0)
     seed, level, dt, nsteps, ic_seed, ng, width = 0, 3, 0.01, 3, 5, 3, 0.1
-    with bve.Server(0, flags=P.FP64) as srv:
+    with bve.Server(0, flags=P.FP64, host_ic=True) as srv:
         r0 = srv.submit(seed, level, dt, 0, ic_seed=ic_seed, n_gaussians=ng, gauss_width=width)
         r3 = srv.submit(seed, level, dt, nsteps, ic_seed=ic_seed, n_gaussians=ng, gauss_width=width)
         assert srv.wait(r0, WAIT) and srv.wait(r3, WAIT)
@@ -135,3 +137,24 @@ def test_invalid_requests_rejected():
         rid = srv.submit(0, 3, 0.01, 1)
         assert srv.wait(rid, WAIT)
         assert srv.stats()["submitted"] == 1
+
+
+def test_device_initial_condition_matches_host():
+    torch.cuda.set_device(0)
+    spec = dict(seed=1, level=4, dt=0.005, nsteps=0, ic_seed=21, n_gaussians=5, gauss_width=0.2)
+    out = {}
+    for host in (True, False):
+        with bve.Server(0, flags=P.FP64, host_ic=host) as srv:
+            r0 = srv.submit(**spec)
+            r2 = srv.submit(**dict(spec, nsteps=2))
+            assert srv.wait(r0, WAIT) and srv.wait(r2, WAIT)
+            out[host] = (srv.result(r0), srv.result(r2))
+    leaf = bve.build_mesh(1, 4)["fmask"] == 0
+    for k, tol in (("vzeta", 1e-13), ("fzeta", 1e-13), ("vvel", 1e-12)):
+        a, b = out[True][0][k], out[False][0][k]
+        assert np.abs(a - b).max() <= tol * np.abs(a).max(), k
+    for k in ("vx", "fx", "fvel"):
+        a, b = out[True][1][k], out[False][1][k]
+        if k.startswith("f"):
+            a, b = a[leaf], b[leaf]
+        assert np.abs(a - b).max() <= 1e-10 * np.abs(a).max(), k

@@ -114,3 +114,29 @@ def test_server_create_fails_cleanly_without_gpu(native):
     opts = L.ServerOpts(0, 0, 0, L.FP32C, 0.0)
     assert lib.lpm_bve_server_create(ctypes.byref(opts), ctypes.byref(h)) != L.LPM_OK
     assert not h.value
+
+
+def _lhuilier(a, b, c):
+    def arc(p, q):
+        return np.arctan2(np.linalg.norm(np.cross(p, q), axis=-1), np.sum(p * q, axis=-1))
+    s1, s2, s3 = arc(a, b), arc(b, c), arc(c, a)
+    h = 0.5 * (s1 + s2 + s3)
+    t = np.tan(0.5 * h) * np.tan(0.5 * (h - s1)) * np.tan(0.5 * (h - s2)) * np.tan(0.5 * (h - s3))
+    return 4 * np.arctan(np.sqrt(t))
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_face_connectivity_reproduces_areas(native, seed):
+    """lpm_mesh_face_verts: every leaf face's area equals the spherical polygon area of its
+    vertices fanned from the face centre (the reference's Faces area rule), to 1e-12 relative."""
+    from lpmkokkos_gb300 import bve
+    m = bve.build_mesh(seed, 3)
+    fv = bve.mesh_face_verts(seed, 3)
+    assert fv.shape == (m["nfaces"], 3 if seed == 0 else 4)
+    assert fv.min() >= 0 and fv.max() < m["nverts"]
+    v, c = m["vx"][fv], m["fx"]
+    n = fv.shape[1]
+    area = sum(_lhuilier(c, v[:, k], v[:, (k + 1) % n]) for k in range(n))
+    leaf = m["fmask"] == 0  # a divided parent passes its area to its children (area 0)
+    assert np.abs(area[leaf] - m["farea"][leaf]).max() <= 1e-12 * m["farea"].max()
+    assert (m["farea"][~leaf] == 0).all()
