@@ -4,8 +4,9 @@
  * tests/LpmBVETest.cpp:98-106 and :228-238) or netCDF (src/LpmNetCDF.hpp:23-103), both absent
  * here.  These entry points cover the same needs without those libraries:
  *   - a binary snapshot of every array of lpm_bve_state (positions, vorticity, velocity at
- *     vertices and faces, areas, mask) with the mesh seed/level, time, dt and Omega, so that a
- *     run restarts bit for bit;
+ *     vertices and faces, areas, mask) with the mesh seed/level, time, dt and Omega, restored bit
+ *     for bit (a run stepped on from it builds a new plan from the restored positions, so it
+ *     matches the uninterrupted run to the rounding of the summation order);
  *   - a legacy VTK PolyData file (vertices as points, leaf faces as polygons, relative vorticity
  *     and velocity as point and cell data, face area) that VTK readers and ParaView open.
  * Arrays may live on the device or the host (copies use cudaMemcpyDefault); every call

@@ -1,6 +1,6 @@
 // server.cpp -- continuous-batching BVE solve server (include/lpm_bve_server.h).
 //
-// Three host threads share one GPU:
+// Two host threads share one GPU:
 //   prep       admits queued requests first-come first-served while their estimated device
 //              footprint fits the HBM budget, then builds the mesh (cached per seed/level/
 //              flags together with its target/source plan) and the pinned host buffer of the
@@ -17,8 +17,8 @@
 //              A solve that has taken its steps is copied back into its pinned buffer and its
 //              device memory is freed in stream order; the thread sleeps until a host function
 //              queued behind a burst of steps, or a new request, wakes it.
-//   completion waits on each finished solve's copy event, marks it done, returns its budget
-//              reservation and wakes waiters and the admission loop.
+// A host function queued on a request's lane behind its copy-back marks it done, returns its
+// budget reservation and wakes waiters and the admission loop.
 // A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
 // summation order depend on nothing but its own mesh and the launch shape, fixed per server.
 
@@ -33,8 +33,11 @@
 #include <deque>
 #include <map>
 #include <mutex>
+#include <set>
 #include <thread>
 #include <tuple>
+
+struct lpm_bve_server;
 
 namespace lpm {
 namespace server {
@@ -69,6 +72,79 @@ struct Layout {
   }
 };
 
+// Page-locked host memory for request states.  cudaHostAlloc is an implicit synchronisation
+// point (work issued after it does not overlap work issued before it) and cudaFreeHost waits
+// for the device, so requests never call either: they take blocks of slabs that are allocated
+// only when the pool must grow (at least kSlabBytes at a time) and kept until the server is
+// destroyed.  First fit over an address-ordered free list, neighbours coalesced on free.
+class PinnedPool {
+ public:
+  static constexpr size_t kSlabBytes = size_t(256) << 20;
+  static constexpr size_t kAlign = 256;
+  ~PinnedPool() {
+    for (auto& sl : slabs_) cudaFreeHost(sl.first);
+  }
+  char* alloc(size_t bytes) {
+    bytes = (bytes + kAlign - 1) / kAlign * kAlign;
+    std::lock_guard<std::mutex> lk(mu_);
+    for (auto it = free_.begin(); it != free_.end(); ++it) {
+      if (it->second >= bytes) {
+        char* p = it->first;
+        const size_t rest = it->second - bytes;
+        free_.erase(it);
+        if (rest) free_[p + bytes] = rest;
+        used_[p] = bytes;
+        return p;
+      }
+    }
+    const size_t slab = std::max(kSlabBytes, bytes);
+    void* q = nullptr;
+    const cudaError_t e = cudaHostAlloc(&q, slab, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      fail(LPM_ERR_OUT_OF_MEMORY, "pinned host memory (%zu bytes): %s", slab, cudaGetErrorString(e));
+    }
+    char* p = static_cast<char*>(q);
+    slabs_.emplace_back(p, slab);
+    if (slab > bytes) free_[p + bytes] = slab - bytes;
+    used_[p] = bytes;
+    return p;
+  }
+  void release(char* p) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    auto u = used_.find(p);
+    if (u == used_.end()) return;
+    size_t len = u->second;
+    used_.erase(u);
+    auto next = free_.lower_bound(p);
+    if (next != free_.end() && p + len == next->first && sameSlab(p, next->first)) {
+      len += next->second;
+      next = free_.erase(next);
+    }
+    if (next != free_.begin()) {
+      auto prev = std::prev(next);
+      if (prev->first + prev->second == p && sameSlab(prev->first, p)) {
+        prev->second += len;
+        return;
+      }
+    }
+    free_[p] = len;
+  }
+
+ private:
+  bool sameSlab(const char* a, const char* b) const {
+    for (const auto& sl : slabs_) {
+      const bool ina = a >= sl.first && a < sl.first + sl.second, inb = b >= sl.first && b < sl.first + sl.second;
+      if (ina || inb) return ina && inb;
+    }
+    return false;
+  }
+  std::mutex mu_;
+  std::vector<std::pair<char*, size_t>> slabs_;
+  std::map<char*, size_t> free_, used_;
+};
+
 struct Req {
   int64_t id = 0;
   lpm_bve_request r{};
@@ -88,7 +164,7 @@ struct Req {
   char* dev = nullptr;
   int stepsDone = 0;
   double pairsPerEval = 0.0;
-  cudaEvent_t done = nullptr;
+  lpm_bve_server* owner = nullptr;  // for the host function that marks the request done
 };
 
 }  // namespace server
@@ -107,28 +183,31 @@ struct lpm_bve_server {
   size_t budget = 0;
   int maxActive = 0;
   cudaStream_t up = nullptr, cap = nullptr;
-  std::vector<cudaStream_t> lanes;  // compute streams, lanes[0] the highest priority
+  std::map<int, cudaStream_t> lanes;  // compute stream per size class (gpu thread creates them)
+  int prioLeast = 0, prioGreatest = 0;  // stream priority range of the device
   cudaMemPool_t pool = nullptr;
+  std::unique_ptr<PinnedPool> pinned = std::make_unique<PinnedPool>();
   // wake-ups of the gpu thread: new requests, finished bursts (host callbacks), stop
   std::mutex wmu;
   std::condition_variable cvWork;
   uint64_t wakeups = 0;
 
   std::mutex mu;
-  std::condition_variable cvPrep, cvComp, cvDone;
-  bool stop = false, compStop = false;
+  std::condition_variable cvPrep, cvDone;
+  bool stop = false;
   std::string fatal;  // non-empty once a CUDA error made the server unusable
   std::string err;    // last error of an API call
   int64_t nextId = 1;
   std::map<int64_t, std::unique_ptr<Req>> reqs;
-  std::deque<Req*> queued, prepared, completing;
+  std::deque<Req*> queued, prepared;
+  std::set<Req*> finishing;  // last step and copy-back queued, not yet complete
   size_t reserved = 0;
   int inflight = 0;  // admitted and not finished
   lpm_bve_server_counters st{};
   std::vector<double> latencies;
   std::map<std::tuple<int, int, int>, std::shared_ptr<const MeshHost>> meshes;  // prep thread only
   std::deque<std::tuple<int, int, int>> meshOrder;
-  std::thread prepT, gpuT, compT;
+  std::thread prepT, gpuT;
 };
 
 namespace lpm {
@@ -221,13 +300,7 @@ void prepare(lpm_bve_server* S, Req* r) {
   r->mesh = meshFor(S, r->r.seed, r->r.level);
   const MeshHost& M = *r->mesh;
   const Layout L(M.nv, M.nf);
-  void* p = nullptr;
-  const cudaError_t e = cudaHostAlloc(&p, L.bytes, cudaHostAllocDefault);
-  if (e != cudaSuccess) {
-    (void)cudaGetLastError();
-    fail(LPM_ERR_OUT_OF_MEMORY, "pinned host buffer (%zu bytes): %s", L.bytes, cudaGetErrorString(e));
-  }
-  r->host = static_cast<char*>(p);
+  r->host = S->pinned->alloc(L.bytes);
   double* d = reinterpret_cast<double*>(r->host);
   std::memcpy(d + L.vx, M.vx.data(), sizeof(double) * M.vx.size());
   std::memcpy(d + L.fx, M.fx.data(), sizeof(double) * M.fx.size());
@@ -315,12 +388,18 @@ int costClass(double pairsPerEval) {
   return c;
 }
 
-// Compute stream of a size class: two classes (a factor 16 in pairs, one mesh level) per
-// priority level, the cheapest classes (up to icosahedral level 4) on the highest priority.
-cudaStream_t laneOf(const lpm_bve_server* S, int cls) {
-  const int n = (int)S->lanes.size();
-  const int i = std::max(0, std::min(n - 1, (cls - 11) / 2));
-  return S->lanes[i];
+// Compute stream of a size class, created on first use: one stream per class, so classes of
+// equal priority still run side by side; two classes (a factor 16 in pairs, one mesh level)
+// per priority level, the cheapest (up to icosahedral level 4) on the highest priority.
+cudaStream_t laneOf(lpm_bve_server* S, int cls) {
+  auto it = S->lanes.find(cls);
+  if (it != S->lanes.end()) return it->second;
+  const int levels = S->prioLeast - S->prioGreatest + 1;
+  const int i = std::max(0, std::min(levels - 1, (cls - 11) / 2));
+  cudaStream_t l = nullptr;
+  LPM_CUDA(cudaStreamCreateWithPriority(&l, cudaStreamNonBlocking, S->prioGreatest + i));
+  S->lanes[cls] = l;
+  return l;
 }
 
 // Uploads a prepared request and builds its plan (upload stream; stream-ordered allocation,
@@ -379,7 +458,10 @@ std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs,
   return B;
 }
 
-void captureStep(lpm_bve_server* S, Batch& B) {
+// Captures one RK4 step of B and installs it in `exec`: updated in place when exec exists (the
+// update affects only later launches, so launches in flight keep their parameters), instantiated
+// otherwise.  Membership changes then never instantiate or destroy an executable graph.
+void installStep(lpm_bve_server* S, Batch& B, cudaGraphExec_t& exec) {
   cudaGraph_t g = nullptr;
   LPM_CUDA(cudaStreamBeginCapture(S->cap, cudaStreamCaptureModeThreadLocal));
   try {
@@ -390,24 +472,52 @@ void captureStep(lpm_bve_server* S, Batch& B) {
     throw;
   }
   LPM_CUDA(cudaStreamEndCapture(S->cap, &g));
-  const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
+  cudaError_t ie = cudaSuccess;
+  if (exec) {
+    cudaGraphExecUpdateResultInfo info{};
+    if (cudaGraphExecUpdate(exec, g, &info) != cudaSuccess) {  // topology changed: rebuild
+      (void)cudaGetLastError();
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+  }
+  if (!exec) ie = cudaGraphInstantiate(&exec, g, 0);
   cudaGraphDestroy(g);
   LPM_CUDA(ie);
 }
 
+// Host function queued on a request's lane behind its copy-back: the request is done.  It runs
+// on a CUDA thread and takes only S->mu, which no thread holds across a CUDA call.
+void CUDART_CB requestDone(void* p) {
+  Req* r = static_cast<Req*>(p);
+  lpm_bve_server* S = r->owner;
+  std::lock_guard<std::mutex> lk(S->mu);
+  S->finishing.erase(r);
+  if (r->state != LPM_REQ_RUNNING) return;  // failed meanwhile by a device error
+  r->state = LPM_REQ_DONE;
+  r->tDone = Clock::now();
+  S->reserved -= r->est;
+  S->inflight -= 1;
+  S->st.completed += 1;
+  S->latencies.push_back(seconds(r->tSubmit, r->tDone));
+  S->cvDone.notify_all();
+  S->cvPrep.notify_all();
+}
+
 // Queues the copy of a finished solve's state into its pinned buffer, frees its device memory
-// in stream order and hands it to the completion thread.
+// in stream order, and queues requestDone behind both on the request's lane.
 void finish(lpm_bve_server* S, Req* r) {
   const Layout L(r->nv, r->nf);
   LPM_CUDA(cudaMemcpyAsync(r->host, r->dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, r->lane));
-  LPM_CUDA(cudaEventCreateWithFlags(&r->done, cudaEventDisableTiming | cudaEventBlockingSync));
-  LPM_CUDA(cudaEventRecord(r->done, r->lane));
   r->plan.reset();
   r->mem.release();
   r->dev = nullptr;
-  std::lock_guard<std::mutex> lk(S->mu);
-  S->completing.push_back(r);
-  S->cvComp.notify_one();
+  r->owner = S;
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    S->finishing.insert(r);
+  }
+  LPM_CUDA(cudaLaunchHostFunc(r->lane, requestDone, r));
 }
 
 // Size classes and lanes.  Solves are grouped by cost (log4 of target-source pairs per
@@ -448,6 +558,7 @@ double modelMs(const lpm_bve_server* S, double pairsPerStep) {
 void gpuLoop(lpm_bve_server* S) {
   cudaSetDevice(S->dev.device);
   std::map<int, SizeClass> classes;  // key: size class
+  std::map<int, cudaGraphExec_t> execs;  // captured step per size class, kept while the server lives
   int nActive = 0;
   cudaEvent_t upEv = nullptr;
   std::vector<cudaEvent_t> evPool;
@@ -526,7 +637,7 @@ void gpuLoop(lpm_bve_server* S) {
           for (Req* r : C.solves) C.pairsPerStep += 4.0 * r->pairsPerEval;
           if (!C.solves.empty()) {
             C.batch = makeBatch(S, C.solves, C.lane);
-            captureStep(S, *C.batch);
+            installStep(S, *C.batch, execs[it->first]);
             waiting.push_back(C.lane);
           }
           C.changed = false;
@@ -589,7 +700,8 @@ void gpuLoop(lpm_bve_server* S) {
           const int k = std::max(1, std::min({(int)(kBurstMs / est), left, kMaxStepsPerBurst}));
           Burst b{getEvent(), getEvent(), k};
           LPM_CUDA(cudaEventRecord(b.e0, C.lane));
-          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(C.batch->graph, C.lane));
+          const cudaGraphExec_t exec = execs[kv.first];
+          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(exec, C.lane));
           LPM_CUDA(cudaEventRecord(b.e1, C.lane));
           LPM_CUDA(cudaLaunchHostFunc(C.lane, burstDone, S));
           C.inflight.push_back(b);
@@ -625,10 +737,16 @@ void gpuLoop(lpm_bve_server* S) {
       for (auto& kv : classes) rebuild |= kv.second.changed;
       if (launched || rebuild || !ok.empty()) continue;
       // 5. nothing to launch: sleep until a burst completes or work arrives (bounded wait)
-      std::unique_lock<std::mutex> lk(S->wmu);
-      S->cvWork.wait_for(lk, std::chrono::milliseconds(nActive > 0 ? 50 : 500),
-                         [&] { return S->wakeups != seenWakeups; });
-      seenWakeups = S->wakeups;
+      {
+        std::unique_lock<std::mutex> lk(S->wmu);
+        S->cvWork.wait_for(lk, std::chrono::milliseconds(nActive > 0 ? 50 : 500),
+                           [&] { return S->wakeups != seenWakeups; });
+        seenWakeups = S->wakeups;
+      }
+      for (auto& ln : S->lanes) {  // a device error stops the host functions: find it here
+        const cudaError_t q = cudaStreamQuery(ln.second);
+        if (q != cudaErrorNotReady) LPM_CUDA(q);
+      }
     }
   } catch (const Error& e) {
     std::lock_guard<std::mutex> lk(S->mu);
@@ -636,13 +754,15 @@ void gpuLoop(lpm_bve_server* S) {
     for (Req* r : allActive()) failLocked(S, r, "server stopped: " + e.msg);
     for (Req* r : S->prepared) failLocked(S, r, "server stopped: " + e.msg);
     for (Req* r : S->queued) failLocked(S, r, "server stopped: " + e.msg);
+    for (Req* r : S->finishing) failLocked(S, r, "server stopped: " + e.msg);
     S->prepared.clear();
     S->queued.clear();
+    S->finishing.clear();
     S->cvDone.notify_all();
   }
   const std::vector<Req*> active = allActive();
   for (auto& kv : classes) kv.second.batch.reset();
-  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
+  for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);
   for (Req* r : active) {  // abandoned at shutdown
     r->plan.reset();
@@ -658,38 +778,9 @@ void gpuLoop(lpm_bve_server* S) {
       cudaEventDestroy(b.e1);
     }
   for (cudaEvent_t e : evPool) cudaEventDestroy(e);
+  for (auto& kv : execs)
+    if (kv.second) cudaGraphExecDestroy(kv.second);
   if (upEv) cudaEventDestroy(upEv);
-}
-
-void completionLoop(lpm_bve_server* S) {
-  cudaSetDevice(S->dev.device);
-  for (;;) {
-    Req* r = nullptr;
-    {
-      std::unique_lock<std::mutex> lk(S->mu);
-      S->cvComp.wait(lk, [&] { return S->compStop || !S->completing.empty(); });
-      if (S->completing.empty()) return;
-      r = S->completing.front();
-      S->completing.pop_front();
-    }
-    const cudaError_t e = cudaEventSynchronize(r->done);
-    cudaEventDestroy(r->done);
-    r->done = nullptr;
-    std::lock_guard<std::mutex> lk(S->mu);
-    if (e != cudaSuccess) {
-      if (S->fatal.empty()) S->fatal = cudaGetErrorString(e);
-      failLocked(S, r, std::string("device error: ") + cudaGetErrorString(e));
-      continue;
-    }
-    r->state = LPM_REQ_DONE;
-    r->tDone = Clock::now();
-    S->reserved -= r->est;
-    S->inflight -= 1;
-    S->st.completed += 1;
-    S->latencies.push_back(seconds(r->tSubmit, r->tDone));
-    S->cvDone.notify_all();
-    S->cvPrep.notify_all();
-  }
 }
 
 Req* findLocked(lpm_bve_server* S, int64_t id) {
@@ -736,14 +827,13 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     LPM_CUDA(cudaMemGetInfo(&freeB, &totalB));
     S->budget = (opts && opts->hbm_budget_bytes) ? opts->hbm_budget_bytes : freeB / 10 * 8;
     S->st.budget_bytes = S->budget;
-    LPM_CUDA(cudaStreamCreateWithFlags(&S->up, cudaStreamNonBlocking));
-    int least = 0, greatest = 0;  // lanes: one compute stream per priority level
-    LPM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-    for (int p = greatest; p <= least; ++p) {
-      cudaStream_t l = nullptr;
-      LPM_CUDA(cudaStreamCreateWithPriority(&l, cudaStreamNonBlocking, p));
-      S->lanes.push_back(l);
-    }
+    int leastP = 0, greatestP = 0;
+    LPM_CUDA(cudaDeviceGetStreamPriorityRange(&leastP, &greatestP));
+    // uploads, initial-vorticity kernels and plan tables: small and waited for by the gpu
+    // thread, so they take the highest priority (else they queue behind a large class's CTAs)
+    LPM_CUDA(cudaStreamCreateWithPriority(&S->up, cudaStreamNonBlocking, greatestP));
+    S->prioLeast = leastP;
+    S->prioGreatest = greatestP;
     LPM_CUDA(cudaStreamCreateWithFlags(&S->cap, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -757,13 +847,12 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     if (S->pool) cudaMemPoolDestroy(S->pool);
     for (cudaStream_t s : {S->up, S->cap})
       if (s) cudaStreamDestroy(s);
-    for (cudaStream_t l : S->lanes) cudaStreamDestroy(l);
+    for (auto& ln : S->lanes) cudaStreamDestroy(ln.second);
     return e.code;
   }
   lpm_bve_server* raw = S.release();
   raw->prepT = std::thread(prepLoop, raw);
   raw->gpuT = std::thread(gpuLoop, raw);
-  raw->compT = std::thread(completionLoop, raw);
   *out = raw;
   return LPM_OK;
 }
@@ -929,7 +1018,7 @@ int lpm_bve_server_release(lpm_bve_server* S, int64_t id) {
     r = std::move(it->second);
     S->reqs.erase(it);
   }
-  if (r->host) cudaFreeHost(r->host);
+  S->pinned->release(r->host);
   return LPM_OK;
 }
 
@@ -986,26 +1075,19 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
   wakeGpu(S);
   if (S->prepT.joinable()) S->prepT.join();
   if (S->gpuT.joinable()) S->gpuT.join();
-  {
-    std::lock_guard<std::mutex> lk(S->mu);
-    S->compStop = true;
-  }
-  S->cvComp.notify_all();
-  if (S->compT.joinable()) S->compT.join();
   cudaSetDevice(S->dev.device);
-  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
+  for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);
   for (auto& kv : S->reqs) {
     kv.second->plan.reset();
     kv.second->mem.release();
   }
-  for (cudaStream_t l : S->lanes) cudaStreamSynchronize(l);
-  for (auto& kv : S->reqs)
-    if (kv.second->host) cudaFreeHost(kv.second->host);
+  for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   S->reqs.clear();
+  S->pinned.reset();
   cudaMemPoolDestroy(S->pool);
   cudaStreamDestroy(S->up);
-  for (cudaStream_t l : S->lanes) cudaStreamDestroy(l);
+  for (auto& ln : S->lanes) cudaStreamDestroy(ln.second);
   cudaStreamDestroy(S->cap);
   delete S;
   return LPM_OK;

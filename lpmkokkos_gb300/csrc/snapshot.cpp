@@ -7,7 +7,9 @@
 //     double omega; padding to 128 bytes
 //   then, row-major float64 unless noted: vx (nverts x 3), vzeta (nverts), vvel (nverts x 3),
 //     fx (nfaces x 3), fzeta (nfaces), fvel (nfaces x 3), farea (nfaces), fmask (nfaces bytes)
-// Every array of lpm_bve_state is saved, so a restart reproduces the run bit for bit.
+// Every array of lpm_bve_state is saved and restored bit for bit.  A run stepped on from a
+// restored state builds a new plan whose target/source order follows the restored positions,
+// so it sums in another order than the uninterrupted run: the two agree to that rounding.
 //
 // VTK: legacy PolyData ("vtk DataFile Version 3.0", BINARY, big-endian as the format requires):
 // POINTS = vertex positions, POLYGONS = leaf faces (mask 0) by their vertices, POINT_DATA
