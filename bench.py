@@ -47,6 +47,11 @@ def time_step(level: int) -> float:
     the reference's 1 - x.y denominator crosses zero for nearest neighbours."""
     return 0.01 * 2.0 ** (4 - level)
 OPS_PER_PAIR = 13  # FP32 FMA-pipe lane operations per velocity pair in the FP32C kernel
+# DRAM bytes per pair-kernel launch per particle (target + source): ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one level-6 launch, 6.91 MB for 150,182 targets + 81,920 sources
+# (profiles/pair_fp32c_icos_L6_ncu_full.md).  Traffic follows the O(N) inputs (each source tile
+# is re-read from L2, not DRAM), so it scales with targets + sources, not with pairs.
+TRAFFIC_BYTES_PER_PARTICLE = 6.91e6 / (150182 + 81920)
 
 
 def fma_peak(P, device):
@@ -323,7 +328,9 @@ def run_ours(args, rank, world, local_rank):
             "frac_of_nominal": achieved / peak_nominal,
             "pair_launch_ms_avg": pair_avg_ms,
             "pair_launches": pair_n,
-            "traffic": None,
+            "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
+            "traffic_note": "bytes per launch: ncu DRAM read+write of a level-6 launch scaled by targets+sources",
+            "algorithmic_bytes": 24 * (nv + nall) + 32 * nl,
         },
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": bytes_step,
                 "d2h_bytes_per_step": bytes_step, "steps": args.e2e_steps},

@@ -185,6 +185,7 @@ struct lpm_bve_server {
   cudaStream_t up = nullptr, cap = nullptr;
   std::map<int, cudaStream_t> lanes;  // compute stream per size class (gpu thread creates them)
   int prioLeast = 0, prioGreatest = 0;  // stream priority range of the device
+  int slots = 1;                         // resident CTAs of the pair kernel on the whole GPU
   cudaMemPool_t pool = nullptr;
   std::unique_ptr<PinnedPool> pinned = std::make_unique<PinnedPool>();
   // wake-ups of the gpu thread: new requests, finished bursts (host callbacks), stop
@@ -443,8 +444,8 @@ void setupSolve(lpm_bve_server* S, Req* r) {
   r->pairsPerEval = (double)r->plan->nslots * r->plan->ns;
 }
 
-// A batch over solves of one lane.  Its pair launches are not persistent: one CTA per work
-// item, so that kernels of higher-priority lanes are scheduled as soon as CTAs retire.
+// A batch over solves of one lane.  Its pair grid is set by shareSlots before its step is
+// captured (initial-velocity batches keep the persistent grid finalizeBatch chose).
 std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs, cudaStream_t lane) {
   auto B = std::make_unique<Batch>();
   B->prec = S->prec;
@@ -454,7 +455,6 @@ std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs,
   B->mem.streamOrdered(S->up, lane, S->pool);
   for (Req* r : rs) B->solves.push_back(r->plan.get());
   finalizeBatch(*B, S->dev, S->up);
-  B->grid = B->nitems;
   return B;
 }
 
@@ -522,14 +522,20 @@ void finish(lpm_bve_server* S, Req* r) {
 
 // Size classes and lanes.  Solves are grouped by cost (log4 of target-source pairs per
 // evaluation); a class is one batch whose RK4 step is one captured graph, launched on the
-// class's lane -- a compute stream whose priority falls with the cost.  Every class advances
-// at its own pace: up to kMaxInflight bursts in flight, a burst being as many steps as take
-// about kBurstMs (measured per class, moving average), capped by the fewest steps any of its
-// solves has left.  Pair launches of the server are not persistent, so the CTAs of a cheap
-// class's kernels start as soon as CTAs of an expensive one retire: a small request finishes
-// in milliseconds beside a level-8 solve instead of waiting out its seconds-long steps.  A
-// host function queued behind each burst wakes this thread when it completes.
+// class's own stream (lane).  Every class advances at its own pace: up to kMaxInflight bursts
+// in flight, a burst being as many steps as take about kBurstMs (measured per class, moving
+// average), capped by the fewest steps any of its solves has left.
+//
+// The classes share the GPU in space, not in time: each class's pair kernel is persistent
+// with a grid from shareSlots, which splits the resident CTA slots water-filling by demand
+// (classes with few work items get what they need, the rest is split evenly).  Measured on
+// GB300, stream priorities do not let a later kernel overtake the pending CTAs of a running
+// grid: a level-7 step beside non-persistent level-8 kernels took as long as a level-8 step.
+// With disjoint slot shares every class's kernels are resident at once, and a class's
+// prep / epilogue kernels run in the slots its own pair kernel frees.  A host function queued
+// behind each burst wakes this thread when it completes.
 constexpr int kMaxInflight = 2;
+constexpr double kLongStepMs = 50.0;
 constexpr double kBurstMs = 10.0;
 constexpr int kMaxStepsPerBurst = 256;
 
@@ -553,6 +559,24 @@ struct SizeClass {
 double modelMs(const lpm_bve_server* S, double pairsPerStep) {
   const double rate = S->prec == Precision::FP32C ? 2.2e12 : 1.2e10;
   return pairsPerStep / rate * 1e3 + 0.06;
+}
+
+// Pair-kernel grid of every class with a batch: water-filling of the resident CTA slots by
+// demand (work items), cheapest demand first.
+std::map<int, int> shareSlots(const std::map<int, SizeClass>& classes, int slots) {
+  std::vector<std::pair<int, int>> demand;  // (work items, class)
+  for (const auto& kv : classes)
+    if (kv.second.batch) demand.emplace_back(std::max(1, kv.second.batch->nitems), kv.first);
+  std::sort(demand.begin(), demand.end());
+  std::map<int, int> grid;
+  int remaining = slots;
+  for (size_t i = 0; i < demand.size(); ++i) {
+    const int share = std::max(1, remaining / (int)(demand.size() - i));
+    const int g = std::min(demand[i].first, share);
+    grid[demand[i].second] = g;
+    remaining = std::max(0, remaining - g);
+  }
+  return grid;
 }
 
 void gpuLoop(lpm_bve_server* S) {
@@ -637,7 +661,7 @@ void gpuLoop(lpm_bve_server* S) {
           for (Req* r : C.solves) C.pairsPerStep += 4.0 * r->pairsPerEval;
           if (!C.solves.empty()) {
             C.batch = makeBatch(S, C.solves, C.lane);
-            installStep(S, *C.batch, execs[it->first]);
+            C.batch->grid = 0;  // installed below with its share of the slots
             waiting.push_back(C.lane);
           }
           C.changed = false;
@@ -646,6 +670,14 @@ void gpuLoop(lpm_bve_server* S) {
           it = classes.erase(it);
         } else {
           ++it;
+        }
+      }
+      // the SM slots of the pair kernels, shared among the classes with a batch
+      for (const auto& kg : shareSlots(classes, S->slots)) {
+        SizeClass& C = classes[kg.first];
+        if (C.batch->grid != kg.second) {
+          C.batch->grid = kg.second;
+          installStep(S, *C.batch, execs[kg.first]);
         }
       }
       for (auto& in : inits) waiting.push_back(in.first);
@@ -693,10 +725,14 @@ void gpuLoop(lpm_bve_server* S) {
       int64_t solveSteps = 0, classSteps = 0;
       for (auto& kv : classes) {
         SizeClass& C = kv.second;
-        while (C.batch && !C.solves.empty() && (int)C.inflight.size() < kMaxInflight) {
+        for (;;) {
+          if (!C.batch || C.solves.empty()) break;
+          const double est = C.msPerStep > 0 ? C.msPerStep : modelMs(S, C.pairsPerStep);
+          // a class with long steps keeps one in flight, so a new slot share applies sooner
+          const int maxInflight = est >= kLongStepMs ? 1 : kMaxInflight;
+          if ((int)C.inflight.size() >= maxInflight) break;
           int left = INT_MAX;
           for (Req* r : C.solves) left = std::min(left, r->r.nsteps - r->stepsDone);
-          const double est = C.msPerStep > 0 ? C.msPerStep : modelMs(S, C.pairsPerStep);
           const int k = std::max(1, std::min({(int)(kBurstMs / est), left, kMaxStepsPerBurst}));
           Burst b{getEvent(), getEvent(), k};
           LPM_CUDA(cudaEventRecord(b.e0, C.lane));
@@ -834,6 +870,7 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     LPM_CUDA(cudaStreamCreateWithPriority(&S->up, cudaStreamNonBlocking, greatestP));
     S->prioLeast = leastP;
     S->prioGreatest = greatestP;
+    S->slots = std::max(1, pairBlocksPerSM(S->prec, S->shape, false) * S->dev.sms);
     LPM_CUDA(cudaStreamCreateWithFlags(&S->cap, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
