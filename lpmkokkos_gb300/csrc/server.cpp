@@ -532,9 +532,11 @@ void finish(lpm_bve_server* S, Req* r) {
 // GB300, stream priorities do not let a later kernel overtake the pending CTAs of a running
 // grid: a level-7 step beside non-persistent level-8 kernels took as long as a level-8 step.
 // With disjoint slot shares every class's kernels are resident at once, and a class's
-// prep / epilogue kernels run in the slots its own pair kernel frees.  A host function queued
+// prep / epilogue kernels run in the slots its own pair kernel frees; a small reserve of
+// slots stays out of every share for newcomers.  A host function queued
 // behind each burst wakes this thread when it completes.
 constexpr int kMaxInflight = 2;
+constexpr int kReserveFrac = 38;  // 1/38 of the slots: 8 of the 304 of the default shape
 constexpr double kLongStepMs = 50.0;
 constexpr double kBurstMs = 10.0;
 constexpr int kMaxStepsPerBurst = 256;
@@ -672,8 +674,11 @@ void gpuLoop(lpm_bve_server* S) {
           ++it;
         }
       }
-      // the SM slots of the pair kernels, shared among the classes with a batch
-      for (const auto& kg : shareSlots(classes, S->slots)) {
+      // the SM slots of the pair kernels, shared among the classes with a batch; kReserveFrac of
+      // them stay free so that a class that arrives while a long step is in flight (launched
+      // with the old shares) finds resident room at once
+      const int reserve = std::max(1, S->slots / kReserveFrac);
+      for (const auto& kg : shareSlots(classes, std::max(1, S->slots - reserve))) {
         SizeClass& C = classes[kg.first];
         if (C.batch->grid != kg.second) {
           C.batch->grid = kg.second;
