@@ -23,7 +23,7 @@ def test_product_mesh_equals_oracle_bitwise(native, oracle, seed, level):
 
 def test_mesh_counts(native):
     from lpmkokkos_gb300 import bve
-    # SURVEY table: icos L4/L7/L8 and cube L4/L7
+    # per-seed counts (n*AtTreeLevel, src/LpmMeshSeed.cpp:369-391): icos L4/L7/L8, cube L4/L7
     assert bve.mesh_counts(0, 4) == (2562, 6820, 5120)
     assert bve.mesh_counts(0, 7) == (163842, 436900, 327680)
     assert bve.mesh_counts(0, 8) == (655362, 1747620, 1310720)
