@@ -128,6 +128,9 @@ __device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc
   constexpr int P = K / 2;
   constexpr float kSign = NEWTON ? -1.f : 1.f;
   const float2 kMinusTwo = make_float2(-2.f, -2.f);
+  // sources per unrolled iteration: 2 with four target pairs per thread (measured 1 % faster
+  // than 4 at 128 x 8; 8 was 5 % slower), 4 otherwise
+  constexpr int kUnroll = K >= 8 ? 2 : 4;
 #pragma unroll 1
   for (int j0 = 0; j0 < nsrc; j0 += kSub) {
     float2 vx[P], vy[P], vz[P], vp[P], vw[P];
@@ -135,7 +138,7 @@ __device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc
     for (int m = 0; m < P; ++m) {
       vx[m] = vy[m] = vz[m] = vp[m] = vw[m] = make_float2(0.f, 0.f);
     }
-#pragma unroll 4
+#pragma unroll kUnroll
     for (int j = j0; j < j0 + kSub; ++j) {
       const float4 xy = T.xy[j];
       const float4 zw = T.zw[j];
