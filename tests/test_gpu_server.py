@@ -158,3 +158,25 @@ def test_device_initial_condition_matches_host():
         if k.startswith("f"):
             a, b = a[leaf], b[leaf]
         assert np.abs(a - b).max() <= 1e-10 * np.abs(a).max(), k
+
+
+def test_tiny_meshes_match_single_solve_path(ctx):
+    """Levels 0-2 of both seeds in one server (a work item smaller than a tile, one source
+    chunk), FP64 with the host initial condition: each equals BVESphere + lpm_bve_rk4_step."""
+    torch.cuda.set_device(0)
+    specs = [dict(seed=sd, level=lv, dt=0.01, nsteps=2, ic_seed=30 + 3 * sd + lv, n_gaussians=ng, gauss_width=0.3)
+             for sd in (0, 1) for lv, ng in ((0, 0), (1, 2), (2, 64))]
+    with bve.Server(0, flags=P.FP64, host_ic=True) as srv:
+        ids = [srv.submit(**sp) for sp in specs]
+        for rid in ids:
+            assert srv.wait(rid, WAIT)
+        got = [srv.result(rid) for rid in ids]
+    for sp, g in zip(specs, got):
+        s = bve.BVESphere(sp["seed"], sp["level"])
+        s.init_vorticity(bve.rh54_gaussians(sp["ic_seed"], sp["n_gaussians"], sp["gauss_width"]), ctx, flags=P.FP64)
+        ctx.rk4_step(s.state(), sp["dt"], OMEGA, sp["nsteps"], flags=P.FP64)
+        torch.cuda.synchronize()
+        want = dict(vx=s.physVerts, vzeta=s.relVortVerts, vvel=s.velocityVerts, fx=s.physFaces,
+                    fzeta=s.relVortFaces, fvel=s.velocityFaces)
+        for k in KEYS:
+            assert _same(g[k], want[k].cpu().numpy()), (sp, k)
