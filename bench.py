@@ -130,6 +130,16 @@ def mesh_sizes(level):
 # ------------------------------------------------------------------------------------------
 # clocks during the timed region
 # ------------------------------------------------------------------------------------------
+def gpu_uuid(local_rank):
+    """nvidia-smi id of this rank's GPU (its UUID), or None to query every visible GPU."""
+    try:
+        import torch
+        u = str(getattr(torch.cuda.get_device_properties(local_rank), "uuid", ""))
+        return ("GPU-" + u) if u and not u.startswith("GPU-") else (u or None)
+    except Exception:
+        return None
+
+
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -243,14 +253,7 @@ def run_ours(args, rank, world, local_rank):
             ctx.set_timing(False)
         return el, pair
 
-    gpu_uuid = None
-    try:
-        props = torch.cuda.get_device_properties(local_rank)
-        u = str(getattr(props, "uuid", ""))
-        gpu_uuid = ("GPU-" + u) if u and not u.startswith("GPU-") else (u or None)
-    except Exception:
-        gpu_uuid = None
-    sampler = ClockSampler(gpu_uuid)
+    sampler = ClockSampler(gpu_uuid(local_rank))
     # 1) instrumented pass: per-launch CUDA events around the pair kernel (direct launches)
     el_instr, (pair_ms, pair_n) = timed(args.steps, True)
     # 2) headline pass: graph-replayed steps (the product's default path)
@@ -510,7 +513,9 @@ def run_ensemble(args, rank, world, local_rank):
     torch.cuda.synchronize()
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
+    sampler = ClockSampler(gpu_uuid(local_rank))
     el = max_over_ranks(_timed_region(torch, stream, lambda: ens.step(dts, oms, 1), args.steps, flush), world, dev)
+    clocks = sampler.stop()
     steps_per_s = whole_job_rate(world, args.steps, el)
     alg = 0
     for sk, lv in picks:
@@ -531,6 +536,7 @@ def run_ensemble(args, rank, world, local_rank):
         "pair_interactions_per_s": world * 4 * alg * args.steps / (el * 1e-3),
         "computed_pairs_per_s": world * 4 * info["pairs_per_eval"] * args.steps / (el * 1e-3),
         "gpu_launches": 13 * args.steps, "init_s": t_init, "all_vertex_velocities_finite": finite,
+        "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -564,8 +570,10 @@ def run_large(args, rank, world, local_rank):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
     ctx.set_timing(True); ctx.timing()
+    sampler = ClockSampler(gpu_uuid(local_rank))
     el = _timed_region(torch, stream, lambda: ctx.rk4_step(st, dt, 2 * math.pi, 1, flags=P.FP32C, eps=eps),
                        args.steps, flush)
+    clocks = sampler.stop()
     pair_ms, pair_n = ctx.timing(); ctx.set_timing(False)
     el = max_over_ranks(el, world, dev)
     # stream function (and velocity) at every vertex and face
@@ -595,7 +603,7 @@ def run_large(args, rank, world, local_rank):
                      "unit": "Gpair/s", "frac": achieved / peak, "pair_launch_ms_avg": pair_ms / pair_n,
                      "peak_source": "FP32 FMA-pipe probe (FFMA / FFMA2, the larger) / 13 lane-ops per pair",
                      "probes": probes, "traffic": None},
-        "fp64_gpu": fp64, "init_s": t_init,
+        "fp64_gpu": fp64, "init_s": t_init, "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)
@@ -668,7 +676,7 @@ def run_server(args, rank, world, local_rank):
                 time.sleep(delay)
             ids[i] = srv.submit(**sp)
 
-    sampler = ClockSampler(os.environ.get("CUDA_VISIBLE_DEVICES", "").split(",")[0] or None)
+    sampler = ClockSampler(gpu_uuid(local_rank))
     t_start = time.perf_counter()
     th = threading.Thread(target=feeder)
     th.start()
