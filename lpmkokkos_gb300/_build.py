@@ -89,7 +89,7 @@ def build(verbose: bool = False) -> str:
     return LIB
 
 
-EXAMPLES = ["bve_solid_body"]
+EXAMPLES = ["bve_solid_body", "bve_serve"]
 
 
 def _build_examples(incs):
@@ -97,10 +97,10 @@ def _build_examples(incs):
     for name in EXAMPLES:
         src = os.path.join(HERE, "examples", name + ".cpp")
         exe = os.path.join(OUT, name)
-        deps = [src, LIB, os.path.join(INCLUDE, "lpm_bve.hpp"), os.path.join(INCLUDE, "lpm_bve.h")]
+        deps = [src, LIB, *_headers()]
         if os.path.exists(exe) and all(os.path.getmtime(d) <= os.path.getmtime(exe) for d in deps):
             continue
-        cmd = ["g++", "-O2", "-std=c++17", *incs, src, "-o", exe, f"-L{OUT}", "-llpm_bve",
+        cmd = ["g++", "-O2", "-std=c++17", "-pthread", *incs, src, "-o", exe, f"-L{OUT}", "-llpm_bve",
                f"-L{os.path.join(CUDA_HOME, 'lib64')}", "-lcudart",
                f"-Wl,-rpath,{OUT}:{os.path.join(CUDA_HOME, 'lib64')}"]
         res = subprocess.run(cmd, capture_output=True, text=True)

@@ -38,3 +38,38 @@ def test_cpp_driver_matches_python(ctx, tmp_path, prec, arg):
     # and the rigid rotation is reproduced to discretisation accuracy
     pos_err = float(res.stdout.split("position error at t=tfinal ErrNorms: l2 =")[1].split()[0])
     assert pos_err < 1e-2
+
+
+SERVE = os.path.join(os.path.dirname(P._build.LIB), "bve_serve")
+
+
+def test_cpp_server_client_matches_python_server(tmp_path):
+    """examples/bve_serve.cpp (include/lpm_bve_server.hpp) submits six overlapping requests and
+    snapshots their final states; the same requests through the Python binding of the same
+    server give the same bits."""
+    from lpmkokkos_gb300 import bve
+    prefix = str(tmp_path / "req")
+    res = subprocess.run([SERVE, "-n", "6", "-steps", "3", "-o", prefix], capture_output=True, text=True, timeout=600)
+    assert res.returncode == 0, res.stdout + res.stderr
+    assert "completed 6" in res.stdout
+    torch.cuda.set_device(0)
+    with bve.Server(0, flags=P.FP32C) as srv:
+        ids = []
+        for k in range(6):
+            seed, level = k % 2, 3 + (k // 2) % 3
+            ids.append(srv.submit(seed, level, 0.01 * 2.0 ** (4 - level), 3, ic_seed=1000 + k, n_gaussians=3,
+                                  gauss_width=0.1))
+        for rid in ids:
+            assert srv.wait(rid, 600)
+        want = [srv.result(rid) for rid in ids]
+    for k in range(6):
+        path = f"{prefix}{k}.snap"
+        info = bve.snapshot_info(path)
+        assert (info["seed"], info["level"]) == (k % 2, 3 + (k // 2) % 3)
+        s = bve.BVESphere(info["seed"], info["level"], layout="right")
+        bve.snapshot_read(path, s.state())
+        torch.cuda.synchronize()
+        got = dict(vx=s.physVerts, vzeta=s.relVortVerts, vvel=s.velocityVerts, fx=s.physFaces, fzeta=s.relVortFaces,
+                   fvel=s.velocityFaces)
+        for key, v in got.items():
+            assert np.array_equal(v.cpu().numpy(), want[k][key], equal_nan=True), (k, key)
