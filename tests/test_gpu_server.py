@@ -180,3 +180,34 @@ def test_tiny_meshes_match_single_solve_path(ctx):
                     fzeta=s.relVortFaces, fvel=s.velocityFaces)
         for k in KEYS:
             assert _same(g[k], want[k].cpu().numpy()), (sp, k)
+
+
+def test_concurrent_clients():
+    """Four client threads submit and wait at the same time; every result equals the same
+    request run alone (the C ABI is safe to call from any thread)."""
+    import threading
+    torch.cuda.set_device(0)
+    specs = [dict(seed=(t + k) % 2, level=3 + (t + k) % 2, dt=0.005, nsteps=2 + k, ic_seed=100 * t + k)
+             for t in range(4) for k in range(3)]
+    alone = [_alone(P.FP32C, sp) for sp in specs]
+    got = [None] * len(specs)
+    errors = []
+    with bve.Server(0, flags=P.FP32C) as srv:
+        def client(t):
+            try:
+                mine = [(i, srv.submit(**specs[i])) for i in range(3 * t, 3 * t + 3)]
+                for i, rid in mine:
+                    assert srv.wait(rid, WAIT)
+                    got[i] = srv.result(rid)
+            except Exception as e:  # noqa: BLE001 - reported below
+                errors.append(e)
+        threads = [threading.Thread(target=client, args=(t,)) for t in range(4)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        assert not errors, errors
+        assert srv.stats()["completed"] == len(specs)
+    for a, g in zip(alone, got):
+        for k in KEYS:
+            assert _same(g[k], a[k]), k
