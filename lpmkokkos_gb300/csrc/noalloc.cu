@@ -49,7 +49,7 @@ constexpr size_t kScratchBytes = kOffLive + 256;
 static __device__ __align__(256) unsigned char g_noallocScratch[kScratchBytes];
 
 constexpr int kNth = 128;   // CTA size of the pair kernel
-constexpr int kK = 4;       // targets per thread
+constexpr int kK = 8;       // targets per thread (four pairs for the f32x2 arithmetic)
 constexpr int kSt = 256;    // sources staged per step
 constexpr int kSub = 32;    // FP32 sub-block before the compensated add
 constexpr double kPi = 3.1415926535897932384626433832795027975;
@@ -152,13 +152,24 @@ __device__ __forceinline__ void kahanAdd(float& h, float& c, float v) {
 }
 __device__ __forceinline__ float relCoord(float hi, float lo, float chi, float clo) { return (hi - chi) + (lo - clo); }
 
-// One CTA per tile of kNth*kK targets, all packed sources, epilogue fused.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+// One CTA per tile of kNth*kK targets, all packed sources, epilogue fused.  Paired FP32
+// (f32x2) arithmetic over a thread's target pairs, each lane rounded as the scalar
+// instruction: d = x_j - x_i, 2q = D_j + C_i + |d|^2, r = rcp.approx(2q), s' = (w r)(2q r - 2)
+// = -s (the Newton step without a sign flip), v += s' d, the block sums negated into the
+// compensated accumulators.  The source tile stores each value twice, (x,x,y,y), (z,z,w,w),
+// (D,D), so one shared load gives the pair operand.
 template <bool PSI>
 __global__ void __launch_bounds__(kNth) pairKernel(unsigned char* base, Pts tgt, bool colloc, double eps2,
                                                    double* u, int64_t usi, int64_t usc, double* psi) {
+  constexpr int P = kK / 2;
   const Scratch S = carve(base);
-  __shared__ float4 sP[kSt];
-  __shared__ float sD[kSt];
+  __shared__ float4 sXY[kSt];
+  __shared__ float4 sZW[kSt];
+  __shared__ float2 sD[kSt];
   __shared__ int sLo, sHi;
   const int n = (int)tgt.n;
   const int ns = *S.nlive;
@@ -194,81 +205,106 @@ __global__ void __launch_bounds__(kNth) pairKernel(unsigned char* base, Pts tgt,
               clz = __double2float_rn(czd - (double)chz);
   if (threadIdx.x == 0) { sLo = INT_MAX; sHi = -1; }
   __syncthreads();
-  float ax[kK], ay[kK], az[kK], C[kK];
-  double X[kK][3];
+  float ax[kK], ay[kK], az[kK], Ck[kK];
   int self[kK];
 #pragma unroll
   for (int k = 0; k < kK; ++k) {
     const int i = tile0 + threadIdx.x + k * kNth;
     self[k] = -1;
     if (threadIdx.x + k * kNth < tcount) {
-      for (int c = 0; c < 3; ++c) X[k][c] = tgt.x[(int64_t)i * tgt.si + c * tgt.sc];
-      const float hx = __double2float_rn(X[k][0]), hy = __double2float_rn(X[k][1]), hz = __double2float_rn(X[k][2]);
-      ax[k] = relCoord(hx, __double2float_rn(X[k][0] - (double)hx), chx, clx);
-      ay[k] = relCoord(hy, __double2float_rn(X[k][1] - (double)hy), chy, cly);
-      az[k] = relCoord(hz, __double2float_rn(X[k][2] - (double)hz), chz, clz);
-      C[k] = __double2float_rn((1.0 - (X[k][0] * X[k][0] + X[k][1] * X[k][1] + X[k][2] * X[k][2])) + 2.0 * eps2);
+      double X[3];
+      for (int c = 0; c < 3; ++c) X[c] = tgt.x[(int64_t)i * tgt.si + c * tgt.sc];
+      const float hx = __double2float_rn(X[0]), hy = __double2float_rn(X[1]), hz = __double2float_rn(X[2]);
+      ax[k] = relCoord(hx, __double2float_rn(X[0] - (double)hx), chx, clx);
+      ay[k] = relCoord(hy, __double2float_rn(X[1] - (double)hy), chy, cly);
+      az[k] = relCoord(hz, __double2float_rn(X[2] - (double)hz), chz, clz);
+      Ck[k] = __double2float_rn((1.0 - (X[0] * X[0] + X[1] * X[1] + X[2] * X[2])) + 2.0 * eps2);
       if (colloc) {
         self[k] = S.srcIdx[i];
         if (self[k] >= 0) { atomicMin(&sLo, self[k]); atomicMax(&sHi, self[k]); }
       }
     } else {
-      ax[k] = ay[k] = az[k] = 0.f; C[k] = 1.f;
-      X[k][0] = X[k][1] = X[k][2] = 0.0;
+      ax[k] = ay[k] = az[k] = 0.f; Ck[k] = 1.f;
     }
+  }
+  float2 nx[P], ny[P], nz[P], C[P];
+#pragma unroll
+  for (int m = 0; m < P; ++m) {
+    nx[m] = make_float2(-ax[2 * m], -ax[2 * m + 1]);
+    ny[m] = make_float2(-ay[2 * m], -ay[2 * m + 1]);
+    nz[m] = make_float2(-az[2 * m], -az[2 * m + 1]);
+    C[m] = make_float2(Ck[2 * m], Ck[2 * m + 1]);
   }
   __syncthreads();
   const int lo = sLo, hi = sHi;
   float hx[kK], hy[kK], hz[kK], cx[kK], cy[kK], cz[kK], hp[kK], cp[kK], hw[kK], cw[kK];
 #pragma unroll
   for (int k = 0; k < kK; ++k) hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
+  const float2 kMinusTwo = make_float2(-2.f, -2.f);
 
   for (int b0 = 0; b0 < ns; b0 += kSt) {
     __syncthreads();
     for (int j = threadIdx.x; j < kSt; j += kNth) {
       const int s = b0 + j;
+      float x = 0.f, y = 0.f, z = 0.f, w = 0.f, d = 1.f;  // padding: at the centre, zero weight
       if (s < ns) {
         const float4 p0 = S.sp0[s], p1 = S.sp1[s];
-        sP[j] = make_float4(relCoord(p0.x, p1.x, chx, clx), relCoord(p0.y, p1.y, chy, cly),
-                            relCoord(p0.z, p1.z, chz, clz), p0.w);
-        sD[j] = p1.w;
-      } else {
-        sP[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        sD[j] = 1.f;
+        x = relCoord(p0.x, p1.x, chx, clx);
+        y = relCoord(p0.y, p1.y, chy, cly);
+        z = relCoord(p0.z, p1.z, chz, clz);
+        w = p0.w;
+        d = p1.w;
       }
+      sXY[j] = make_float4(x, x, y, y);
+      sZW[j] = make_float4(z, z, w, w);
+      sD[j] = make_float2(d, d);
     }
     __syncthreads();
     const bool checked = lo <= b0 + kSt - 1 && hi >= b0;
 #pragma unroll 1
     for (int j0 = 0; j0 < kSt; j0 += kSub) {
-      float vx[kK], vy[kK], vz[kK], vp[kK], vw[kK];
+      float2 vx[P], vy[P], vz[P], vp[P], vw[P];
 #pragma unroll
-      for (int k = 0; k < kK; ++k) vx[k] = vy[k] = vz[k] = vp[k] = vw[k] = 0.f;
-#pragma unroll 4
+      for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = vp[m] = vw[m] = make_float2(0.f, 0.f);
+#pragma unroll 2
       for (int j = j0; j < j0 + kSub; ++j) {
-        const float4 P = sP[j];
-        const float Dj = sD[j];
+        const float4 xy = sXY[j], zw = sZW[j];
+        const float2 Dj = sD[j];
+        const float2 X = make_float2(xy.x, xy.y), Y = make_float2(xy.z, xy.w), Z = make_float2(zw.x, zw.y);
+        const float2 W = make_float2(zw.z, zw.w);
 #pragma unroll
-        for (int k = 0; k < kK; ++k) {
-          const float dx = P.x - ax[k], dy = P.y - ay[k], dz = P.z - az[k];
-          const float q2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, Dj + C[k])));
-          float r = rcpApprox(q2);
-          const float e = fmaf(-q2, r, 1.0f);
-          r = fmaf(r, e, r);
-          float s = P.w * r;
-          float wl = 0.f, ww = 0.f;
-          if (PSI) { wl = P.w * lg2Approx(q2); ww = P.w; }
-          if (checked && (b0 + j) == self[k]) { s = 0.f; wl = 0.f; ww = 0.f; }
-          vx[k] = fmaf(s, dx, vx[k]);
-          vy[k] = fmaf(s, dy, vy[k]);
-          vz[k] = fmaf(s, dz, vz[k]);
-          if (PSI) { vp[k] += wl; vw[k] += ww; }
+        for (int m = 0; m < P; ++m) {
+          const float2 dx = add2(X, nx[m]), dy = add2(Y, ny[m]), dz = add2(Z, nz[m]);
+          float2 q = add2(Dj, C[m]);
+          q = fma2(dx, dx, q);
+          q = fma2(dy, dy, q);
+          q = fma2(dz, dz, q);
+          const float2 r = make_float2(rcpApprox(q.x), rcpApprox(q.y));
+          float2 sp = mul2(mul2(W, r), fma2(q, r, kMinusTwo));
+          float2 lg, ww;
+          if (PSI) { lg = make_float2(lg2Approx(q.x), lg2Approx(q.y)); ww = W; }
+          if (checked) {  // a self pair has q ~ 0: drop its (inf/NaN) terms after they are formed
+            if (b0 + j == self[2 * m]) { sp.x = 0.f; if (PSI) { lg.x = 0.f; ww.x = 0.f; } }
+            if (b0 + j == self[2 * m + 1]) { sp.y = 0.f; if (PSI) { lg.y = 0.f; ww.y = 0.f; } }
+          }
+          vx[m] = fma2(sp, dx, vx[m]);
+          vy[m] = fma2(sp, dy, vy[m]);
+          vz[m] = fma2(sp, dz, vz[m]);
+          if (PSI) {
+            vp[m] = fma2(W, lg, vp[m]);
+            vw[m] = add2(vw[m], ww);
+          }
         }
       }
 #pragma unroll
-      for (int k = 0; k < kK; ++k) {
-        kahanAdd(hx[k], cx[k], vx[k]); kahanAdd(hy[k], cy[k], vy[k]); kahanAdd(hz[k], cz[k], vz[k]);
-        if (PSI) { kahanAdd(hp[k], cp[k], vp[k]); kahanAdd(hw[k], cw[k], vw[k]); }
+      for (int m = 0; m < P; ++m) {
+        kahanAdd(hx[2 * m], cx[2 * m], -vx[m].x); kahanAdd(hx[2 * m + 1], cx[2 * m + 1], -vx[m].y);
+        kahanAdd(hy[2 * m], cy[2 * m], -vy[m].x); kahanAdd(hy[2 * m + 1], cy[2 * m + 1], -vy[m].y);
+        kahanAdd(hz[2 * m], cz[2 * m], -vz[m].x); kahanAdd(hz[2 * m + 1], cz[2 * m + 1], -vz[m].y);
+        if (PSI) {
+          kahanAdd(hp[2 * m], cp[2 * m], vp[m].x); kahanAdd(hp[2 * m + 1], cp[2 * m + 1], vp[m].y);
+          kahanAdd(hw[2 * m], cw[2 * m], vw[m].x); kahanAdd(hw[2 * m + 1], cw[2 * m + 1], vw[m].y);
+        }
       }
     }
   }
@@ -276,12 +312,14 @@ __global__ void __launch_bounds__(kNth) pairKernel(unsigned char* base, Pts tgt,
   for (int k = 0; k < kK; ++k) {
     const int64_t i = tile0 + threadIdx.x + k * kNth;
     if (threadIdx.x + k * kNth >= tcount) continue;
+    double X[3];
+    for (int c = 0; c < 3; ++c) X[c] = tgt.x[i * tgt.si + c * tgt.sc];
     const double V0 = (double)hx[k] - (double)cx[k], V1 = (double)hy[k] - (double)cy[k],
                  V2 = (double)hz[k] - (double)cz[k];
     if (u) {
-      u[i * usi] = X[k][1] * V2 - X[k][2] * V1;
-      u[i * usi + usc] = X[k][2] * V0 - X[k][0] * V2;
-      u[i * usi + 2 * usc] = X[k][0] * V1 - X[k][1] * V0;
+      u[i * usi] = X[1] * V2 - X[2] * V1;
+      u[i * usi + usc] = X[2] * V0 - X[0] * V2;
+      u[i * usi + 2 * usc] = X[0] * V1 - X[1] * V0;
     }
     if (PSI && psi) psi[i] = 0.34657359027997264 * (((double)hp[k] - (double)cp[k]) - ((double)hw[k] - (double)cw[k]));
   }
