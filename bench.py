@@ -67,6 +67,24 @@ def fma_peak(P, device):
                                  "ffma2_lane_ops_per_s": rates["lpm_probe_fp32_fma2"]}
 
 
+def measured_peaks():
+    """The machine's measured peaks (HBM copy bandwidth, bf16 GEMM) when the file is present."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh)
+    except (OSError, ValueError):
+        return {}
+
+
+def hbm_line(traffic_bytes, launch_ms):
+    """DRAM bandwidth of the pair kernel against the measured HBM copy peak: shows that the
+    kernel is not memory-bound (its traffic follows the O(N) inputs)."""
+    peak = measured_peaks().get("hbm_gbs")
+    achieved = traffic_bytes / (launch_ms * 1e-3) / 1e9
+    return {"achieved_gbs": achieved, "peak_gbs": peak, "frac": (achieved / peak) if peak else None,
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peak else None}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -334,6 +352,7 @@ def run_ours(args, rank, world, local_rank):
             "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
             "traffic_note": "bytes per launch: ncu DRAM read+write of a level-6 launch scaled by targets+sources",
             "algorithmic_bytes": 24 * (nv + nall) + 32 * nl,
+            "hbm": hbm_line(TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl), pair_avg_ms),
         },
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": bytes_step,
                 "d2h_bytes_per_step": bytes_step, "steps": args.e2e_steps},
@@ -602,7 +621,8 @@ def run_large(args, rank, world, local_rank):
         "roofline": {"bound": "fp32_fma_pipe", "kernel": "pairFP32C", "achieved": achieved, "peak": peak,
                      "unit": "Gpair/s", "frac": achieved / peak, "pair_launch_ms_avg": pair_ms / pair_n,
                      "peak_source": "FP32 FMA-pipe probe (FFMA / FFMA2, the larger) / 13 lane-ops per pair",
-                     "probes": probes, "traffic": None},
+                     "probes": probes, "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
+                     "hbm": hbm_line(TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl), pair_ms / pair_n)},
         "fp64_gpu": fp64, "init_s": t_init, "clocks": clocks,
     }
     if rank == 0:
