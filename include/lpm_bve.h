@@ -40,6 +40,7 @@ typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = l
 #define LPM_ERR_ADMISSION        (-5) /* server: request does not fit the HBM budget */
 #define LPM_ERR_STATE            (-6) /* object used in the wrong state (e.g. unknown request id) */
 #define LPM_ERR_TIMEOUT          (-7) /* a bounded wait gave up */
+#define LPM_ERR_INTERNAL         (-8) /* an unexpected host-side failure (message in last_error) */
 
 /* ---- flags ------------------------------------------------------------------ */
 #define LPM_BVE_FP64                0u        /* plain FP64 pair arithmetic (the GPU oracle) */

@@ -18,6 +18,7 @@ LPM_ERR_NOT_SUPPORTED = -4
 LPM_ERR_ADMISSION = -5
 LPM_ERR_STATE = -6
 LPM_ERR_TIMEOUT = -7
+LPM_ERR_INTERNAL = -8
 
 FP64 = 0
 FP32C = 1 << 0

@@ -528,7 +528,8 @@ extern "C" {
 int lpm_bve_ctx_create(lpm_bve_ctx** out, const lpm_bve_opts* opts) {
   if (!out) return LPM_ERR_INVALID_ARGUMENT;
   *out = nullptr;
-  auto* ctx = new lpm_bve_ctx();
+  auto* ctx = new (std::nothrow) lpm_bve_ctx();
+  if (!ctx) return LPM_ERR_OUT_OF_MEMORY;
   try {
     int dev = opts ? opts->device : -1;
     if (dev < 0) LPM_CUDA(cudaGetDevice(&dev));
@@ -549,6 +550,10 @@ int lpm_bve_ctx_create(lpm_bve_ctx** out, const lpm_bve_opts* opts) {
     std::fprintf(stderr, "lpm_bve_ctx_create: %s\n", e.msg.c_str());
     delete ctx;
     return code;
+  } catch (const std::exception& e) {
+    std::fprintf(stderr, "lpm_bve_ctx_create: %s\n", e.what());
+    delete ctx;
+    return fromStd(e).code;
   }
   *out = ctx;
   return LPM_OK;
@@ -578,6 +583,8 @@ int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx) {
     ctx->rkBatch.reset();
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -593,6 +600,8 @@ int lpm_bve_ctx_set_timing(lpm_bve_ctx* ctx, int enable) {
     }
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -643,6 +652,8 @@ int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches
     if (pair_launches) *pair_launches = n;
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -710,6 +721,8 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     B.timer = nullptr;
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -790,6 +803,8 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     }
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -826,6 +841,8 @@ int lpm_bve_rk4_increments(lpm_bve_ctx* ctx, int stage, double* vx_inc, double* 
     }
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -862,6 +879,8 @@ int lpm_errnorms(lpm_bve_ctx* ctx, const double* appx, int64_t a_si, int64_t a_s
     for (int k = 0; k < 3; ++k) out[k] = ctx->normHost[k];
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -940,6 +959,8 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     *out = E.release();
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }
@@ -990,6 +1011,8 @@ int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* O
     }
   } catch (const Error& e) {
     return handle(ctx, e);
+  } catch (const std::exception& e) {
+    return handle(ctx, fromStd(e));
   }
   return LPM_OK;
 }

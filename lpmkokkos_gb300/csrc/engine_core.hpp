@@ -10,7 +10,9 @@
 #include <climits>
 #include <cstdarg>
 #include <cstdio>
+#include <exception>
 #include <memory>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -43,6 +45,12 @@ struct Error {
 // Owns a set of device buffers.  By default they come from cudaMalloc/cudaFree; after
 // streamOrdered(a, f, pool) they come from `pool` in stream order on `a` and are freed in
 // stream order on `f` (the stream of their last use), so neither call waits for work in flight.
+// A standard-library exception as a status of the C ABI: no exception may cross extern "C".
+inline Error fromStd(const std::exception& e) {
+  if (dynamic_cast<const std::bad_alloc*>(&e)) return Error{LPM_ERR_OUT_OF_MEMORY, "host memory exhausted"};
+  return Error{LPM_ERR_INTERNAL, e.what()};
+}
+
 class DeviceArena {
  public:
   ~DeviceArena() { release(); }

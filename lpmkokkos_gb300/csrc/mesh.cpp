@@ -15,6 +15,8 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <exception>
+#include <new>
 #include <random>
 #include <vector>
 
@@ -299,23 +301,35 @@ int lpm_mesh_counts(int seed, int level, int64_t* nverts, int64_t* nfaces, int64
 
 int lpm_mesh_build(int seed, int level, double* vx, double* fx, double* farea, uint8_t* fmask) {
   if ((seed != LPM_SEED_ICOS_TRI && seed != LPM_SEED_CUBED) || level < 0 || level > 10) return LPM_ERR_INVALID_ARGUMENT;
-  lpm::TreeMesh m(lpm::kSeeds[seed]);
-  m.refine(level);
-  const auto& v = m.verts();
-  const auto& c = m.centres();
-  for (size_t i = 0; vx && i < v.size(); ++i) { vx[3*i] = v[i].x; vx[3*i+1] = v[i].y; vx[3*i+2] = v[i].z; }
-  for (size_t i = 0; fx && i < c.size(); ++i) { fx[3*i] = c[i].x; fx[3*i+1] = c[i].y; fx[3*i+2] = c[i].z; }
-  if (farea) std::memcpy(farea, m.areas().data(), sizeof(double) * m.areas().size());
-  if (fmask) std::memcpy(fmask, m.masks().data(), m.masks().size());
+  try {
+    lpm::TreeMesh m(lpm::kSeeds[seed]);
+    m.refine(level);
+    const auto& v = m.verts();
+    const auto& c = m.centres();
+    for (size_t i = 0; vx && i < v.size(); ++i) { vx[3*i] = v[i].x; vx[3*i+1] = v[i].y; vx[3*i+2] = v[i].z; }
+    for (size_t i = 0; fx && i < c.size(); ++i) { fx[3*i] = c[i].x; fx[3*i+1] = c[i].y; fx[3*i+2] = c[i].z; }
+    if (farea) std::memcpy(farea, m.areas().data(), sizeof(double) * m.areas().size());
+    if (fmask) std::memcpy(fmask, m.masks().data(), m.masks().size());
+  } catch (const std::bad_alloc&) {
+    return LPM_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception&) {
+    return LPM_ERR_INTERNAL;
+  }
   return LPM_OK;
 }
 
 int lpm_mesh_face_verts(int seed, int level, int32_t* face_verts, int* verts_per_face) {
   if ((seed != LPM_SEED_ICOS_TRI && seed != LPM_SEED_CUBED) || level < 0 || level > 10) return LPM_ERR_INVALID_ARGUMENT;
-  lpm::TreeMesh m(lpm::kSeeds[seed]);
-  m.refine(level);
-  if (verts_per_face) *verts_per_face = m.vertsPerFace();
-  if (face_verts) std::memcpy(face_verts, m.faceVerts().data(), sizeof(int32_t) * m.faceVerts().size());
+  try {
+    lpm::TreeMesh m(lpm::kSeeds[seed]);
+    m.refine(level);
+    if (verts_per_face) *verts_per_face = m.vertsPerFace();
+    if (face_verts) std::memcpy(face_verts, m.faceVerts().data(), sizeof(int32_t) * m.faceVerts().size());
+  } catch (const std::bad_alloc&) {
+    return LPM_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception&) {
+    return LPM_ERR_INTERNAL;
+  }
   return LPM_OK;
 }
 

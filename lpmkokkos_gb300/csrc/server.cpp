@@ -372,10 +372,10 @@ void prepLoop(lpm_bve_server* S) {
       std::lock_guard<std::mutex> lk(S->mu);
       r->mesh.reset();
       failLocked(S, r, e.msg);
-    } catch (const std::bad_alloc&) {
+    } catch (const std::exception& e) {
       std::lock_guard<std::mutex> lk(S->mu);
       r->mesh.reset();
-      failLocked(S, r, "host memory exhausted while preparing the request");
+      failLocked(S, r, "preparing the request: " + fromStd(e).msg);
     }
   }
 }
@@ -605,6 +605,7 @@ void gpuLoop(lpm_bve_server* S) {
     for (auto& kv : classes) v.insert(v.end(), kv.second.solves.begin(), kv.second.solves.end());
     return v;
   };
+  std::string fatal;
   try {
     LPM_CUDA(cudaEventCreateWithFlags(&upEv, cudaEventDisableTiming));
     for (;;) {
@@ -620,17 +621,22 @@ void gpuLoop(lpm_bve_server* S) {
       }
       // 1. upload the newcomers (a failure that leaves the context usable fails the request only)
       std::vector<Req*> ok;
+      auto failJoiner = [&](Req* r, const std::string& msg) {
+        cudaStreamSynchronize(S->up);  // copies into the request's memory may be queued
+        r->plan.reset();
+        r->mem.release();
+        std::lock_guard<std::mutex> lk(S->mu);
+        failLocked(S, r, msg);
+      };
       for (Req* r : joiners) {
         try {
           setupSolve(S, r);
           ok.push_back(r);
         } catch (const Error& e) {
           if (e.code == LPM_ERR_CUDA) throw;
-          cudaStreamSynchronize(S->up);  // copies into the request's memory may be queued
-          r->plan.reset();
-          r->mem.release();
-          std::lock_guard<std::mutex> lk(S->mu);
-          failLocked(S, r, e.msg);
+          failJoiner(r, e.msg);
+        } catch (const std::exception& e) {
+          failJoiner(r, fromStd(e).msg);
         }
         r->mesh.reset();
       }
@@ -790,12 +796,17 @@ void gpuLoop(lpm_bve_server* S) {
       }
     }
   } catch (const Error& e) {
+    fatal = e.msg;
+  } catch (const std::exception& e) {
+    fatal = fromStd(e).msg;
+  }
+  if (!fatal.empty()) {  // every request not yet done fails; submit refuses new ones
     std::lock_guard<std::mutex> lk(S->mu);
-    S->fatal = e.msg;
-    for (Req* r : allActive()) failLocked(S, r, "server stopped: " + e.msg);
-    for (Req* r : S->prepared) failLocked(S, r, "server stopped: " + e.msg);
-    for (Req* r : S->queued) failLocked(S, r, "server stopped: " + e.msg);
-    for (Req* r : S->finishing) failLocked(S, r, "server stopped: " + e.msg);
+    S->fatal = fatal;
+    for (Req* r : allActive()) failLocked(S, r, "server stopped: " + fatal);
+    for (Req* r : S->prepared) failLocked(S, r, "server stopped: " + fatal);
+    for (Req* r : S->queued) failLocked(S, r, "server stopped: " + fatal);
+    for (Req* r : S->finishing) failLocked(S, r, "server stopped: " + fatal);
     S->prepared.clear();
     S->queued.clear();
     S->finishing.clear();
@@ -838,8 +849,17 @@ extern "C" {
 int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out) {
   if (!out) return LPM_ERR_INVALID_ARGUMENT;
   *out = nullptr;
-  auto S = std::make_unique<lpm_bve_server>();
+  std::unique_ptr<lpm_bve_server> S;
+  auto undo = [&](const Error& e) {
+    std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.msg.c_str());
+    if (S && S->pool) cudaMemPoolDestroy(S->pool);
+    if (S)
+      for (cudaStream_t s : {S->up, S->cap})
+        if (s) cudaStreamDestroy(s);
+    return e.code;
+  };
   try {
+    S = std::make_unique<lpm_bve_server>();
     int dev = opts ? opts->device : -1;
     if (dev < 0) LPM_CUDA(cudaGetDevice(&dev));
     LPM_CUDA(cudaSetDevice(dev));
@@ -885,16 +905,19 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     uint64_t keep = UINT64_MAX;  // keep freed blocks for the next requests
     LPM_CUDA(cudaMemPoolSetAttribute(S->pool, cudaMemPoolAttrReleaseThreshold, &keep));
   } catch (const Error& e) {
-    std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.msg.c_str());
-    if (S->pool) cudaMemPoolDestroy(S->pool);
-    for (cudaStream_t s : {S->up, S->cap})
-      if (s) cudaStreamDestroy(s);
-    for (auto& ln : S->lanes) cudaStreamDestroy(ln.second);
-    return e.code;
+    return undo(e);
+  } catch (const std::exception& e) {
+    return undo(fromStd(e));
   }
   lpm_bve_server* raw = S.release();
-  raw->prepT = std::thread(prepLoop, raw);
-  raw->gpuT = std::thread(gpuLoop, raw);
+  try {
+    raw->prepT = std::thread(prepLoop, raw);
+    raw->gpuT = std::thread(gpuLoop, raw);
+  } catch (const std::exception& e) {  // no thread: stop and join the one that started
+    std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.what());
+    lpm_bve_server_destroy(raw);
+    return LPM_ERR_INTERNAL;
+  }
   *out = raw;
   return LPM_OK;
 }
@@ -906,31 +929,44 @@ int lpm_bve_server_submit(lpm_bve_server* S, const lpm_bve_request* req, int64_t
   if (!bad.empty()) return setErr(S, LPM_ERR_INVALID_ARGUMENT, "submit: " + bad);
   int64_t nv = 0, nf = 0, nl = 0;
   lpm_mesh_counts(q.seed, q.level, &nv, &nf, &nl);
-  auto r = std::make_unique<Req>();
-  r->r = q;
-  r->nv = nv;
-  r->nf = nf;
-  r->nl = nl;
-  r->est = estimateBytes(S->prec, S->shape, S->skip, nv, nf, nl);
-  r->tSubmit = Clock::now();
-  std::lock_guard<std::mutex> lk(S->mu);
-  if (!S->fatal.empty()) {
-    S->err = "server stopped after a device error: " + S->fatal;
-    return LPM_ERR_CUDA;
+  try {
+    auto r = std::make_unique<Req>();
+    r->r = q;
+    r->nv = nv;
+    r->nf = nf;
+    r->nl = nl;
+    r->est = estimateBytes(S->prec, S->shape, S->skip, nv, nf, nl);
+    r->tSubmit = Clock::now();
+    std::lock_guard<std::mutex> lk(S->mu);
+    if (!S->fatal.empty()) {
+      S->err = "server stopped after a device error: " + S->fatal;
+      return LPM_ERR_CUDA;
+    }
+    if (r->est > S->budget) {
+      char buf[192];
+      std::snprintf(buf, sizeof(buf), "submit: request needs about %zu bytes, the HBM budget is %zu", r->est,
+                    S->budget);
+      S->err = buf;
+      return LPM_ERR_ADMISSION;
+    }
+    Req* raw = r.get();
+    raw->id = S->nextId;
+    S->reqs.emplace(raw->id, std::move(r));  // a throw here changes nothing
+    try {
+      S->queued.push_back(raw);
+    } catch (...) {
+      S->reqs.erase(raw->id);
+      throw;
+    }
+    S->nextId += 1;
+    if (id) *id = raw->id;
+    S->st.submitted += 1;
+    S->cvPrep.notify_one();
+    return LPM_OK;
+  } catch (const std::exception& e) {
+    const Error x = fromStd(e);
+    return setErr(S, x.code, "submit: " + x.msg);
   }
-  if (r->est > S->budget) {
-    char buf[192];
-    std::snprintf(buf, sizeof(buf), "submit: request needs about %zu bytes, the HBM budget is %zu", r->est, S->budget);
-    S->err = buf;
-    return LPM_ERR_ADMISSION;
-  }
-  r->id = S->nextId++;
-  if (id) *id = r->id;
-  S->queued.push_back(r.get());
-  S->reqs[r->id] = std::move(r);
-  S->st.submitted += 1;
-  S->cvPrep.notify_one();
-  return LPM_OK;
 }
 
 int lpm_bve_server_estimate(const lpm_bve_server_opts* opts, const lpm_bve_request* req, size_t* bytes) {
@@ -1041,6 +1077,10 @@ int lpm_bve_server_snapshot(lpm_bve_server* S, int64_t id, const char* path) {
   } catch (const Error& e) {
     S->err = e.msg;
     return e.code;
+  } catch (const std::exception& e) {
+    const Error x = fromStd(e);
+    S->err = x.msg;
+    return x.code;
   }
   return LPM_OK;
 }
@@ -1078,9 +1118,12 @@ int lpm_bve_server_timing(lpm_bve_server* S, int64_t id, double* total_s, double
 int lpm_bve_server_latency(lpm_bve_server* S, const double* q, int nq, double* out) {
   if (!S || (nq > 0 && (!q || !out))) return LPM_ERR_INVALID_ARGUMENT;
   std::vector<double> v;
-  {
+  try {
     std::lock_guard<std::mutex> lk(S->mu);
     v = S->latencies;
+  } catch (const std::exception& e) {
+    const Error x = fromStd(e);
+    return setErr(S, x.code, "latency: " + x.msg);
   }
   if (v.empty()) return LPM_ERR_STATE;
   std::sort(v.begin(), v.end());

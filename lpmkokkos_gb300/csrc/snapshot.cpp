@@ -210,6 +210,8 @@ int lpm_bve_snapshot_write(const char* path, const lpm_bve_state* st, int seed, 
                       fz.data(), fv.data(), fa.data(), fm.data());
   } catch (const Error& e) {
     return fail_code(e, nullptr);
+  } catch (const std::exception& e) {
+    return fail_code(fromStd(e), nullptr);
   }
   return LPM_OK;
 }
@@ -231,6 +233,8 @@ int lpm_bve_snapshot_info(const char* path, int* seed, int* level, int64_t* nver
     if (omega) *omega = h.omega;
   } catch (const Error& e) {
     return fail_code(e, nullptr);
+  } catch (const std::exception& e) {
+    return fail_code(fromStd(e), nullptr);
   }
   return LPM_OK;
 }
@@ -272,6 +276,8 @@ int lpm_bve_snapshot_read(const char* path, const lpm_bve_state* st, double* t, 
     if (t) *t = h.t;
   } catch (const Error& e) {
     return fail_code(e, nullptr);
+  } catch (const std::exception& e) {
+    return fail_code(fromStd(e), nullptr);
   }
   return LPM_OK;
 }
@@ -343,6 +349,8 @@ int lpm_bve_vtk_write(const char* path, const lpm_bve_state* st, int seed, int l
     put("\n");
   } catch (const Error& e) {
     return fail_code(e, nullptr);
+  } catch (const std::exception& e) {
+    return fail_code(fromStd(e), nullptr);
   }
   return LPM_OK;
 }

@@ -79,6 +79,17 @@ def test_library_exports_every_declared_symbol(native):
     assert not missing, missing
 
 
+def test_status_codes_match_header():
+    """Every LPM_OK / LPM_ERR_* status of include/lpm_bve.h has the same value in the bindings."""
+    from lpmkokkos_gb300 import _lib as L
+    with open(os.path.join(ROOT, "include", "lpm_bve.h")) as f:
+        codes = {m.group(1): int(m.group(2))
+                 for m in re.finditer(r"#define\s+(LPM_(?:OK|ERR_\w+))\s+\(?(-?\d+)\)?", f.read())}
+    assert "LPM_ERR_INTERNAL" in codes and len(codes) >= 9
+    assert {k: getattr(L, k, None) for k in codes} == codes
+    assert len(set(codes.values())) == len(codes)
+
+
 def test_no_cpu_fallback_without_library(tmp_path, monkeypatch):
     """The product refuses to run if the native library is missing."""
     from lpmkokkos_gb300 import _build, _lib
