@@ -183,6 +183,13 @@ int lpm_errnorms(lpm_bve_ctx* ctx, const double* appx, int64_t a_si, int64_t a_s
                  int64_t e_si, int64_t e_sc, const double* wt, const uint8_t* skip, int64_t n, int ncomp,
                  unsigned flags, double out[3], lpm_stream_t stream);
 
+/* Velocity tangency diagnostic of SphereVelocityTangentTestFunctor (src/LpmSphereTestKernels.hpp:11-25,
+ * run by tests/LpmBVETest.cpp:61-64,160-163): udotx[i] = x_i . u_i for n points of DEVICE arrays
+ * (strides as above), FP64, in the order (x0 u0 + x1 u1) + x2 u2 without fused multiply-add.
+ * Zero up to rounding for velocities tangent to the sphere.  Stream-ordered; no context. */
+int lpm_sphere_tangency(const double* x, int64_t x_si, int64_t x_sc, const double* u, int64_t u_si, int64_t u_sc,
+                        int64_t n, double* udotx, lpm_stream_t stream);
+
 /* ---- host-side mesh and initial conditions ------------------------------------------ */
 #define LPM_SEED_ICOS_TRI 0 /* IcosTriSphereSeed  (src/LpmMeshSeed.hpp:134-152) */
 #define LPM_SEED_CUBED    1 /* CubedSphereSeed    (src/LpmMeshSeed.hpp:113-128) */

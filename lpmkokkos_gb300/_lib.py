@@ -131,6 +131,7 @@ def _declare(L):
     L.lpm_ic_gaussian_params.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.c_double, ctypes.c_double, vp, vp]
     L.lpm_ic_rh54_gaussians_device.argtypes = [vp, c_i64, c_i64, c_i64, vp, vp, ctypes.c_int, ctypes.c_double, vp,
                                                vp]
+    L.lpm_sphere_tangency.argtypes = [vp, c_i64, c_i64, vp, c_i64, c_i64, c_i64, vp, vp]
     L.lpm_errnorms.argtypes = [vp, vp, c_i64, c_i64, vp, c_i64, c_i64, vp, vp, c_i64, ctypes.c_int, ctypes.c_uint,
                                c_dp, vp]
     L.lpm_bve_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]

@@ -118,6 +118,17 @@ def ic_rh54_gaussians_device(x: torch.Tensor, seed: int, ng: int, width: float =
     return z
 
 
+def sphere_tangency(x: torch.Tensor, u: torch.Tensor, out: Optional[torch.Tensor] = None, stream=None) -> torch.Tensor:
+    """u . x per point of float64 (n, 3) device arrays (SphereVelocityTangentTestFunctor,
+    src/LpmSphereTestKernels.hpp:11-25); zero up to rounding for a tangent velocity field."""
+    assert x.dtype == u.dtype == torch.float64 and x.is_cuda and u.is_cuda and x.shape == u.shape and x.shape[1] == 3
+    if out is None:
+        out = torch.empty(x.shape[0], dtype=torch.float64, device=x.device)
+    L.check(L.lib().lpm_sphere_tangency(_vp(x), x.stride(0), x.stride(1), _vp(u), u.stride(0), u.stride(1),
+                                        x.shape[0], _vp(out), _stream(stream)))
+    return out
+
+
 def mesh_face_verts(seed: int, level: int) -> np.ndarray:
     """Face-to-vertex connectivity (nfaces x 3 or 4) of build_mesh(seed, level)."""
     _, nf, _ = mesh_counts(seed, level)

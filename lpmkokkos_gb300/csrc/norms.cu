@@ -12,6 +12,7 @@
 // HBM-bound: 7 doubles (+ mask byte) read per vector entry.
 
 #include "engine.hpp"
+#include "lpm_bve.h"
 
 #include <cfloat>
 #include <cstdint>
@@ -120,6 +121,20 @@ __global__ void __launch_bounds__(kNormThreads) normsPass2(const double* partial
   }
 }
 
+// u.x per point in FP64 with the reference's operation order (a0 b0 + a1 b1) + a2 b2 and no
+// fused multiply-add, so each entry equals the host's bit for bit.
+__global__ void __launch_bounds__(256) tangencyKernel(const double* __restrict__ x, int64_t xsi, int64_t xsc,
+                                                      const double* __restrict__ u, int64_t usi, int64_t usc,
+                                                      int64_t n, double* __restrict__ udotx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* xi = x + i * xsi;
+  const double* ui = u + i * usi;
+  const double d = __dadd_rn(__dadd_rn(__dmul_rn(xi[0], ui[0]), __dmul_rn(xi[xsc], ui[usc])),
+                             __dmul_rn(xi[2 * xsc], ui[2 * usc]));
+  udotx[i] = d;
+}
+
 }  // namespace
 
 int normBlocks(int sms) { return 2 * sms; }
@@ -131,3 +146,15 @@ cudaError_t launchNorms(const NormArgs& a, double* partial, int nblocks, double*
 }
 
 }  // namespace lpm
+
+extern "C" int lpm_sphere_tangency(const double* x, int64_t x_si, int64_t x_sc, const double* u, int64_t u_si,
+                                   int64_t u_sc, int64_t n, double* udotx, lpm_stream_t stream) {
+  if (n < 0) return LPM_ERR_INVALID_ARGUMENT;
+  if (n == 0) return LPM_OK;
+  if (!x || !u || !udotx || x_si < 0 || x_sc < 0 || u_si < 0 || u_sc < 0) return LPM_ERR_INVALID_ARGUMENT;
+  constexpr int kBlock = 256;
+  const int64_t blocks = (n + kBlock - 1) / kBlock;
+  if (blocks > INT32_MAX) return LPM_ERR_INVALID_ARGUMENT;
+  lpm::tangencyKernel<<<(unsigned)blocks, kBlock, 0, (cudaStream_t)stream>>>(x, x_si, x_sc, u, u_si, u_sc, n, udotx);
+  return cudaGetLastError() == cudaSuccess ? LPM_OK : LPM_ERR_CUDA;
+}

@@ -645,6 +645,12 @@ void oracle_errnorms_scalar(const double* appx, const double* exact, const doubl
   out[0] = l1n/l1d; out[1] = std::sqrt(l2n/l2d); out[2] = lin/lid;
 }
 
+// Velocity tangency diagnostic: SphereVelocityTangentTestFunctor (src/LpmSphereTestKernels.hpp:11-25)
+// with SphereGeometry::dot (src/LpmGeometry.hpp:280-282): udotx[i] = x0 u0 + x1 u1 + x2 u2.
+void oracle_tangency(const double* x, const double* u, long n, double* udotx) {
+  for (long i = 0; i < n; ++i) udotx[i] = x[3*i]*u[3*i] + x[3*i+1]*u[3*i+1] + x[3*i+2]*u[3*i+2];
+}
+
 // ---------------------------------------------------------------------------
 // Spherical Poisson known-answer solve: SpherePoisson::init/solve (src/LpmSpherePoisson.hpp:419-475)
 // with its own kernel spelling (:32-55): psi = -log(1 - x.y)*f*A/(4pi).  RH54 forcing,

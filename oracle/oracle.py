@@ -79,6 +79,7 @@ def _setup(L):
     L.oracle_gaussian_params.argtypes = [ctypes.c_ulonglong, ctypes.c_int, ctypes.c_double, ctypes.c_double, D, D]
     L.oracle_errnorms_vec.argtypes = [D, D, D, ctypes.c_long, D]
     L.oracle_errnorms_scalar.argtypes = [D, D, D, ctypes.c_long, D]
+    L.oracle_tangency.argtypes = [D, D, ctypes.c_long, D]
     L.oracle_poisson.argtypes = [ctypes.c_int, ctypes.c_int, D]
     L.oracle_poisson.restype = ctypes.c_int
     L.oracle_tri_area.argtypes = [D, D, D]
@@ -212,6 +213,15 @@ def errnorms_scalar(appx, exact, wt):
     out = np.zeros(3)
     lib().oracle_errnorms_scalar(_dp(appx), _dp(exact), _dp(wt), appx.shape[0], _dp(out))
     return dict(l1=out[0], l2=out[1], linf=out[2])
+
+
+def tangency(x, u):
+    """u . x per point of row-major (n, 3) arrays."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.zeros(x.shape[0])
+    lib().oracle_tangency(_dp(x), _dp(u), x.shape[0], _dp(out))
+    return out
 
 
 def poisson(kind, level):

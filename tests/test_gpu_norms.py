@@ -72,3 +72,48 @@ def test_invalid_arguments(ctx):
     assert rc == L.LPM_ERR_INVALID_ARGUMENT
     rc = L.lib().lpm_errnorms(ctx.handle, x.data_ptr(), 3, 1, x.data_ptr(), 3, 1, None, None, 0, 3, 0, out, None)
     assert rc == L.LPM_ERR_INVALID_ARGUMENT
+
+
+def test_tangency_matches_oracle_bitwise(ctx, oracle):
+    """lpm_sphere_tangency against the oracle's SphereVelocityTangentTestFunctor
+    (src/LpmSphereTestKernels.hpp:11-25) on the velocity the device computed, as
+    tests/LpmBVETest.cpp:160-163 runs it after a step: bit for bit (same order, no contraction),
+    row-major and LayoutLeft, and |u . x| at rounding level for the tangent Biot-Savart field."""
+    import math
+    from lpmkokkos_gb300 import FP64, bve
+    s = bve.BVESphere(1, 4)
+    s.init_vorticity(bve.rh54_gaussians(11, 3), ctx, flags=FP64)
+    ctx.rk4_step(s.state(), 0.01, 2 * math.pi, 1, flags=FP64)
+    torch.cuda.synchronize()
+    for x, u in ((s.physVerts, s.velocityVerts), (s.physFaces, s.velocityFaces)):
+        ref = oracle.tangency(x.cpu().numpy(), u.cpu().numpy())
+        got = bve.sphere_tangency(x, u)
+        torch.cuda.synchronize()
+        assert np.array_equal(got.cpu().numpy(), ref)
+        xl = x.t().contiguous().t()
+        ul = u.t().contiguous().t()
+        assert np.array_equal(bve.sphere_tangency(xl, ul).cpu().numpy(), ref)
+        assert np.abs(ref).max() <= 1e-14 * np.abs(u.cpu().numpy()).max()
+
+
+def test_tangency_solid_body(ctx, oracle):
+    """The solid-body field of tests/LpmBVETest.cpp:55-64: u = Omega (-y, x, 0) is tangent;
+    u . x equals the oracle's bit for bit and is at most a few ulps of |u| (4.4e-16 here)."""
+    from lpmkokkos_gb300 import bve
+    m = bve.build_mesh(0, 3)
+    x = m["vx"]
+    u = 2 * np.pi * np.stack([-x[:, 1], x[:, 0], np.zeros(len(x))], axis=1)
+    got = bve.sphere_tangency(torch.from_numpy(x).cuda(), torch.from_numpy(u).cuda())
+    ref = oracle.tangency(x, u)
+    assert np.array_equal(got.cpu().numpy(), ref)
+    assert np.abs(ref).max() <= 1e-15
+
+
+def test_tangency_invalid_arguments():
+    from lpmkokkos_gb300 import _lib as L
+    x = torch.zeros(4, 3, dtype=torch.float64, device="cuda")
+    assert L.lib().lpm_sphere_tangency(x.data_ptr(), 3, 1, x.data_ptr(), 3, 1, -1, x.data_ptr(), None) \
+        == L.LPM_ERR_INVALID_ARGUMENT
+    assert L.lib().lpm_sphere_tangency(None, 3, 1, x.data_ptr(), 3, 1, 4, x.data_ptr(), None) \
+        == L.LPM_ERR_INVALID_ARGUMENT
+    assert L.lib().lpm_sphere_tangency(x.data_ptr(), 3, 1, x.data_ptr(), 3, 1, 0, None, None) == L.LPM_OK
