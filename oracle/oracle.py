@@ -80,6 +80,15 @@ def _setup(L):
     L.oracle_errnorms_vec.argtypes = [D, D, D, ctypes.c_long, D]
     L.oracle_errnorms_scalar.argtypes = [D, D, D, ctypes.c_long, D]
     L.oracle_tangency.argtypes = [D, D, ctypes.c_long, D]
+    IP = ctypes.POINTER(ctypes.c_int)
+    L.oracle_octree_counts.argtypes = [D, ctypes.c_long, ctypes.c_int, IP]
+    L.oracle_octree_counts.restype = ctypes.c_long
+    L.oracle_octree_build.argtypes = [D, ctypes.c_long, ctypes.c_int, D, IP, IP, ctypes.c_void_p, IP, IP, IP, IP, D,
+                                      IP, IP]
+    L.oracle_octree_tables.argtypes = [IP, IP]
+    L.oracle_octree_key.argtypes = [ctypes.c_int, D, D, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_int, ctypes.c_int]
+    L.oracle_octree_key.restype = ctypes.c_uint64
+    L.oracle_octree_box.argtypes = [ctypes.c_uint64, D, ctypes.c_int, ctypes.c_int, D]
     L.oracle_poisson.argtypes = [ctypes.c_int, ctypes.c_int, D]
     L.oracle_poisson.restype = ctypes.c_int
     L.oracle_tri_area.argtypes = [D, D, D]
@@ -221,6 +230,58 @@ def tangency(x, u):
     u = np.ascontiguousarray(u, dtype=np.float64)
     out = np.zeros(x.shape[0])
     lib().oracle_tangency(_dp(x), _dp(u), x.shape[0], _dp(out))
+    return out
+
+
+def _ip(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+
+
+def octree(x, depth):
+    """The Morton octree of src/LpmOctree.cpp over row-major (n, 3) points: box (6,),
+    base_address / nnodes_per_level (depth + 1), keys (uint32), pt_inds (nn, 2), parents,
+    kids (nn, 8), neighbors (nn, 27) -- level-local indices or -1 -- sorted_pts (n, 3), orig_ids,
+    pt_in_leaf."""
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    n = x.shape[0]
+    npl = np.zeros(depth + 1, dtype=np.int32)
+    nn = lib().oracle_octree_counts(_dp(x), n, depth, _ip(npl))
+    if nn < 0:
+        raise ValueError("invalid octree depth or empty point set")
+    out = dict(box=np.zeros(6), base_address=np.zeros(depth + 1, dtype=np.int32), nnodes_per_level=npl,
+               keys=np.zeros(nn, dtype=np.uint32), pt_inds=np.zeros((nn, 2), dtype=np.int32),
+               parents=np.zeros(nn, dtype=np.int32), kids=np.zeros((nn, 8), dtype=np.int32),
+               neighbors=np.zeros((nn, 27), dtype=np.int32), sorted_pts=np.zeros((n, 3)),
+               orig_ids=np.zeros(n, dtype=np.int32), pt_in_leaf=np.zeros(n, dtype=np.int32))
+    rc = lib().oracle_octree_build(_dp(x), n, depth, _dp(out["box"]), _ip(out["base_address"]), _ip(npl),
+                                   out["keys"].ctypes.data, _ip(out["pt_inds"]), _ip(out["parents"]),
+                                   _ip(out["kids"]), _ip(out["neighbors"]), _dp(out["sorted_pts"]),
+                                   _ip(out["orig_ids"]), _ip(out["pt_in_leaf"]))
+    assert rc == 0
+    return out
+
+
+def octree_tables():
+    """(ParentLUT, ChildLUT) as (8, 27) int arrays, generated from their geometric definition."""
+    tp = np.zeros((8, 27), dtype=np.int32)
+    tc = np.zeros((8, 27), dtype=np.int32)
+    lib().oracle_octree_tables(_ip(tp), _ip(tc))
+    return tp, tc
+
+
+def octree_key(op, x=None, box=None, k=0, lk=0, lev=1, maxd=1):
+    """Key algebra: op 0 compute_key_for_point(x, lev, box), 1 parent_key(k, lev, maxd),
+    2 local_key(k, lev, maxd), 3 node_key(k, lk, lev, maxd)."""
+    xx = np.ascontiguousarray(x if x is not None else np.zeros(3), dtype=np.float64)
+    bb = np.ascontiguousarray(box if box is not None else np.zeros(6), dtype=np.float64)
+    return int(lib().oracle_octree_key(op, _dp(xx), _dp(bb), k, lk, lev, maxd))
+
+
+def octree_box(k, rbox, lev, maxd):
+    """box_from_key: (xmin, xmax, ymin, ymax, zmin, zmax)."""
+    rb = np.ascontiguousarray(rbox, dtype=np.float64)
+    out = np.zeros(6)
+    lib().oracle_octree_box(k, _dp(rb), lev, maxd, _dp(out))
     return out
 
 
