@@ -61,6 +61,10 @@ typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = l
 #define LPM_BVE_RCP_APPROX          (1u << 10) /* FP32C: use the hardware reciprocal without its Newton step
                                                   (11 instead of 13 FMA-pipe ops per pair, about one more
                                                   FP32 rounding per pair) */
+#define LPM_BVE_TREECODE            (1u << 11) /* FP32C velocity()/rk4: tree code instead of the direct sum --
+                                                 octree clusters far from a target tile act through
+                                                 interpolated proxies (lpm_bve_ctx_set_treecode); an
+                                                 approximation with its own tolerance, not in the reference */
 
 /* ---- context ---------------------------------------------------------------- */
 typedef struct lpm_bve_ctx lpm_bve_ctx;
@@ -189,6 +193,19 @@ int lpm_errnorms(lpm_bve_ctx* ctx, const double* appx, int64_t a_si, int64_t a_s
  * Zero up to rounding for velocities tangent to the sphere.  Stream-ordered; no context. */
 int lpm_sphere_tangency(const double* x, int64_t x_si, int64_t x_sc, const double* u, int64_t u_si, int64_t u_sc,
                         int64_t n, double* udotx, lpm_stream_t stream);
+
+/* Tree-code parameters of the context (LPM_BVE_TREECODE): interpolation degree n per chart
+ * axis (2..10; (n+1)^2 proxies per cluster), opening parameter theta (0 < theta < 1: a cluster
+ * is far from a target tile when r_tile + r_cluster < theta * distance), and the mean sources per
+ * octree leaf that set the octree depth.  Defaults 8, 0.6, 512. */
+int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points);
+/* Statistics of the context's last tree-code evaluation: octree depth and node count, far-field
+ * clusters taken over all tiles, target x source pairs evaluated (direct + proxy), and -- with
+ * timing enabled (lpm_bve_ctx_set_timing) -- phase_ms[3] = milliseconds of the octree build, the
+ * upward pass and the interaction lists (the pair kernel is reported by lpm_bve_ctx_timing).
+ * Any pointer may be NULL. */
+int lpm_bve_ctx_tree_stats(lpm_bve_ctx* ctx, int* depth, int64_t* nodes, int64_t* far_clusters, double* pairs,
+                           double* direct_pairs, double* far_pairs, double* phase_ms);
 
 /* ---- host-side mesh and initial conditions ------------------------------------------ */
 #define LPM_SEED_ICOS_TRI 0 /* IcosTriSphereSeed  (src/LpmMeshSeed.hpp:134-152) */

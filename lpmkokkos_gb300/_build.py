@@ -21,7 +21,7 @@ LIB = os.path.join(OUT, "liblpm_bve.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 
-CU_SOURCES = ["pair_kernels.cu", "stage_kernels.cu", "probe.cu", "noalloc.cu", "norms.cu", "ic.cu"]
+CU_SOURCES = ["pair_kernels.cu", "stage_kernels.cu", "probe.cu", "noalloc.cu", "norms.cu", "ic.cu", "octree.cu", "tree.cu"]
 CXX_SOURCES = ["engine.cpp", "mesh.cpp", "server.cpp", "snapshot.cpp"]
 
 

@@ -32,6 +32,7 @@ NO_GRAPH = 1 << 7
 NO_SORT = 1 << 8
 MESH_TARGETS = 1 << 9
 RCP_APPROX = 1 << 10
+TREECODE = 1 << 11
 
 SEED_ICOS_TRI = 0
 SEED_CUBED = 1
@@ -132,6 +133,15 @@ def _declare(L):
     L.lpm_ic_rh54_gaussians_device.argtypes = [vp, c_i64, c_i64, c_i64, vp, vp, ctypes.c_int, ctypes.c_double, vp,
                                                vp]
     L.lpm_sphere_tangency.argtypes = [vp, c_i64, c_i64, vp, c_i64, c_i64, c_i64, vp, vp]
+    L.lpm_bve_ctx_set_treecode.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int]
+    L.lpm_bve_ctx_tree_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(c_i64),
+                                         ctypes.POINTER(c_i64), c_dp, c_dp, c_dp, c_dp]
+    L.lpm_octree_build.argtypes = [vp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp), vp]
+    c_ip = ctypes.POINTER(ctypes.c_int32)
+    L.lpm_octree_info.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), c_ip,
+                                  c_ip, c_dp]
+    L.lpm_octree_arrays.argtypes = [vp] + [ctypes.POINTER(vp)] * 8
+    L.lpm_octree_destroy.argtypes = [vp]
     L.lpm_errnorms.argtypes = [vp, vp, c_i64, c_i64, vp, c_i64, c_i64, vp, vp, c_i64, ctypes.c_int, ctypes.c_uint,
                                c_dp, vp]
     L.lpm_bve_server_create.argtypes = [ctypes.POINTER(ServerOpts), ctypes.POINTER(vp)]

@@ -129,6 +129,67 @@ def sphere_tangency(x: torch.Tensor, u: torch.Tensor, out: Optional[torch.Tensor
     return out
 
 
+class _DeviceView:
+    """A borrowed device array, exposed to torch through __cuda_array_interface__."""
+
+    def __init__(self, ptr: int, shape, typestr: str):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (ptr, False),
+                                         "version": 2, "strides": None}
+
+
+class Octree:
+    """The Morton octree of src/LpmOctree.cpp built on the device (include/lpm_octree.h) over
+    float64 (n, 3) device points; `arrays()` copies its device arrays into torch tensors."""
+
+    def __init__(self, x: torch.Tensor, max_depth: int, neighbors: bool = True, stream=None):
+        assert x.dtype == torch.float64 and x.is_cuda and x.dim() == 2 and x.shape[1] == 3
+        h = ctypes.c_void_p()
+        L.check(L.lib().lpm_octree_build(_vp(x), x.stride(0), x.stride(1), x.shape[0], max_depth, int(neighbors),
+                                         ctypes.byref(h), _stream(stream)))
+        self._h = h
+        d, nn, n = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int64()
+        L.lib().lpm_octree_info(h, ctypes.byref(d), ctypes.byref(nn), ctypes.byref(n), None, None, None)
+        self.max_depth, self.nnodes, self.npoints = d.value, nn.value, n.value
+        npl = (ctypes.c_int32 * (self.max_depth + 1))()
+        base = (ctypes.c_int32 * (self.max_depth + 1))()
+        box = (ctypes.c_double * 6)()
+        L.lib().lpm_octree_info(h, None, None, None, npl, base, box)
+        self.nnodes_per_level = np.array(npl[:], dtype=np.int32)
+        self.base_address = np.array(base[:], dtype=np.int32)
+        self.box = np.array(box[:])
+        self.neighbors = neighbors
+
+    def arrays(self) -> dict:
+        ptrs = [ctypes.c_void_p() for _ in range(8)]
+        L.lib().lpm_octree_arrays(self._h, *[ctypes.byref(p) for p in ptrs])
+        nn, n = self.nnodes, self.npoints
+        spec = [("keys", (nn,), "<u4"), ("pt_inds", (nn, 2), "<i4"), ("parents", (nn,), "<i4"),
+                ("kids", (nn, 8), "<i4"), ("neighbors", (nn, 27), "<i4"), ("sorted_pts", (n, 3), "<f8"),
+                ("orig_ids", (n,), "<i4"), ("pt_in_leaf", (n,), "<i4")]
+        out = {}
+        for (name, shape, ts), p in zip(spec, ptrs):
+            if p.value is None:
+                out[name] = None
+                continue
+            if ts == "<u4":  # torch has no uint32 arithmetic everywhere: read as int32, reinterpret on the host
+                t = torch.as_tensor(_DeviceView(p.value, shape, "<i4"), device="cuda").clone()
+                out[name] = t.cpu().numpy().view(np.uint32)
+            else:
+                out[name] = torch.as_tensor(_DeviceView(p.value, shape, ts), device="cuda").clone()
+        return out
+
+    def close(self):
+        if self._h:
+            L.lib().lpm_octree_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def mesh_face_verts(seed: int, level: int) -> np.ndarray:
     """Face-to-vertex connectivity (nfaces x 3 or 4) of build_mesh(seed, level)."""
     _, nf, _ = mesh_counts(seed, level)
@@ -250,6 +311,21 @@ class Context:
         afterwards (None = default)."""
         t, k, s, b = shape if shape else (0, 0, 0, 0)
         L.check(self._lib.lpm_bve_ctx_set_shape(self.handle, t, k, s, b), self.handle)
+
+    def set_treecode(self, degree: int = 8, theta: float = 0.6, leaf_points: int = 512):
+        """Tree-code parameters for calls with flags & TREECODE (include/lpm_bve.h)."""
+        L.check(self._lib.lpm_bve_ctx_set_treecode(self.handle, degree, theta, leaf_points), self.handle)
+
+    def tree_stats(self) -> dict:
+        """Octree depth and nodes, far clusters and pairs of the last tree-code evaluation."""
+        d, nodes, far = ctypes.c_int(), L.c_i64(), L.c_i64()
+        pairs, dp, fp = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        ph = (ctypes.c_double * 3)()
+        L.check(self._lib.lpm_bve_ctx_tree_stats(self.handle, ctypes.byref(d), ctypes.byref(nodes), ctypes.byref(far),
+                                                 ctypes.byref(pairs), ctypes.byref(dp), ctypes.byref(fp), ph),
+                self.handle)
+        return dict(depth=d.value, nodes=nodes.value, far_clusters=far.value, pairs=pairs.value,
+                    direct_pairs=dp.value, far_pairs=fp.value, build_ms=ph[0], upward_ms=ph[1], list_ms=ph[2])
 
     def timing(self, reset: bool = True):
         """(summed pair-kernel milliseconds, launches) since the last reset."""

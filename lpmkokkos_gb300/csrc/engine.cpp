@@ -12,6 +12,7 @@
 #include "lpm_bve_ensemble.h"
 #include "engine.hpp"
 #include "engine_core.hpp"
+#include "tree_eval.hpp"
 
 #include <algorithm>
 #include <array>
@@ -90,6 +91,8 @@ HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha
     for (size_t i = 0; i < ids.size(); ++i) kv[i] = {keyOf(ids[i]), ids[i]};
     std::sort(kv.begin(), kv.end());
     for (size_t i = 0; i < ids.size(); ++i) ids[i] = kv[i].second;
+    H.slotKeys.resize(ids.size());
+    for (size_t i = 0; i < ids.size(); ++i) H.slotKeys[i] = kv[i].first;
     std::vector<std::pair<uint32_t, int>> ks(srcFace.size());
     for (size_t i = 0; i < srcFace.size(); ++i) ks[i] = {mortonKey(&hb[3 * (size_t)srcFace[i]]), srcFace[i]};
     std::sort(ks.begin(), ks.end());
@@ -145,18 +148,33 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
     }
   // Tile centres: the target nearest the middle of each tile that is not a masked face
   // (masked parents can sit on a leaf and run away; vertices and leaves stay on the sphere).
-  std::vector<int> tileCentre((size_t)P.ntiles);
-  for (int t = 0; t < P.ntiles; ++t) {
-    const int t0 = t * tileSize, cnt = std::min(tileSize, nslots - t0), mid = t0 + cnt / 2;
-    int best = mid;
+  auto centreOf = [&](int t0, int cnt) {
+    const int mid = t0 + cnt / 2;
     for (int d = 0; d < cnt; ++d) {
       const int a = mid - d, b = mid + d;
       auto ok = [&](int q) { return q >= t0 && q < t0 + cnt && (ids[q] < na || !hmask[ids[q] - na]); };
-      if (ok(a)) { best = a; break; }
-      if (ok(b)) { best = b; break; }
+      if (ok(a)) return a;
+      if (ok(b)) return b;
     }
-    tileCentre[t] = best;
+    return mid;
+  };
+  std::vector<int> tileCentre((size_t)P.ntiles);
+  for (int t = 0; t < P.ntiles; ++t) tileCentre[t] = centreOf(t * tileSize, std::min(tileSize, nslots - t * tileSize));
+  // Tree-code tiles: the same slot order cut into runs of at most tileSize slots that never
+  // cross a level-3 Morton cell (a run across a cell boundary can join distant parts of the
+  // sphere, and its one bounding sphere would then accept no far field).
+  std::vector<int2> treeTiles;
+  std::vector<int> treeCentres;
+  for (int t = 0, start = 0; t <= nslots; ++t) {
+    const bool cut = t == nslots || t - start == tileSize ||
+                     (!H.slotKeys.empty() && t > start && (H.slotKeys[t] >> 21) != (H.slotKeys[start] >> 21));
+    if (cut && t > start) {
+      treeTiles.push_back(make_int2(start, t - start));
+      treeCentres.push_back(centreOf(start, t - start));
+      start = t;
+    }
   }
+  P.nTreeTiles = (int)treeTiles.size();
 
   DeviceArena& M = P.mem;
   M.release();
@@ -171,6 +189,10 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   upload(dSelf, self, s);
   upload(dTileSelf, P.tileSelfHost, s);
   upload(dTileCentre, tileCentre, s);
+  P.treeTiles = M.alloc<int2>(std::max<size_t>(1, treeTiles.size()));
+  P.treeCentres = M.alloc<int>(std::max<size_t>(1, treeCentres.size()));
+  upload(P.treeTiles, treeTiles, s);
+  upload(P.treeCentres, treeCentres, s);
   upload(dSrcFace, srcFace, s);
   upload(dSrcSlot, srcSlot, s);
 
@@ -267,6 +289,7 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   }
   B.nitems = (int)items.size();
   B.grid = std::min(B.nitems, slots);
+  B.slots = slots;
   B.itemPairs.resize(items.size());
   for (size_t i = 0; i < items.size(); ++i) {
     const SolvePlan& P = *B.solves[items[i].solve];
@@ -328,6 +351,11 @@ void refreshTables(Batch& B, cudaStream_t s) {
 // One evaluation of the direct sums for every solve of the batch.
 void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s) {
   LPM_CUDA(launchPrep(B.stageDev, B.prepMap, B.nPrepBlocks, prepStage, B.prec, B.counter, s));
+  if (B.treeMode) {  // tree code: octree, lists and the gathered pair kernel, then the same epilogue
+    B.tree->evaluate(*B.solves[0], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
+    LPM_CUDA(launchEpilogue(B.tree->stageDev(), B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
+    return;
+  }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (B.timer) {
     e0 = B.timer->get();
@@ -358,6 +386,8 @@ void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s) {
 // context and C ABI
 // ---------------------------------------------------------------------------------------
 struct lpm_bve_ctx {
+  lpm::TreeParams treeParams;                 // tree-code parameters (lpm_bve_ctx_set_treecode)
+  std::shared_ptr<lpm::TreeEval> lastTree;    // tree state of the last tree-code evaluation
   lpm::DeviceInfo dev;
   int autotune = 0, verbose = 0;
   std::string err;
@@ -395,8 +425,9 @@ void setDevice(lpm_bve_ctx* ctx) {
 
 Precision precOf(unsigned flags) { return (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64; }
 
-PairShape shapeFor(const lpm_bve_ctx* ctx, Precision p) {
+PairShape shapeFor(const lpm_bve_ctx* ctx, Precision p, bool tree) {
   if (p != Precision::FP32C) return kFP64Shape;
+  if (tree) return kTreeShape;  // the tree kernel's shape
   return ctx && ctx->forced.threads > 0 ? ctx->forced : kDefaultFP32C;
 }
 
@@ -404,9 +435,9 @@ bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si &
 
 // True when a cached single-solve batch was built for the same geometry.
 bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision prec, const ParticleIO& io,
-                  const uint8_t* mask, bool skipMasked, bool sort, double eps) {
+                  const uint8_t* mask, bool skipMasked, bool sort, double eps, bool tree) {
   if (!B || B->solves.size() != 1) return false;
-  if (!(shapeFor(ctx, prec) == B->shape)) return false;
+  if (!(shapeFor(ctx, prec, tree) == B->shape)) return false;
   const SolvePlan& P = *B->solves[0];
   return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
          sameVec(P.io.bx, io.bx) && P.mask == mask && P.skipMasked == skipMasked && P.sorted == sort &&
@@ -420,12 +451,12 @@ PairShape autotune(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO
 
 std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io,
                                   const uint8_t* mask, bool skipMasked, bool sort, double eps, bool precise,
-                                  cudaStream_t s) {
+                                  bool tree, cudaStream_t s) {
   const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s);
   auto B = std::make_unique<Batch>();
   B->prec = prec;
-  B->shape = shapeFor(ctx, prec);
-  if (prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0)
+  B->shape = shapeFor(ctx, prec, tree);
+  if (!tree && prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0)
     B->shape = autotune(ctx, mode, prec, io, mask, skipMasked, sort, eps, precise, H, s);
   B->rk4 = (mode == Mode::RK4);
   B->precise = precise;
@@ -516,6 +547,15 @@ void bindIO(Batch& B, size_t m, const ParticleIO& io, double dt, double omega, c
     changed = true;
   }
   (void)s;
+}
+
+// Switches a single-solve batch between the direct sum and the tree code for this call.
+void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree) {
+  B.treeMode = tree;
+  if (!tree) return;
+  if (!B.tree) B.tree = std::make_shared<TreeEval>();
+  B.treeParams = ctx->treeParams;
+  ctx->lastTree = B.tree;
 }
 
 }  // namespace
@@ -658,6 +698,40 @@ int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches
   return LPM_OK;
 }
 
+int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  if (degree < 2 || degree > 10 || !(theta > 0.0 && theta < 1.0) || leaf_points < 1) {
+    ctx->err = "set_treecode: degree 2..10, theta in (0, 1), leaf_points >= 1";
+    return LPM_ERR_INVALID_ARGUMENT;
+  }
+  ctx->treeParams.degree = degree;
+  ctx->treeParams.theta = theta;
+  ctx->treeParams.leafPoints = leaf_points;
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_tree_stats(lpm_bve_ctx* ctx, int* depth, int64_t* nodes, int64_t* far_clusters, double* pairs,
+                           double* direct_pairs, double* far_pairs, double* phase_ms) {
+  if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  if (!ctx->lastTree) {
+    ctx->err = "tree_stats: no tree-code evaluation yet";
+    return LPM_ERR_STATE;
+  }
+  const TreeStats& t = ctx->lastTree->stats();
+  if (depth) *depth = t.depth;
+  if (nodes) *nodes = t.nodes;
+  if (far_clusters) *far_clusters = t.farClusters;
+  if (pairs) *pairs = t.pairs;
+  if (direct_pairs) *direct_pairs = t.directPairs;
+  if (far_pairs) *far_pairs = t.farPairs;
+  if (phase_ms) {
+    phase_ms[0] = t.buildMs;
+    phase_ms[1] = t.upwardMs;
+    phase_ms[2] = t.listMs;
+  }
+  return LPM_OK;
+}
+
 int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources* src, double* u, int64_t u_si,
                      int64_t u_sc, double* psi, unsigned flags, double eps, lpm_stream_t stream) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
@@ -702,17 +776,20 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     const Precision prec = precOf(flags);
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = colloc && (flags & LPM_BVE_SKIP_MASKED_TARGETS);
-    if (!sameGeometry(ctx, ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps)) {
+    const bool tree = flags & LPM_BVE_TREECODE;
+    if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "velocity: the tree code needs LPM_BVE_FP32C");
+    if (!sameGeometry(ctx, ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
       if (ctx->velBatch) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
       ctx->velBatch.reset();
       const bool precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
-      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, s);
+      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s);
       ctx->velBatch->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
     Batch& B = *ctx->velBatch;
     // Distinct targets are arbitrary points unless the caller says they are mesh points.
     B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
+    useTree(ctx, B, tree);
     bool changed = false;
     bindIO(B, 0, io, 0.0, 0.0, s, changed);
     if (changed) refreshTables(B, s);
@@ -758,10 +835,12 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const Precision prec = precOf(flags);
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
-    if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps)) {
+    const bool tree = flags & LPM_BVE_TREECODE;
+    if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "rk4_step: the tree code needs LPM_BVE_FP32C");
+    if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps, tree)) {
       if (ctx->rkBatch) LPM_CUDA(cudaDeviceSynchronize());
       ctx->rkBatch.reset();
-      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, false, s);
+      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, false, tree, s);
       ctx->rkBatch->solves[0]->stage.io = ParticleIO{};
     }
     Batch& B = *ctx->rkBatch;
@@ -772,7 +851,8 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const bool renorm = flags & LPM_BVE_RENORM;
     const bool rcp = flags & LPM_BVE_RCP_APPROX;
     B.rcpApprox = rcp;
-    if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer) {
+    useTree(ctx, B, tree);
+    if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // the tree build reads sizes back: no capture
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
       B.timer = nullptr;
@@ -903,7 +983,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     E->batch = std::make_unique<Batch>();
     Batch& B = *E->batch;
     B.prec = precOf(flags);
-    B.shape = shapeFor(ctx, B.prec);
+    B.shape = shapeFor(ctx, B.prec, false);
     B.rk4 = true;
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
     const bool sort = !(flags & LPM_BVE_NO_SORT);

@@ -5,6 +5,7 @@
 
 #include "lpm_bve.h"
 #include "engine.hpp"
+#include "tree.hpp"
 
 #include <algorithm>
 #include <climits>
@@ -143,6 +144,10 @@ struct SolvePlan {
   int nslots = 0, ns = 0, ntiles = 0, nchunks = 1, tileSize = 1, chunkLen = 0;
   double eps2 = 0.0;
   std::vector<int2> tileSelfHost;
+  // tree-code target tiles: runs of <= tileSize slots inside one level-3 Morton cell
+  int nTreeTiles = 0;
+  int2* treeTiles = nullptr;    // [nTreeTiles] {first slot, count}
+  int* treeCentres = nullptr;   // [nTreeTiles] centre slot
   DeviceArena mem;
   bool partialReady = false;  // partial-sum buffer allocated (once per plan)
   SolveStage stage{};
@@ -179,6 +184,8 @@ struct PairTimer {
   }
 };
 
+class TreeEval;
+
 struct Batch {
   PairTimer* timer = nullptr;  // non-null: bracket each pair launch with events (direct launches only)
   std::vector<std::unique_ptr<SolvePlan>> owned;  // plans owned by this batch (single solves, ensembles)
@@ -197,6 +204,11 @@ struct Batch {
   int4* prepMap = nullptr;
   int4* slotMap = nullptr;
   int* counter = nullptr;
+  // tree code (LPM_BVE_TREECODE): evaluation state, created on first use
+  std::shared_ptr<TreeEval> tree;
+  bool treeMode = false;
+  TreeParams treeParams;
+  int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)
   // captured RK4 step
   cudaGraphExec_t graph = nullptr;
   bool graphQuirk = false, graphRenorm = false, graphRcp = false;
@@ -216,6 +228,7 @@ struct HostPlan {
   int64_t na = 0, nb = 0;
   std::vector<uint8_t> hmask;
   std::vector<int> ids, srcFace, self, srcSlot;
+  std::vector<uint32_t> slotKeys;  // Morton key of each slot (sorted plans only)
 };
 
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,

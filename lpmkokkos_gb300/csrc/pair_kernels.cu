@@ -27,6 +27,7 @@
 // common path carries no compare.
 
 #include "engine.hpp"
+#include "tree.hpp"
 
 #include <climits>
 #include <cstdio>
@@ -116,8 +117,10 @@ struct SourceTile<true> {
 //             operand needs a sign flip), accumulated as v += s' d and folded with a minus sign;
 //   !NEWTON:  s  = w r, folded with a plus sign.
 // Each kSub-source block is summed in FP32, then added to the Kahan-compensated accumulators.
-template <int K, bool PSI, bool CHECKED, bool PRECISE, bool NEWTON>
-__device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc, int jbase,
+// GATHER: the staged sources are not consecutive; ids[j] holds the source index of slot j for
+// the self-pair check (the tree code's index lists), else slot j is source jbase + j.
+template <int K, bool PSI, bool CHECKED, bool PRECISE, bool NEWTON, bool GATHER = false>
+__device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc, int jbase, const int* ids,
                                           const float2 (&nx)[K / 2], const float2 (&ny)[K / 2],
                                           const float2 (&nz)[K / 2], const float2 (&nlx)[K / 2],
                                           const float2 (&nly)[K / 2], const float2 (&nlz)[K / 2],
@@ -174,8 +177,9 @@ __device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc
         float2 lg, ww;
         if (PSI) { lg = make_float2(lg2Approx(q.x), lg2Approx(q.y)); ww = W; }
         if (CHECKED) {  // a self pair has q ~ 0: drop its (inf/NaN) terms after they are formed
-          if (jbase + j == self[2 * m]) { sp.x = 0.f; if (PSI) { lg.x = 0.f; ww.x = 0.f; } }
-          if (jbase + j == self[2 * m + 1]) { sp.y = 0.f; if (PSI) { lg.y = 0.f; ww.y = 0.f; } }
+          const int jj = GATHER ? ids[j] : jbase + j;
+          if (jj == self[2 * m]) { sp.x = 0.f; if (PSI) { lg.x = 0.f; ww.x = 0.f; } }
+          if (jj == self[2 * m + 1]) { sp.y = 0.f; if (PSI) { lg.y = 0.f; ww.y = 0.f; } }
         }
         vx[m] = fma2(sp, dx, vx[m]);
         vy[m] = fma2(sp, dy, vy[m]);
@@ -199,6 +203,120 @@ __device__ __forceinline__ void fp32cTile(const SourceTile<PRECISE>& T, int nsrc
         kahanAdd(hp[2 * m + 1], cp[2 * m + 1], vp[m].y);
         kahanAdd(hw[2 * m], cw[2 * m], vw[m].x);
         kahanAdd(hw[2 * m + 1], cw[2 * m + 1], vw[m].y);
+      }
+    }
+  }
+}
+
+// The K targets of a thread in tile-relative FP32 form (fast) or hi/lo form (precise), as K/2
+// negated pairs, with C = D_i + 2 eps^2 and each target's self index; plus the tile centre's
+// hi/lo parts (fast formulation).
+template <int K>
+struct TileTargets {
+  float2 nx[K / 2], ny[K / 2], nz[K / 2], nlx[K / 2], nly[K / 2], nlz[K / 2], C[K / 2];
+  int self[K];
+  float chx, chy, chz, clx, cly, clz;
+};
+
+template <int NTH, int K, bool PRECISE>
+__device__ __forceinline__ void loadTileTargets(const double* __restrict__ tx, int n, int tile0, int tcount,
+                                                int centreSlot, const int* __restrict__ selfIdx, double eps2,
+                                                int* sCentre, TileTargets<K>& tt) {
+  // Tile centre (slots are spatially sorted).  A masked parent that coincides with a leaf
+  // carries inf/NaN or a runaway position (as in the reference); it must never become the
+  // centre, or every target of the tile would lose its precision.
+  float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
+  if (!PRECISE) {
+    double cxd, cyd, czd;
+    tileCentre(tx, n, tile0, tcount, NTH, centreSlot, sCentre, cxd, cyd, czd);
+    chx = __double2float_rn(cxd); chy = __double2float_rn(cyd); chz = __double2float_rn(czd);
+    clx = __double2float_rn(cxd - (double)chx);
+    cly = __double2float_rn(cyd - (double)chy);
+    clz = __double2float_rn(czd - (double)chz);
+  }
+  tt.chx = chx; tt.chy = chy; tt.chz = chz; tt.clx = clx; tt.cly = cly; tt.clz = clz;
+
+  // Targets k = 2m, 2m+1 of this thread form pair m (slots tile0 + threadIdx.x + k NTH).
+  float ax[K], ay[K], az[K], lx[K], ly[K], lz[K], Ck[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int slot = tile0 + threadIdx.x + k * NTH;
+    if (threadIdx.x + k * NTH < tcount) {
+      const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
+      const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
+      const float ex = __double2float_rn(x - (double)hx), ey = __double2float_rn(y - (double)hy),
+                  ez = __double2float_rn(z - (double)hz);
+      if (PRECISE) {
+        ax[k] = hx; ay[k] = hy; az[k] = hz; lx[k] = ex; ly[k] = ey; lz[k] = ez;
+      } else {
+        ax[k] = relCoord(hx, ex, chx, clx);
+        ay[k] = relCoord(hy, ey, chy, cly);
+        az[k] = relCoord(hz, ez, chz, clz);
+        lx[k] = ly[k] = lz[k] = 0.f;
+      }
+      Ck[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * eps2);
+      tt.self[k] = selfIdx[slot];
+    } else {
+      ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; lx[k] = ly[k] = lz[k] = 0.f; Ck[k] = 1.f; tt.self[k] = -1;
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < K / 2; ++m) {
+    tt.nx[m] = make_float2(-ax[2 * m], -ax[2 * m + 1]);
+    tt.ny[m] = make_float2(-ay[2 * m], -ay[2 * m + 1]);
+    tt.nz[m] = make_float2(-az[2 * m], -az[2 * m + 1]);
+    tt.nlx[m] = make_float2(-lx[2 * m], -lx[2 * m + 1]);
+    tt.nly[m] = make_float2(-ly[2 * m], -ly[2 * m + 1]);
+    tt.nlz[m] = make_float2(-lz[2 * m], -lz[2 * m + 1]);
+    tt.C[m] = make_float2(Ck[2 * m], Ck[2 * m + 1]);
+  }
+}
+
+// Stages one source record (p0, p1) in slot j: relative to the tile centre (fast) or as hi/lo
+// parts (precise).  A dead slot gets zero weight and D = 1 at the centre / origin, so it adds
+// exactly 0.
+template <int K, bool PRECISE>
+__device__ __forceinline__ void stageSource(int j, bool live, const float4& p0, const float4& p1,
+                                            const TileTargets<K>& tt, float4* sXY, float4* sZW, float2* sD,
+                                            float4* sLXY, float2* sLZ) {
+  float x = 0.f, y = 0.f, z = 0.f, wj = 0.f, dj = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
+  if (live) {
+    if (PRECISE) {
+      x = p0.x; y = p0.y; z = p0.z; ux = p1.x; uy = p1.y; uz = p1.z;
+    } else {
+      x = relCoord(p0.x, p1.x, tt.chx, tt.clx);
+      y = relCoord(p0.y, p1.y, tt.chy, tt.cly);
+      z = relCoord(p0.z, p1.z, tt.chz, tt.clz);
+    }
+    wj = p0.w;
+    dj = p1.w;
+  }
+  sXY[j] = make_float4(x, x, y, y);
+  sZW[j] = make_float4(z, z, wj, wj);
+  sD[j] = make_float2(dj, dj);
+  if (PRECISE) {
+    sLXY[j] = make_float4(ux, ux, uy, uy);
+    sLZ[j] = make_float2(uz, uz);
+  }
+}
+
+// Writes a thread's compensated sums as FP64 partials [comp][slot] of one chunk.
+template <int NTH, int K, bool PSI>
+__device__ __forceinline__ void writePartials(double* __restrict__ out, int n, int tile0, int tcount,
+                                              const float (&hx)[K], const float (&hy)[K], const float (&hz)[K],
+                                              const float (&cx)[K], const float (&cy)[K], const float (&cz)[K],
+                                              const float (&hp)[K], const float (&cp)[K], const float (&hw)[K],
+                                              const float (&cw)[K]) {
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const int slot = tile0 + threadIdx.x + k * NTH;
+    if (threadIdx.x + k * NTH < tcount) {
+      out[slot] = (double)hx[k] - (double)cx[k];
+      out[n + slot] = (double)hy[k] - (double)cy[k];
+      out[2 * n + slot] = (double)hz[k] - (double)cz[k];
+      if (PSI) {
+        out[3 * n + slot] = (double)hp[k] - (double)cp[k];
+        out[4 * n + slot] = (double)hw[k] - (double)cw[k];
       }
     }
   }
@@ -242,55 +360,16 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
     const int tile0 = w.tile * (NTH * K);
     const int tcount = min(NTH * K, n - tile0);
 
-    // Tile centre (slots are spatially sorted).  A masked parent that coincides with a leaf
-    // carries inf/NaN or a runaway position (as in the reference); it must never become the
-    // centre, or every target of the tile would lose its precision.
-    float chx = 0.f, chy = 0.f, chz = 0.f, clx = 0.f, cly = 0.f, clz = 0.f;
-    if (!PRECISE) {
-      double cxd, cyd, czd;
-      tileCentre(S.tx, n, tile0, tcount, NTH, S.tileCentre[w.tile], &sCentre, cxd, cyd, czd);
-      chx = __double2float_rn(cxd); chy = __double2float_rn(cyd); chz = __double2float_rn(czd);
-      clx = __double2float_rn(cxd - (double)chx);
-      cly = __double2float_rn(cyd - (double)chy);
-      clz = __double2float_rn(czd - (double)chz);
-    }
-
-    // Targets k = 2m, 2m+1 of this thread form pair m (slots tile0 + threadIdx.x + k NTH).
-    float ax[K], ay[K], az[K], lx[K], ly[K], lz[K], Ck[K];
-    int self[K];
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      const int slot = tile0 + threadIdx.x + k * NTH;
-      if (threadIdx.x + k * NTH < tcount) {
-        const double x = S.tx[slot], y = S.tx[n + slot], z = S.tx[2 * n + slot];
-        const float hx = __double2float_rn(x), hy = __double2float_rn(y), hz = __double2float_rn(z);
-        const float ex = __double2float_rn(x - (double)hx), ey = __double2float_rn(y - (double)hy),
-                    ez = __double2float_rn(z - (double)hz);
-        if (PRECISE) {
-          ax[k] = hx; ay[k] = hy; az[k] = hz; lx[k] = ex; ly[k] = ey; lz[k] = ez;
-        } else {
-          ax[k] = relCoord(hx, ex, chx, clx);
-          ay[k] = relCoord(hy, ey, chy, cly);
-          az[k] = relCoord(hz, ez, chz, clz);
-          lx[k] = ly[k] = lz[k] = 0.f;
-        }
-        Ck[k] = __double2float_rn((1.0 - (x * x + y * y + z * z)) + 2.0 * S.eps2);
-        self[k] = S.self[slot];
-      } else {
-        ax[k] = 0.f; ay[k] = 0.f; az[k] = 0.f; lx[k] = ly[k] = lz[k] = 0.f; Ck[k] = 1.f; self[k] = -1;
-      }
-    }
-    float2 nx[P], ny[P], nz[P], nlx[P], nly[P], nlz[P], C[P];
-#pragma unroll
-    for (int m = 0; m < P; ++m) {
-      nx[m] = make_float2(-ax[2 * m], -ax[2 * m + 1]);
-      ny[m] = make_float2(-ay[2 * m], -ay[2 * m + 1]);
-      nz[m] = make_float2(-az[2 * m], -az[2 * m + 1]);
-      nlx[m] = make_float2(-lx[2 * m], -lx[2 * m + 1]);
-      nly[m] = make_float2(-ly[2 * m], -ly[2 * m + 1]);
-      nlz[m] = make_float2(-lz[2 * m], -lz[2 * m + 1]);
-      C[m] = make_float2(Ck[2 * m], Ck[2 * m + 1]);
-    }
+    TileTargets<K> tt;
+    loadTileTargets<NTH, K, PRECISE>(S.tx, n, tile0, tcount, S.tileCentre[w.tile], S.self, S.eps2, &sCentre, tt);
+    const float2 (&nx)[P] = tt.nx;
+    const float2 (&ny)[P] = tt.ny;
+    const float2 (&nz)[P] = tt.nz;
+    const float2 (&nlx)[P] = tt.nlx;
+    const float2 (&nly)[P] = tt.nly;
+    const float2 (&nlz)[P] = tt.nlz;
+    const float2 (&C)[P] = tt.C;
+    const int (&self)[K] = tt.self;
     float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
@@ -302,55 +381,99 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
     for (int b0 = w.s0; b0 < w.s1; b0 += ST) {
       // Stage ST sources; padding (w = 0, D = 1) adds exactly 0.
       for (int j = threadIdx.x; j < ST; j += NTH) {
-        const int s = b0 + j;
-        float x = 0.f, y = 0.f, z = 0.f, wj = 0.f, dj = 1.f, ux = 0.f, uy = 0.f, uz = 0.f;
-        if (s < w.s1) {  // else: at the centre (fast) or the origin (precise), finite q, zero weight
-          const float4 p0 = S.sp0[s];
-          const float4 p1 = S.sp1[s];
-          if (PRECISE) {
-            x = p0.x; y = p0.y; z = p0.z; ux = p1.x; uy = p1.y; uz = p1.z;
-          } else {
-            x = relCoord(p0.x, p1.x, chx, clx);
-            y = relCoord(p0.y, p1.y, chy, cly);
-            z = relCoord(p0.z, p1.z, chz, clz);
-          }
-          wj = p0.w;
-          dj = p1.w;
-        }
-        sXY[j] = make_float4(x, x, y, y);
-        sZW[j] = make_float4(z, z, wj, wj);
-        sD[j] = make_float2(dj, dj);
-        if (PRECISE) {
-          sLXY[j] = make_float4(ux, ux, uy, uy);
-          sLZ[j] = make_float2(uz, uz);
-        }
+        const int src = b0 + j;
+        const bool live = src < w.s1;
+        stageSource<K, PRECISE>(j, live, live ? S.sp0[src] : float4{}, live ? S.sp1[src] : float4{}, tt, sXY, sZW,
+                                sD, sLXY, sLZ);
       }
       __syncthreads();
       const bool checked = (ts.x <= b0 + ST - 1) && (ts.y >= b0);
       if (checked)
-        fp32cTile<K, PSI, true, PRECISE, NEWTON>(T, ST, b0, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz, cx, cy,
-                                                 cz, hp, cp, hw, cw);
+        fp32cTile<K, PSI, true, PRECISE, NEWTON>(T, ST, b0, nullptr, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz,
+                                                 cx, cy, cz, hp, cp, hw, cw);
       else
-        fp32cTile<K, PSI, false, PRECISE, NEWTON>(T, ST, b0, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz, cx, cy,
-                                                  cz, hp, cp, hw, cw);
+        fp32cTile<K, PSI, false, PRECISE, NEWTON>(T, ST, b0, nullptr, nx, ny, nz, nlx, nly, nlz, C, self, hx, hy, hz,
+                                                  cx, cy, cz, hp, cp, hw, cw);
       __syncthreads();
     }
 
     // Partials: [chunk][comp][slot], FP64.
-    double* out = S.partial + (size_t)w.chunk * (PSI ? 5 : 3) * n;
+    writePartials<NTH, K, PSI>(S.partial + (size_t)w.chunk * (PSI ? 5 : 3) * n, n, tile0, tcount, hx, hy, hz, cx,
+                               cy, cz, hp, cp, hw, cw);
+  }
+}
+
+// The tree code's gathered pair kernel: persistent CTAs take target tiles (longest index
+// lists first); each tile walks its flattened list of sorted-source and proxy indices
+// (tree.hpp), staging up to ST gathered records at a time.  Only the last block of a list is
+// padded (to the sub-block of 64).  The self-pair check runs on blocks that hold a source of
+// the tile's own self range.  One FP64 partial chunk per target.
+template <int NTH, int K, int ST, int MINB, bool PSI, bool PRECISE, bool NEWTON>
+__global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict__ dev, int nitems,
+                                                 int* __restrict__ counter) {
+  static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
+  constexpr int P = K / 2;
+  __shared__ float4 sXY[ST];
+  __shared__ float4 sZW[ST];
+  __shared__ float2 sD[ST];
+  __shared__ float4 sLXY[PRECISE ? ST : 1];
+  __shared__ float2 sLZ[PRECISE ? ST : 1];
+  __shared__ int sId[ST];
+  __shared__ int sItem;
+  __shared__ int sCentre;
+  SourceTile<PRECISE> T;
+  T.xy = sXY; T.zw = sZW; T.d = sD;
+  if constexpr (PRECISE) { T.lxy = sLXY; T.lz = sLZ; }
+  const TreeDev& S = *dev;
+
+  for (;;) {
+    if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = sItem;
+    __syncthreads();
+    if (it >= nitems) return;
+    const int item = S.order[it];
+    const int tile = item / S.nchunks, part = item % S.nchunks;
+    const int n = S.nslots;
+    const int2 tr = S.tiles[tile];
+    const int tile0 = tr.x, tcount = tr.y;  // tcount <= NTH * K
+    TileTargets<K> tt;
+    loadTileTargets<NTH, K, PRECISE>(S.tx, n, tile0, tcount, S.tileCentre[tile], S.self, S.eps2, &sCentre, tt);
+    float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-      const int slot = tile0 + threadIdx.x + k * NTH;
-      if (threadIdx.x + k * NTH < tcount) {
-        out[slot] = (double)hx[k] - (double)cx[k];
-        out[n + slot] = (double)hy[k] - (double)cy[k];
-        out[2 * n + slot] = (double)hz[k] - (double)cz[k];
-        if (PSI) {
-          out[3 * n + slot] = (double)hp[k] - (double)cp[k];
-          out[4 * n + slot] = (double)hw[k] - (double)cw[k];
-        }
-      }
+      hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
+      hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
     }
+    const int2 ts = S.tileSelf[tile];
+    // part `part` of the tile's list: [l0, l1), cut at multiples of the sub-block
+    const int64_t tl = S.listOff[tile + 1] - S.listOff[tile];
+    const int64_t l0 = tl * part / S.nchunks / kSub * kSub;
+    const int64_t l1 = part + 1 == S.nchunks ? tl : tl * (part + 1) / S.nchunks / kSub * kSub;
+    const int64_t off = S.listOff[tile] + l0;
+    const int64_t len = l1 - l0;
+    for (int64_t b0 = 0; b0 < len; b0 += ST) {
+      const int nsrc = (int)min((int64_t)ST, (len - b0 + kSub - 1) / kSub * kSub);
+      int hit = 0;
+      for (int j = threadIdx.x; j < nsrc; j += NTH) {
+        const bool live = b0 + j < len;
+        const int id = live ? S.list[off + b0 + j] : INT_MIN;
+        hit |= live && id >= ts.x && id <= ts.y;
+        stageSource<K, PRECISE>(j, live, live ? S.sp0[id] : float4{}, live ? S.sp1[id] : float4{}, tt, sXY, sZW, sD,
+                                sLXY, sLZ);
+        sId[j] = id;
+      }
+      if (__syncthreads_or(hit))
+        fp32cTile<K, PSI, true, PRECISE, NEWTON, true>(T, nsrc, 0, sId, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
+                                                       tt.C, tt.self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+      else
+        fp32cTile<K, PSI, false, PRECISE, NEWTON, true>(T, nsrc, 0, sId, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
+                                                        tt.C, tt.self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+      __syncthreads();
+    }
+    writePartials<NTH, K, PSI>(S.partial + (size_t)part * (PSI ? 5 : 3) * n, n, tile0, tcount, hx, hy, hz, cx, cy, cz,
+                               hp, cp, hw, cw);
+    (void)P;
   }
 }
 
@@ -468,6 +591,24 @@ bool pairShapeSupported(Precision prec, const PairShape& shape) {
 int pairNumComponents(Precision prec, bool psi) {
   if (prec == Precision::FP64) return psi ? 4 : 3;
   return psi ? 5 : 3;
+}
+
+bool treePairShapeSupported(const PairShape& shape) { return shape == kTreeShape; }
+
+cudaError_t launchTreePair(const PairShape& shape, bool psi, bool precise, bool rcpApprox, const TreeDev* dev,
+                           int nitems, int* counter, int grid, cudaStream_t s) {
+  if (!(shape == kTreeShape)) return cudaErrorInvalidValue;
+  if (nitems <= 0 || grid <= 0) return cudaSuccess;
+  constexpr int T = kTreeShape.threads, K = kTreeShape.k, ST = kTreeShape.srcTile, B = kTreeShape.minBlocks;
+  void* fn;
+  if (precise)
+    fn = psi ? (void*)treeFP32C<T, K, ST, B, true, true, true> : (void*)treeFP32C<T, K, ST, B, false, true, true>;
+  else if (rcpApprox)
+    fn = psi ? (void*)treeFP32C<T, K, ST, B, true, false, false> : (void*)treeFP32C<T, K, ST, B, false, false, false>;
+  else
+    fn = psi ? (void*)treeFP32C<T, K, ST, B, true, false, true> : (void*)treeFP32C<T, K, ST, B, false, false, true>;
+  void* args[] = {(void*)&dev, (void*)&nitems, (void*)&counter};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(T), args, 0, s);
 }
 
 int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {

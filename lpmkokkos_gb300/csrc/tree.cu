@@ -1,0 +1,562 @@
+// tree.cu -- the tree-code evaluation (tree.hpp): source octree, upward pass (cluster centres,
+// radii, gnomonic charts and proxy charges), target-tile geometry, interaction lists, and the
+// host orchestration around the gathered pair kernel (pair_kernels.cu).
+//
+// Proxy charges use the barycentric form of Lagrange interpolation at Chebyshev points of the
+// second kind, t_a = cos(pi a / n), weights (-1)^a (halved at both ends) (Berrut & Trefethen,
+// "Barycentric Lagrange interpolation", SIAM Review 46(3), 2004), in the tensor-product form
+// of the barycentric Lagrange tree code (Wang, Krasny & Tlupova, Commun. Comput. Phys. 28(4),
+// 2020), here on a per-cluster gnomonic chart of the sphere.  All reductions run in a fixed
+// order, so an evaluation is reproducible bit for bit.
+
+#include "tree_eval.hpp"
+
+#include <cub/cub.cuh>
+
+#include <algorithm>
+#include <cfloat>
+#include <climits>
+#include <cmath>
+#include <numeric>
+
+namespace lpm {
+namespace {
+
+constexpr int kBlock = 256;
+constexpr int kUpThreads = 128;
+constexpr int kMaxDegree = 10;            // (n+1)^2 <= 121 proxies: one thread per proxy charge
+constexpr int kMaxNodes1D = kMaxDegree + 1;
+constexpr int kStack = 96;                // DFS stack: <= 7 depth + 8 entries for depth <= 10
+// A chart covers sources within ~37 degrees of its centre direction: an octant (54.7 degrees)
+// stretches its gnomonic chart 3x at the edge and its degree-8 interpolant then errs by 1e-5.
+constexpr double kMinChartCos = 0.8;
+
+__device__ __forceinline__ bool sane(double x, double y, double z) {
+  const double r2 = x * x + y * y + z * z;
+  return r2 >= 0.25 && r2 <= 4.0;  // false for NaN
+}
+
+// Fixed-order block reductions (warp shuffles, then the warps' partials in order).
+template <int NT>
+__device__ __forceinline__ double blockSum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int w = 0; w < NT / 32; ++w) t += sh[w];
+  return t;
+}
+template <int NT>
+__device__ __forceinline__ double blockMax(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = -DBL_MAX;
+  for (int w = 0; w < NT / 32; ++w) t = fmax(t, sh[w]);
+  return t;
+}
+template <int NT>
+__device__ __forceinline__ int blockMinI(int v, int* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  int t = INT_MAX;
+  for (int w = 0; w < NT / 32; ++w) t = min(t, sh[w]);
+  return t;
+}
+
+__global__ void srcPositions(const float4* __restrict__ sp0, const float4* __restrict__ sp1, int ns,
+                             double* __restrict__ pos) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ns) return;
+  const float4 a = sp0[i], b = sp1[i];
+  pos[3 * i] = (double)a.x + (double)b.x;
+  pos[3 * i + 1] = (double)a.y + (double)b.y;
+  pos[3 * i + 2] = (double)a.z + (double)b.z;
+}
+
+__global__ void gatherSources(const int* __restrict__ orig, const float4* __restrict__ sp0,
+                              const float4* __restrict__ sp1, int ns, float4* __restrict__ tsp0,
+                              float4* __restrict__ tsp1, int* __restrict__ inv) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= ns) return;
+  const int o = orig[k];
+  tsp0[k] = sp0[o];
+  tsp1[k] = sp1[o];
+  inv[o] = k;
+}
+
+__global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__ inv, int nslots,
+                           int* __restrict__ out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nslots) return;
+  const int s = self[t];
+  out[t] = s >= 0 ? inv[s] : -1;
+}
+
+// Centroid and radius of each target tile over its sane targets (masked parents that sit on a
+// leaf run away or become NaN, as in the reference; they do not widen the tile), and the tile's
+// range of self indices in key order.
+__global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
+                                                       const int2* __restrict__ tiles,
+                                                       const int* __restrict__ selfSorted, double4* __restrict__ geom,
+                                                       int2* __restrict__ tileSelf) {
+  __shared__ double sh[kBlock / 32];
+  __shared__ int shi[kBlock / 32];
+  const int2 tr = tiles[blockIdx.x];
+  const int t0 = tr.x, cnt = tr.y;
+  double sx = 0, sy = 0, sz = 0, sc = 0;
+  int smin = INT_MAX, smax = INT_MIN;
+  for (int q = threadIdx.x; q < cnt; q += kBlock) {
+    const int slot = t0 + q;
+    const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
+    if (sane(x, y, z)) { sx += x; sy += y; sz += z; sc += 1.0; }
+    const int s = selfSorted[slot];
+    if (s >= 0) { smin = min(smin, s); smax = max(smax, s); }
+  }
+  sx = blockSum<kBlock>(sx, sh);
+  sy = blockSum<kBlock>(sy, sh);
+  sz = blockSum<kBlock>(sz, sh);
+  sc = blockSum<kBlock>(sc, sh);
+  smin = blockMinI<kBlock>(smin, shi);
+  smax = -blockMinI<kBlock>(smax == INT_MIN ? INT_MAX : -smax, shi);
+  if (sc == 0.0) {
+    if (threadIdx.x == 0) {
+      geom[blockIdx.x] = make_double4(0, 0, 0, INFINITY);
+      tileSelf[blockIdx.x] = make_int2(smin, smin == INT_MAX ? -1 : smax);
+    }
+    return;
+  }
+  const double cx = sx / sc, cy = sy / sc, cz = sz / sc;
+  double r2 = 0.0;
+  for (int q = threadIdx.x; q < cnt; q += kBlock) {
+    const int slot = t0 + q;
+    const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
+    if (sane(x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
+  }
+  r2 = blockMax<kBlock>(r2, sh);
+  if (threadIdx.x == 0) {
+    geom[blockIdx.x] = make_double4(cx, cy, cz, sqrt(r2));
+    tileSelf[blockIdx.x] = make_int2(smin, smin == INT_MAX ? -1 : smax);
+  }
+}
+
+// Chebyshev points of the second kind t_a = cos(pi a / n) and their barycentric weights.
+struct Cheb {
+  double t[kMaxNodes1D];
+  double w[kMaxNodes1D];
+};
+
+Cheb chebFor(int n) {
+  Cheb c{};
+  for (int a = 0; a <= n; ++a) {
+    c.t[a] = std::cos(kPi * a / n);
+    c.w[a] = ((a & 1) ? -1.0 : 1.0) * ((a == 0 || a == n) ? 0.5 : 1.0);
+  }
+  c.t[0] = 1.0;
+  c.t[n] = -1.0;
+  return c;
+}
+
+// Barycentric Lagrange basis at s of the nodes m + h t_a, a = 0..n.
+__device__ __forceinline__ void basis(double s, double m, double h, int n, const Cheb& C, double* L) {
+  const double u = (s - m) / h;  // in [-1, 1] for the sources of the chart
+  double den = 0.0;
+  int hit = -1;
+  for (int a = 0; a <= n; ++a) {
+    const double d = u - C.t[a];
+    if (d == 0.0) hit = a;
+    L[a] = C.w[a] / d;
+    den += L[a];
+  }
+  if (hit >= 0) {
+    for (int a = 0; a <= n; ++a) L[a] = a == hit ? 1.0 : 0.0;
+    return;
+  }
+  const double r = 1.0 / den;
+  for (int a = 0; a <= n; ++a) L[a] *= r;
+}
+
+// Upward pass, one CTA per octree node: centre and radius of the node's sources; for nodes with
+// more than (n+1)^2 sources all within ~37 degrees of the centre direction, the gnomonic chart,
+// the proxy charges Q_ab (one thread per proxy, sources in index order) and the proxy records
+// at sp0/sp1[ns + g (n+1)^2 + ab].
+__global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, const double* __restrict__ pos,
+                                                     int degree, const Cheb C, int ns, double4* __restrict__ geom,
+                                                     int* __restrict__ approx, float4* __restrict__ sp0,
+                                                     float4* __restrict__ sp1) {
+  __shared__ double sh[kUpThreads / 32];
+  __shared__ double sL[kUpThreads][2 * kMaxNodes1D];
+  const int g = blockIdx.x;
+  const int2 pt = ptInds[g];
+  const int n1 = degree + 1, P = n1 * n1;
+  if (pt.y == 0) {
+    if (threadIdx.x == 0) { geom[g] = make_double4(0, 0, 0, -1.0); approx[g] = 0; }
+    return;
+  }
+  const int k0 = pt.x, k1 = pt.x + pt.y;
+  double sx = 0, sy = 0, sz = 0;
+  for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) { sx += pos[3 * k]; sy += pos[3 * k + 1]; sz += pos[3 * k + 2]; }
+  sx = blockSum<kUpThreads>(sx, sh);
+  sy = blockSum<kUpThreads>(sy, sh);
+  sz = blockSum<kUpThreads>(sz, sh);
+  const double cx = sx / pt.y, cy = sy / pt.y, cz = sz / pt.y;
+  const double cn = sqrt(cx * cx + cy * cy + cz * cz);
+  const bool cand = pt.y > P && cn > 1e-3;
+  // chart frame: c^ and two tangent directions
+  double ux = 0, uy = 0, uz = 1, e1x = 1, e1y = 0, e1z = 0, e2x = 0, e2y = 1, e2z = 0;
+  if (cand) {
+    ux = cx / cn; uy = cy / cn; uz = cz / cn;
+    const double ax = fabs(ux) < 0.9 ? 1.0 : 0.0, ay = 1.0 - ax;  // a = x^ or y^
+    e1x = uy * 0.0 - uz * ay; e1y = uz * ax - ux * 0.0; e1z = ux * ay - uy * ax;  // c^ x a
+    const double e1n = sqrt(e1x * e1x + e1y * e1y + e1z * e1z);
+    e1x /= e1n; e1y /= e1n; e1z /= e1n;
+    e2x = uy * e1z - uz * e1y; e2y = uz * e1x - ux * e1z; e2z = ux * e1y - uy * e1x;
+  }
+  double r2 = 0.0, dmin = DBL_MAX, xmin = DBL_MAX, xmax = -DBL_MAX, ymin = DBL_MAX, ymax = -DBL_MAX;
+  for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) {
+    const double x = pos[3 * k], y = pos[3 * k + 1], z = pos[3 * k + 2];
+    r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
+    if (cand) {
+      const double d = x * ux + y * uy + z * uz;
+      dmin = fmin(dmin, d);
+      if (d > 0.0) {
+        const double xi = (x * e1x + y * e1y + z * e1z) / d, eta = (x * e2x + y * e2y + z * e2z) / d;
+        xmin = fmin(xmin, xi); xmax = fmax(xmax, xi); ymin = fmin(ymin, eta); ymax = fmax(ymax, eta);
+      }
+    }
+  }
+  r2 = blockMax<kUpThreads>(r2, sh);
+  dmin = -blockMax<kUpThreads>(-dmin, sh);
+  xmin = -blockMax<kUpThreads>(-xmin, sh);
+  xmax = blockMax<kUpThreads>(xmax, sh);
+  ymin = -blockMax<kUpThreads>(-ymin, sh);
+  ymax = blockMax<kUpThreads>(ymax, sh);
+  const bool valid = cand && dmin >= kMinChartCos && xmax > xmin && ymax > ymin;
+  if (threadIdx.x == 0) {
+    geom[g] = make_double4(cx, cy, cz, sqrt(r2));
+    approx[g] = valid ? 1 : 0;
+  }
+  if (!valid) return;
+  const double mx = 0.5 * (xmin + xmax), hx = 0.5 * (xmax - xmin);
+  const double my = 0.5 * (ymin + ymax), hy = 0.5 * (ymax - ymin);
+  const int t = threadIdx.x;
+  const int ia = t / n1, ib = t % n1;
+  double q = 0.0;
+  for (int c0 = k0; c0 < k1; c0 += kUpThreads) {
+    const int k = c0 + t;
+    if (k < k1) {
+      const double x = pos[3 * k], y = pos[3 * k + 1], z = pos[3 * k + 2];
+      const double d = x * ux + y * uy + z * uz;
+      basis((x * e1x + y * e1y + z * e1z) / d, mx, hx, degree, C, &sL[t][0]);
+      basis((x * e2x + y * e2y + z * e2z) / d, my, hy, degree, C, &sL[t][n1]);
+      const double w = (double)sp0[k].w;
+      for (int a = 0; a <= degree; ++a) sL[t][a] *= w;  // w L_a(xi): one FMA per proxy below
+    }
+    __syncthreads();
+    if (t < P) {
+      const int m = min(kUpThreads, k1 - c0);
+      for (int j = 0; j < m; ++j) q = fma(sL[j][ia], sL[j][n1 + ib], q);
+    }
+    __syncthreads();
+  }
+  if (t < P) {
+    const double xi = mx + hx * C.t[ia], eta = my + hy * C.t[ib];
+    double px = ux + xi * e1x + eta * e2x, py = uy + xi * e1y + eta * e2y, pz = uz + xi * e1z + eta * e2z;
+    const double pn = sqrt(px * px + py * py + pz * pz);
+    px /= pn; py /= pn; pz /= pn;
+    const float hx0 = __double2float_rn(px), hy0 = __double2float_rn(py), hz0 = __double2float_rn(pz);
+    const int slot = ns + g * P + t;
+    sp0[slot] = make_float4(hx0, hy0, hz0, __double2float_rn(q));
+    sp1[slot] = make_float4(__double2float_rn(px - (double)hx0), __double2float_rn(py - (double)hy0),
+                            __double2float_rn(pz - (double)hz0), __double2float_rn(1.0 - (px * px + py * py + pz * pz)));
+  }
+}
+
+struct Levels {
+  int base[kOctreeMaxDepth + 2];
+};
+
+// Interaction lists, one warp per target tile (every lane walks the same tree; ranges are
+// written by the whole warp).  FILL = false: list length and far-field length per tile;
+// FILL = true: the flattened index list at listOff[tile], contiguous direct ranges merged.
+template <bool FILL>
+__global__ void __launch_bounds__(128) traverse(const double4* __restrict__ tileGeom, int ntiles,
+                                                const double4* __restrict__ geom, const int* __restrict__ approx,
+                                                const int2* __restrict__ ptInds, const int* __restrict__ kids,
+                                                Levels lv, int depth, double theta, int P, int ns,
+                                                int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
+                                                const int64_t* __restrict__ listOff, int* __restrict__ list) {
+  const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (tile >= ntiles) return;
+  const double4 tg = tileGeom[tile];
+  int stack[kStack];
+  int sp = 0;
+  stack[sp++] = 0;  // the root (level 0, global index 0)
+  int64_t len = 0, far = 0;
+  int64_t o = FILL ? listOff[tile] : 0;
+  int rs = 0, rl = 0;  // pending direct range (FILL)
+  auto flush = [&]() {
+    for (int k = lane; k < rl; k += 32) list[o + k] = rs + k;
+    o += rl;
+    rl = 0;
+  };
+  auto direct = [&](int start, int count) {
+    len += count;
+    if (FILL) {
+      if (rl > 0 && rs + rl == start) {
+        rl += count;
+      } else {
+        flush();
+        rs = start;
+        rl = count;
+      }
+    }
+  };
+  while (sp > 0) {
+    const int g = stack[--sp];
+    const int2 pt = ptInds[g];
+    if (pt.y == 0) continue;
+    const double4 ng = geom[g];
+    const double dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
+    const double R = sqrt(dx * dx + dy * dy + dz * dz);
+    const bool mac = (tg.w + ng.w) < theta * R;
+    int lev = 0;
+    while (lev < depth && g >= lv.base[lev + 1]) ++lev;
+    if (mac && approx[g]) {
+      len += P;
+      far += P;
+      if (FILL) {
+        flush();
+        const int p0 = ns + g * P;
+        for (int k = lane; k < P; k += 32) list[o + k] = p0 + k;
+        o += P;
+      }
+    } else if (mac && pt.y <= P) {  // well separated but smaller than its proxy set
+      direct(pt.x, pt.y);
+    } else if (lev < depth) {  // too close, or no valid chart: open the node
+      for (int c = 7; c >= 0; --c) {
+        const int kid = kids[8 * g + c];
+        if (kid >= 0 && sp < kStack) stack[sp++] = lv.base[lev + 1] + kid;
+      }
+    } else {
+      direct(pt.x, pt.y);
+    }
+  }
+  if (FILL) {
+    flush();
+  } else if (lane == 0) {
+    lens[tile] = len;
+    farLens[tile] = far;
+  }
+}
+
+inline unsigned blocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
+
+void ck(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    fail(e == cudaErrorMemoryAllocation ? LPM_ERR_OUT_OF_MEMORY : LPM_ERR_CUDA, "tree code %s: %s", what,
+         cudaGetErrorString(e));
+  }
+}
+
+}  // namespace
+
+int treeDepthFor(int64_t n, int leafPoints) {
+  int d = 1;
+  while (d < kOctreeMaxDepth && 4.7 * std::pow(4.0, d) * std::max(1, leafPoints) < (double)n) ++d;
+  return d;
+}
+
+template <typename T>
+T* TreeEval::grow(Buf& b, size_t count, cudaStream_t s) {
+  const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
+  if (b.bytes < bytes) {
+    if (b.p) ck(cudaFreeAsync(b.p, s), "free");
+    b.p = nullptr;
+    b.bytes = 0;
+    const size_t want = bytes + bytes / 4;
+    ck(cudaMallocAsync(&b.p, want, s), "allocation");
+    b.bytes = want;
+  }
+  return static_cast<T*>(b.p);
+}
+
+TreeEval::~TreeEval() {
+  cudaDeviceSynchronize();
+  for (Buf* b : all_)
+    if (b->p) cudaFree(b->p);
+}
+
+void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& shape, bool psi, bool precise,
+                        bool rcpApprox, int slots, PairTimer* timer, cudaStream_t s) {
+  if (tp.degree < 2 || tp.degree > kMaxDegree) fail(LPM_ERR_INVALID_ARGUMENT, "tree code: degree must be 2..%d", kMaxDegree);
+  if (!(tp.theta > 0.0 && tp.theta < 1.0)) fail(LPM_ERR_INVALID_ARGUMENT, "tree code: theta must be in (0, 1)");
+  if (!treePairShapeSupported(shape)) fail(LPM_ERR_NOT_SUPPORTED, "tree code: plan built for another launch shape");
+  const int ns = Pl.ns, nslots = Pl.nslots, ntiles = Pl.nTreeTiles;
+  if (tilesOf_ != Pl.treeTiles) {  // tile sizes of this plan, for the pair statistics
+    tilesOf_ = Pl.treeTiles;
+    hTiles_.resize(ntiles);
+    ck(cudaMemcpyAsync(hTiles_.data(), Pl.treeTiles, sizeof(int2) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
+  }
+  const int P = (tp.degree + 1) * (tp.degree + 1);
+  stats_ = TreeStats{};
+  // phase timing (with the context's timer): events at the phase boundaries, read at the sync
+  cudaEvent_t ev[5] = {};
+  if (timer)
+    for (auto& e : ev) e = timer->get();
+  auto mark = [&](int i) {
+    if (timer) ck(cudaEventRecord(ev[i], s), "event");
+  };
+  mark(0);
+
+  const int* selfSorted = nullptr;
+  int nnodes = 0;
+  float4* tsp0 = nullptr;
+  float4* tsp1 = nullptr;
+  double4* geom = nullptr;
+  int* approx = nullptr;
+  if (ns > 0) {
+    // 1-3. octree over the stage positions, sources in key order
+    double* pos = grow<double>(bPos, 3 * (size_t)ns, s);
+    srcPositions<<<blocks(ns), kBlock, 0, s>>>(Pl.stage.sp0, Pl.stage.sp1, ns, pos);
+    const int depth = treeDepthFor(ns, tp.leafPoints);
+    tree_.build(pos, 3, 1, ns, depth, false, s);
+    mark(1);
+    nnodes = (int)tree_.nnodes;
+    stats_.depth = depth;
+    stats_.nodes = nnodes;
+    const size_t nrec = (size_t)ns + (size_t)nnodes * P;
+    tsp0 = grow<float4>(bSp0, nrec, s);
+    tsp1 = grow<float4>(bSp1, nrec, s);
+    int* inv = grow<int>(bInv, ns, s);
+    gatherSources<<<blocks(ns), kBlock, 0, s>>>(tree_.origIds, Pl.stage.sp0, Pl.stage.sp1, ns, tsp0, tsp1, inv);
+    int* ss = grow<int>(bSelf, nslots, s);
+    sortedSelf<<<blocks(nslots), kBlock, 0, s>>>(Pl.dev.self, inv, nslots, ss);
+    selfSorted = ss;
+    // 4. upward pass
+    geom = grow<double4>(bGeom, nnodes, s);
+    approx = grow<int>(bApprox, nnodes, s);
+    upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns, geom, approx,
+                                         tsp0, tsp1);
+    mark(2);
+  } else {
+    mark(1);
+    mark(2);
+    int* ss = grow<int>(bSelf, nslots, s);
+    ck(cudaMemsetAsync(ss, 0xff, sizeof(int) * (size_t)nslots, s), "memset");  // -1: no sources
+    selfSorted = ss;
+    tsp0 = grow<float4>(bSp0, 1, s);
+    tsp1 = grow<float4>(bSp1, 1, s);
+  }
+  // 5. tiles
+  double4* tgeom = grow<double4>(bTileGeom, ntiles, s);
+  int2* tself = grow<int2>(bTileSelf, ntiles, s);
+  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, selfSorted, tgeom, tself);
+  // 6. interaction lists: lengths, offsets and launch order on the host, then the indices
+  int64_t* lens = grow<int64_t>(bLen, ntiles, s);
+  int64_t* fars = grow<int64_t>(bFar, ntiles, s);
+  Levels lv{};
+  for (int l = 0; l <= tree_.depth; ++l) lv.base[l] = tree_.base[l];
+  lv.base[tree_.depth + 1] = nnodes;
+  const unsigned tb = blocks((int64_t)ntiles * 32, 128);
+  if (ns > 0) {
+    traverse<false><<<tb, 128, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
+                                       tp.theta, P, ns, lens, fars, nullptr, nullptr);
+  } else {
+    ck(cudaMemsetAsync(lens, 0, sizeof(int64_t) * ntiles, s), "memset");
+    ck(cudaMemsetAsync(fars, 0, sizeof(int64_t) * ntiles, s), "memset");
+  }
+  mark(3);
+  hLen_.resize(ntiles);
+  hFar_.resize(ntiles);
+  ck(cudaMemcpyAsync(hLen_.data(), lens, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
+  ck(cudaMemcpyAsync(hFar_.data(), fars, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
+  ck(cudaStreamSynchronize(s), "synchronise");
+  hOff_.assign((size_t)ntiles + 1, 0);
+  for (int t = 0; t < ntiles; ++t) {
+    hOff_[t + 1] = hOff_[t] + hLen_[t];
+    const double tc = (double)hTiles_[t].y;
+    stats_.pairs += tc * (double)hLen_[t];
+    stats_.farPairs += tc * (double)hFar_[t];
+    stats_.farClusters += hFar_[t] / std::max(1, P);
+  }
+  stats_.directPairs = stats_.pairs - stats_.farPairs;
+  // Work items: each tile's list in `nchunks` parts (enough items for ~8 waves of CTAs), each
+  // part with its own partial chunk; longest parts first.
+  const int nchunks = std::max(1, std::min(16, (8 * std::max(1, slots) + ntiles - 1) / std::max(1, ntiles)));
+  const int nitems = ntiles * nchunks;
+  hOrder_.resize(nitems);
+  std::iota(hOrder_.begin(), hOrder_.end(), 0);
+  std::stable_sort(hOrder_.begin(), hOrder_.end(),
+                   [&](int a, int b) { return hLen_[a / nchunks] > hLen_[b / nchunks]; });
+  int64_t* off = grow<int64_t>(bOff, (size_t)ntiles + 1, s);
+  int* order = grow<int>(bOrder, nitems, s);
+  int* list = grow<int>(bList, (size_t)std::max<int64_t>(1, hOff_[ntiles]), s);
+  ck(cudaMemcpyAsync(off, hOff_.data(), sizeof(int64_t) * (ntiles + 1), cudaMemcpyHostToDevice, s), "upload");
+  ck(cudaMemcpyAsync(order, hOrder_.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, s), "upload");
+  if (ns > 0)
+    traverse<true><<<tb, 128, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
+                                      tp.theta, P, ns, nullptr, nullptr, off, list);
+  mark(4);
+  // 7. the gathered pair kernel
+  double* partial = grow<double>(bPartial, (size_t)nchunks * 5 * std::max(1, nslots), s);
+  TreeDev& hd = hDev_;
+  hd = TreeDev{};
+  hd.tx = Pl.stage.tx;
+  hd.sp0 = tsp0;
+  hd.sp1 = tsp1;
+  hd.self = selfSorted;
+  hd.tiles = Pl.treeTiles;
+  hd.tileSelf = tself;
+  hd.tileCentre = Pl.treeCentres;
+  hd.listOff = off;
+  hd.list = list;
+  hd.order = order;
+  hd.partial = partial;
+  hd.nslots = nslots;
+  hd.ntiles = ntiles;
+  hd.nchunks = nchunks;
+  hd.eps2 = Pl.eps2;
+  TreeDev* dd = grow<TreeDev>(bDev, 1, s);
+  ck(cudaMemcpyAsync(dd, &hd, sizeof(hd), cudaMemcpyHostToDevice, s), "upload");
+  SolveStage& st = hStage_;
+  st = Pl.stage;
+  st.partial = partial;
+  st.nchunks = nchunks;
+  SolveStage* sd = grow<SolveStage>(bStage, 1, s);
+  ck(cudaMemcpyAsync(sd, &st, sizeof(st), cudaMemcpyHostToDevice, s), "upload");
+  stageDev_ = sd;
+  int* counter = grow<int>(bCounter, 1, s);
+  ck(cudaMemsetAsync(counter, 0, sizeof(int), s), "memset");
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (timer) {
+    e0 = timer->get();
+    e1 = timer->get();
+    ck(cudaEventRecord(e0, s), "event");
+  }
+  ck(launchTreePair(shape, psi, precise, rcpApprox, dd, nitems, counter, std::min(nitems, std::max(1, slots)), s),
+     "pair launch");
+  if (timer) {
+    ck(cudaEventRecord(e1, s), "event");
+    timer->pending.emplace_back(e0, e1);
+    // phases (the traversals end before the pair kernel starts)
+    ck(cudaEventSynchronize(ev[4]), "event");
+    float a = 0.f, b = 0.f, c = 0.f, d = 0.f;
+    ck(cudaEventElapsedTime(&a, ev[0], ev[1]), "event");
+    ck(cudaEventElapsedTime(&b, ev[1], ev[2]), "event");
+    ck(cudaEventElapsedTime(&c, ev[2], ev[3]), "event");
+    ck(cudaEventElapsedTime(&d, ev[3], ev[4]), "event");
+    stats_.buildMs = a;
+    stats_.upwardMs = b;
+    stats_.listMs = c + d;  // tile geometry and count traversal, then the fill traversal
+    for (auto& e : ev) timer->pool.push_back(e);
+  }
+}
+
+}  // namespace lpm
