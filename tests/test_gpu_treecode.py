@@ -1,0 +1,140 @@
+"""Tree-code evaluation (LPM_BVE_TREECODE, include/lpm_bve.h) against the direct sums.
+
+The tree code is an approximation outside the reference: far source clusters act through
+chart-interpolated proxies (lpmkokkos_gb300/csrc/tree.hpp).  Its bar is the FP32C bar --
+relative L2 <= 1e-6 against the FP64 direct sum -- at the default parameters (degree 8,
+theta 0.6, 512 sources per leaf; measured 8e-8 at icosahedral levels 6-7 and 1.2e-7 at level 8).
+Masked icosahedral parents coincide with a leaf and are NaN in every path, so comparisons take
+vertices and leaf faces."""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+import lpmkokkos_gb300 as P
+from lpmkokkos_gb300 import bve
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-6
+OMEGA = 2 * math.pi
+
+
+def _rel(a, b):
+    return (torch.linalg.norm(a - b) / torch.linalg.norm(b)).item()
+
+
+def _sphere(ctx, seed, level):
+    s = bve.BVESphere(seed, level)
+    s.init_vorticity(bve.rh54_gaussians(7, 3), ctx, flags=P.FP32C)
+    torch.cuda.synchronize()
+    leaf = torch.from_numpy(s.mesh["fmask"] == 0).cuda()
+    return s, (s.physFaces, s.relVortFaces, s.faces_area, s.faces_mask), leaf
+
+
+@pytest.fixture
+def tctx(ctx):
+    ctx.set_treecode()  # defaults
+    yield ctx
+    ctx.set_treecode()
+
+
+@pytest.mark.parametrize("seed,level", [(0, 5), (0, 6), (1, 6)])
+def test_velocity_and_psi_against_fp64(tctx, seed, level):
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, seed, level)
+    rv, pv = ctx.velocity(s.physVerts, *src, flags=P.FP64 | P.PSI)
+    rf, pf = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED | P.PSI)
+    tv, qv = ctx.velocity(s.physVerts, *src, flags=P.FP32C | P.MESH_TARGETS | P.TREECODE | P.PSI)
+    tf, qf = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE | P.PSI)
+    torch.cuda.synchronize()
+    errs = [_rel(tv, rv), _rel(tf[leaf], rf[leaf]), _rel(qv, pv), _rel(qf[leaf], pf[leaf])]
+    print("tree code vs FP64 (u verts, u leaves, psi verts, psi leaves):", errs)
+    assert max(errs) <= TOL, errs
+    st = ctx.tree_stats()
+    assert st["far_clusters"] > 0 and st["far_pairs"] > 0
+
+
+def test_reproducible_and_work_reduction(tctx):
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 0, 6)
+    a, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    b, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    torch.cuda.synchronize()
+    assert torch.equal(a[leaf], b[leaf])
+    st = ctx.tree_stats()
+    nt, ns = s.physFaces.shape[0], int(leaf.sum())
+    assert st["pairs"] < 0.5 * nt * ns  # measured 0.23 of the direct pairs at level 6
+    assert st["pairs"] == st["direct_pairs"] + st["far_pairs"]
+
+
+def test_all_direct_limit(tctx):
+    """With a tiny opening parameter no cluster is far: every target meets every source directly
+    (the pair count is exactly targets x sources) and the result is the FP32C direct sum to
+    within FP32C rounding."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 1, 4)
+    ctx.set_treecode(8, 0.01, 512)
+    t, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    r, _ = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED)
+    torch.cuda.synchronize()
+    st = ctx.tree_stats()
+    assert st["far_pairs"] == 0
+    assert st["pairs"] == s.physFaces.shape[0] * int(leaf.sum())
+    assert _rel(t[leaf], r[leaf]) <= TOL
+
+
+def test_arbitrary_distinct_targets(tctx):
+    """Targets that are not mesh points (the hi/lo 'precise' form), 200 of them 1e-4 from a leaf
+    source (a hundredth of the mesh spacing; much closer and 1 - x.y underflows the FP64 sum)."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 0, 6)
+    rng = np.random.default_rng(11)
+    x = rng.normal(size=(30000, 3))
+    x /= np.linalg.norm(x, axis=1, keepdims=True)
+    f = s.physFaces[leaf].cpu().numpy()[:200] + 1e-4
+    x = np.concatenate([x, f / np.linalg.norm(f, axis=1, keepdims=True)])
+    xt = torch.from_numpy(x).cuda()
+    r, _ = ctx.velocity(xt, *src, flags=P.FP64)
+    t, _ = ctx.velocity(xt, *src, flags=P.FP32C | P.TREECODE)
+    torch.cuda.synchronize()
+    assert _rel(t, r) <= TOL
+
+
+def test_rk4_steps(tctx):
+    """Five RK4 steps with the tree code against five FP64 direct steps."""
+    ctx = tctx
+    a, _, leaf = _sphere(ctx, 0, 5)
+    b, _, _ = _sphere(ctx, 0, 5)
+    ctx.rk4_step(a.state(), 0.005, OMEGA, 5, flags=P.FP64)
+    ctx.rk4_step(b.state(), 0.005, OMEGA, 5, flags=P.FP32C | P.TREECODE)
+    torch.cuda.synchronize()
+    errs = [_rel(b.physVerts, a.physVerts), _rel(b.velocityVerts, a.velocityVerts),
+            _rel(b.relVortVerts, a.relVortVerts), _rel(b.velocityFaces[leaf], a.velocityFaces[leaf])]
+    print("rk4 tree vs FP64 (x, u, zeta verts; u leaves):", errs)
+    assert max(errs) <= TOL, errs
+
+
+def test_level8_against_fp32c_direct(tctx):
+    """Full size (icosahedral level 8: 655,362 vertices, 1,310,720 leaf sources): the tree code
+    against the FP32C direct sum (itself 7e-8 from FP64 at this size)."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 0, 8)
+    r, _ = ctx.velocity(s.physVerts, *src, flags=P.FP32C | P.MESH_TARGETS)
+    t, _ = ctx.velocity(s.physVerts, *src, flags=P.FP32C | P.MESH_TARGETS | P.TREECODE)
+    torch.cuda.synchronize()
+    assert _rel(t, r) <= TOL
+    st = ctx.tree_stats()
+    assert st["pairs"] < 0.05 * s.physVerts.shape[0] * int(leaf.sum())
+
+
+def test_invalid(ctx):
+    for args in ((1, 0.6, 512), (11, 0.6, 512), (8, 0.0, 512), (8, 1.0, 512), (8, 0.6, 0)):
+        with pytest.raises(RuntimeError):
+            ctx.set_treecode(*args)
+    s, src, _ = _sphere(ctx, 0, 2)
+    with pytest.raises(RuntimeError) as e:
+        ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED | P.TREECODE)
+    assert "FP32C" in str(e.value)
+    ctx.set_treecode()
