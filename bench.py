@@ -113,6 +113,8 @@ def parse():
                     help="c4: comma-separated weights per level (empty: uniform)")
     ap.add_argument("--kinds", choices=["both", "icos"], default="both", help="c4: mesh seeds")
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
+    ap.add_argument("--no-tree", action="store_true",
+                    help="c2/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
     return ap.parse_args()
 
 
@@ -229,6 +231,7 @@ def run_ours(args, rank, world, local_rank):
     sphere.init_vorticity(ic, ctx, flags=prec, eps=w["eps"])
     torch.cuda.synchronize()
     t_init = time.time() - t0
+    s0 = clone_sphere(bve, sphere) if not args.no_tree and prec == P.FP32C and rank == 0 else None
     st = sphere.state()
 
     def barrier():
@@ -366,6 +369,13 @@ def run_ours(args, rank, world, local_rank):
     # 4) plain FP64 GPU path and FP32C accuracy on a target sample (same state)
     if not args.no_fp64 and rank == 0:
         out["fp64_gpu"] = fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step)
+
+    # 4b) the tree code beside the direct sum (approximation; not the headline)
+    if s0 is not None:
+        tree = tree_leg(P, bve, torch, ctx, s0, w["dt"], w["eps"], args.steps, flush, fma_peak_lane_ops)
+        tree["speedup_vs_direct_fp32c"] = tree["rk4_steps_per_s"] / (args.steps / (el_graph * 1e-3))
+        out["treecode"] = tree
+        del s0
 
     # 5) CPU baseline (rank 0, single GPU only)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
@@ -563,6 +573,58 @@ def run_ensemble(args, rank, world, local_rank):
     ctx.close()
 
 
+def clone_sphere(bve, s):
+    """A second BVESphere on the same mesh holding a copy of s's evolving state."""
+    c = bve.BVESphere(s.seed, s.level, mesh=s.mesh, device=s.physVerts.device)
+    for name in ("physVerts", "relVortVerts", "velocityVerts", "physFaces", "relVortFaces", "velocityFaces"):
+        getattr(c, name).copy_(getattr(s, name))
+    return c
+
+
+def tree_leg(P, bve, torch, ctx, s0, dt, eps, steps, flush, lane_ops, check_steps=2):
+    """The tree code (LPM_BVE_TREECODE: far clusters through chart-interpolated proxies; an
+    approximation outside the reference, reported beside the direct-sum numbers, never in their
+    place) on the same workload, from copies of the initial state s0: its distance from the FP32C
+    direct sum after `check_steps` RK4 steps, then RK4 steps/s over `steps` timed steps with the
+    phase times, the gathered pair kernel's rate and its fraction of the FMA-pipe peak."""
+    omega = 2 * math.pi
+    a, b = clone_sphere(bve, s0), clone_sphere(bve, s0)
+    leaf = torch.from_numpy(s0.mesh["fmask"] == 0).to(s0.physVerts.device)
+    ctx.rk4_step(a.state(), dt, omega, check_steps, flags=P.FP32C, eps=eps)
+    ctx.rk4_step(b.state(), dt, omega, check_steps, flags=P.FP32C | P.TREECODE, eps=eps)
+    torch.cuda.synchronize()
+    rel = lambda x, y: (torch.linalg.norm(x - y) / torch.linalg.norm(y)).item()
+    errs = {"velocity_vertices": rel(b.velocityVerts, a.velocityVerts),
+            "velocity_leaves": rel(b.velocityFaces[leaf], a.velocityFaces[leaf]),
+            "vorticity_vertices": rel(b.relVortVerts, a.relVortVerts),
+            "positions_vertices": rel(b.physVerts, a.physVerts)}
+    del a
+    stream = torch.cuda.current_stream()
+    st = b.state()
+    el = _timed_region(torch, stream, lambda: ctx.rk4_step(st, dt, omega, 1, flags=P.FP32C | P.TREECODE, eps=eps),
+                       steps, flush)
+    ctx.set_timing(True); ctx.timing()
+    ctx.rk4_step(st, dt, omega, 1, flags=P.FP32C | P.TREECODE, eps=eps)
+    torch.cuda.synchronize()
+    pair_ms, pair_n = ctx.timing(); ctx.set_timing(False)
+    ts = ctx.tree_stats()  # the last of the step's four evaluations
+    nv, nf, nl = b.physVerts.shape[0], b.physFaces.shape[0], int(leaf.sum())
+    peak = lane_ops / OPS_PER_PAIR
+    rate = ts["pairs"] / (pair_ms / pair_n * 1e-3)
+    return {
+        "rk4_steps_per_s": steps / (el * 1e-3), "ms_per_step": el / steps,
+        "params": {"degree": 8, "theta": 0.6, "leaf_points": 512},
+        "rel_l2_vs_fp32c_direct_after_steps": check_steps, "rel_l2_vs_fp32c_direct": errs,
+        "work_fraction_of_direct_pairs": ts["pairs"] / ((nv + nf) * nl),
+        "octree": {"depth": ts["depth"], "nodes": ts["nodes"], "far_clusters": ts["far_clusters"]},
+        "phase_ms_per_evaluation": {"octree_build": ts["build_ms"], "upward_pass": ts["upward_ms"],
+                                    "interaction_lists": ts["list_ms"], "pair_kernel": pair_ms / pair_n},
+        "pair_kernel": {"kernel": "treeFP32C<64,8,256,4>", "pairs_per_evaluation": ts["pairs"],
+                        "direct_pairs": ts["direct_pairs"], "proxy_pairs": ts["far_pairs"],
+                        "computed_pairs_per_s": rate, "frac_of_fma_peak": rate / peak},
+    }
+
+
 def run_large(args, rank, world, local_rank):
     """Config 5: icosahedral level 8 (655,362 vertices, 1,747,620 faces, 1,310,720 sources), RH54 + 8
     Gaussian vortices, eps = 0.01, RK4 steps, then the stream function at all targets."""
@@ -583,6 +645,7 @@ def run_large(args, rank, world, local_rank):
     s.init_vorticity(bve.rh54_gaussians(SEED_BASE + 5, 8), ctx, flags=P.FP32C, eps=eps)
     torch.cuda.synchronize()
     t_init = time.time() - t0
+    s0 = clone_sphere(bve, s) if not args.no_tree else None
     st = s.state()
     ctx.rk4_step(st, dt, 2 * math.pi, max(1, args.warmup), flags=P.FP32C, eps=eps)
     torch.cuda.synchronize()
@@ -608,6 +671,13 @@ def run_large(args, rank, world, local_rank):
     peak = lane_ops / OPS_PER_PAIR / 1e9
     fp64 = fp64_sample(ctx, s, dict(WORKLOAD, level=level, dt=dt), P, torch, np, (nv + nall) * nl,
                        el / args.steps, eps=eps)
+    tree = None
+    if s0 is not None:
+        tree = tree_leg(P, bve, torch, ctx, s0, dt, eps, args.steps, flush, lane_ops)
+        tree["speedup_vs_direct_fp32c"] = tree["rk4_steps_per_s"] / whole_job_rate(1, args.steps, el)
+        tree["speedup_vs_direct_fp64_gpu"] = (tree["rk4_steps_per_s"] / fp64["steps_per_s_extrapolated"]
+                                              if fp64 and fp64.get("steps_per_s_extrapolated") else None)
+        del s0
     out = {
         "metric": "pair-interactions/s", "value": world * 4 * pairs_alg * args.steps / (el * 1e-3),
         "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -623,7 +693,7 @@ def run_large(args, rank, world, local_rank):
                      "peak_source": "FP32 FMA-pipe probe (FFMA / FFMA2, the larger) / 13 lane-ops per pair",
                      "probes": probes, "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
                      "hbm": hbm_line(TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl), pair_ms / pair_n)},
-        "fp64_gpu": fp64, "init_s": t_init, "clocks": clocks,
+        "fp64_gpu": fp64, "init_s": t_init, "clocks": clocks, "treecode": tree,
     }
     if rank == 0:
         print(json.dumps(out), flush=True)

@@ -97,11 +97,15 @@ __global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__
   out[t] = s >= 0 ? inv[s] : -1;
 }
 
-// Centroid and radius of each target tile over its sane targets (masked parents that sit on a
-// leaf run away or become NaN, as in the reference; they do not widen the tile), and the tile's
-// range of self indices in key order.
+// Centroid and radius of each target tile over its vertices and leaf faces, and the tile's
+// range of self indices in key order.  Masked parent faces do not shape the tile: on the
+// icosahedral mesh a parent's centre is its middle child's, its velocity is singular in the
+// reference's formula, and after a step it runs away (its bounding sphere would then admit no
+// far field).  Parents are still evaluated with their tile's list; a cubed-sphere parent sits on
+// its children's shared corner, inside the tile.
 __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
-                                                       const int2* __restrict__ tiles,
+                                                       const int2* __restrict__ tiles, const int* __restrict__ perm,
+                                                       int64_t na, const uint8_t* __restrict__ mask,
                                                        const int* __restrict__ selfSorted, double4* __restrict__ geom,
                                                        int2* __restrict__ tileSelf) {
   __shared__ double sh[kBlock / 32];
@@ -113,7 +117,9 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
   for (int q = threadIdx.x; q < cnt; q += kBlock) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
-    if (sane(x, y, z)) { sx += x; sy += y; sz += z; sc += 1.0; }
+    const int id = perm[slot];
+    const bool shape = sane(x, y, z) && !(mask && id >= na && mask[id - na]);
+    if (shape) { sx += x; sy += y; sz += z; sc += 1.0; }
     const int s = selfSorted[slot];
     if (s >= 0) { smin = min(smin, s); smax = max(smax, s); }
   }
@@ -135,7 +141,9 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
   for (int q = threadIdx.x; q < cnt; q += kBlock) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
-    if (sane(x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
+    const int id = perm[slot];
+    if (sane(x, y, z) && !(mask && id >= na && mask[id - na]))
+      r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
   }
   r2 = blockMax<kBlock>(r2, sh);
   if (threadIdx.x == 0) {
@@ -457,7 +465,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   // 5. tiles
   double4* tgeom = grow<double4>(bTileGeom, ntiles, s);
   int2* tself = grow<int2>(bTileSelf, ntiles, s);
-  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, selfSorted, tgeom, tself);
+  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask,
+                                         selfSorted, tgeom, tself);
   // 6. interaction lists: lengths, offsets and launch order on the host, then the indices
   int64_t* lens = grow<int64_t>(bLen, ntiles, s);
   int64_t* fars = grow<int64_t>(bFar, ntiles, s);
