@@ -115,6 +115,8 @@ def parse():
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     ap.add_argument("--no-tree", action="store_true",
                     help="c2/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
+    ap.add_argument("--tree-only", action="store_true",
+                    help="c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
     return ap.parse_args()
 
 
@@ -588,17 +590,20 @@ def tree_leg(P, bve, torch, ctx, s0, dt, eps, steps, flush, lane_ops, check_step
     direct sum after `check_steps` RK4 steps, then RK4 steps/s over `steps` timed steps with the
     phase times, the gathered pair kernel's rate and its fraction of the FMA-pipe peak."""
     omega = 2 * math.pi
-    a, b = clone_sphere(bve, s0), clone_sphere(bve, s0)
+    b = clone_sphere(bve, s0)
     leaf = torch.from_numpy(s0.mesh["fmask"] == 0).to(s0.physVerts.device)
-    ctx.rk4_step(a.state(), dt, omega, check_steps, flags=P.FP32C, eps=eps)
-    ctx.rk4_step(b.state(), dt, omega, check_steps, flags=P.FP32C | P.TREECODE, eps=eps)
-    torch.cuda.synchronize()
-    rel = lambda x, y: (torch.linalg.norm(x - y) / torch.linalg.norm(y)).item()
-    errs = {"velocity_vertices": rel(b.velocityVerts, a.velocityVerts),
-            "velocity_leaves": rel(b.velocityFaces[leaf], a.velocityFaces[leaf]),
-            "vorticity_vertices": rel(b.relVortVerts, a.relVortVerts),
-            "positions_vertices": rel(b.physVerts, a.physVerts)}
-    del a
+    errs = None
+    if check_steps > 0:
+        a = clone_sphere(bve, s0)
+        ctx.rk4_step(a.state(), dt, omega, check_steps, flags=P.FP32C, eps=eps)
+        ctx.rk4_step(b.state(), dt, omega, check_steps, flags=P.FP32C | P.TREECODE, eps=eps)
+        torch.cuda.synchronize()
+        rel = lambda x, y: (torch.linalg.norm(x - y) / torch.linalg.norm(y)).item()
+        errs = {"velocity_vertices": rel(b.velocityVerts, a.velocityVerts),
+                "velocity_leaves": rel(b.velocityFaces[leaf], a.velocityFaces[leaf]),
+                "vorticity_vertices": rel(b.relVortVerts, a.relVortVerts),
+                "positions_vertices": rel(b.physVerts, a.physVerts)}
+        del a
     stream = torch.cuda.current_stream()
     st = b.state()
     el = _timed_region(torch, stream, lambda: ctx.rk4_step(st, dt, omega, 1, flags=P.FP32C | P.TREECODE, eps=eps),
@@ -645,6 +650,23 @@ def run_large(args, rank, world, local_rank):
     s.init_vorticity(bve.rh54_gaussians(SEED_BASE + 5, 8), ctx, flags=P.FP32C, eps=eps)
     torch.cuda.synchronize()
     t_init = time.time() - t0
+    if args.tree_only:
+        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+        lane_ops, probes = fma_peak(P, local_rank)
+        sampler = ClockSampler(gpu_uuid(local_rank))
+        ctx.rk4_step(clone_sphere(bve, s).state(), dt, 2 * math.pi, max(1, args.warmup),
+                     flags=P.FP32C | P.TREECODE, eps=eps)
+        tree = tree_leg(P, bve, torch, ctx, s, dt, eps, args.steps, flush, lane_ops, check_steps=0)
+        clocks = sampler.stop()
+        if rank == 0:
+            print(json.dumps({"metric": "RK4 steps/s (tree code)", "value": tree["rk4_steps_per_s"],
+                              "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+                              "higher_is_better": True, "dtype": "f32c", "data": "synthetic",
+                              "config": {"workload": f"icosahedral level 8, RH54 + 8 Gaussian vortices, eps {eps}, "
+                                                     f"dt {dt:g}; tree code only"},
+                              "treecode": tree, "probes": probes, "clocks": clocks}), flush=True)
+        ctx.close()
+        return
     s0 = clone_sphere(bve, s) if not args.no_tree else None
     st = s.state()
     ctx.rk4_step(st, dt, 2 * math.pi, max(1, args.warmup), flags=P.FP32C, eps=eps)

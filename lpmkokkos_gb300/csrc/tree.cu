@@ -169,22 +169,23 @@ Cheb chebFor(int n) {
   return c;
 }
 
-// Barycentric Lagrange basis at s of the nodes m + h t_a, a = 0..n.
-__device__ __forceinline__ void basis(double s, double m, double h, int n, const Cheb& C, double* L) {
-  const double u = (s - m) / h;  // in [-1, 1] for the sources of the chart
-  double den = 0.0;
+// Barycentric Lagrange basis at u in [-1, 1] (second form; forward stable at Chebyshev points,
+// Higham 2004), in FP32: the proxy charges are stored as floats, and the basis needs no more.
+// scale multiplies every value (the source weight for the xi factor, 1 for eta).
+__device__ __forceinline__ void basisF(float u, int n, const float* t, const float* w, float scale, float* L) {
+  float den = 0.f;
   int hit = -1;
   for (int a = 0; a <= n; ++a) {
-    const double d = u - C.t[a];
-    if (d == 0.0) hit = a;
-    L[a] = C.w[a] / d;
+    const float d = u - t[a];
+    if (d == 0.f) hit = a;
+    L[a] = w[a] / d;
     den += L[a];
   }
   if (hit >= 0) {
-    for (int a = 0; a <= n; ++a) L[a] = a == hit ? 1.0 : 0.0;
+    for (int a = 0; a <= n; ++a) L[a] = a == hit ? scale : 0.f;
     return;
   }
-  const double r = 1.0 / den;
+  const float r = scale / den;
   for (int a = 0; a <= n; ++a) L[a] *= r;
 }
 
@@ -197,7 +198,12 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
                                                      int* __restrict__ approx, float4* __restrict__ sp0,
                                                      float4* __restrict__ sp1) {
   __shared__ double sh[kUpThreads / 32];
-  __shared__ double sL[kUpThreads][2 * kMaxNodes1D];
+  __shared__ float sL[kUpThreads][2 * kMaxNodes1D];
+  __shared__ float sT[kMaxNodes1D], sBw[kMaxNodes1D];
+  if (threadIdx.x <= degree) {
+    sT[threadIdx.x] = (float)C.t[threadIdx.x];
+    sBw[threadIdx.x] = (float)C.w[threadIdx.x];
+  }
   const int g = blockIdx.x;
   const int2 pt = ptInds[g];
   const int n1 = degree + 1, P = n1 * n1;
@@ -232,7 +238,8 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
       const double d = x * ux + y * uy + z * uz;
       dmin = fmin(dmin, d);
       if (d > 0.0) {
-        const double xi = (x * e1x + y * e1y + z * e1z) / d, eta = (x * e2x + y * e2y + z * e2z) / d;
+        const double rd = 1.0 / d;
+        const double xi = (x * e1x + y * e1y + z * e1z) * rd, eta = (x * e2x + y * e2y + z * e2z) * rd;
         xmin = fmin(xmin, xi); xmax = fmax(xmax, xi); ymin = fmin(ymin, eta); ymax = fmax(ymax, eta);
       }
     }
@@ -251,6 +258,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   if (!valid) return;
   const double mx = 0.5 * (xmin + xmax), hx = 0.5 * (xmax - xmin);
   const double my = 0.5 * (ymin + ymax), hy = 0.5 * (ymax - ymin);
+  const double ihx = 1.0 / hx, ihy = 1.0 / hy;
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
   double q = 0.0;
@@ -258,16 +266,16 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
     const int k = c0 + t;
     if (k < k1) {
       const double x = pos[3 * k], y = pos[3 * k + 1], z = pos[3 * k + 2];
-      const double d = x * ux + y * uy + z * uz;
-      basis((x * e1x + y * e1y + z * e1z) / d, mx, hx, degree, C, &sL[t][0]);
-      basis((x * e2x + y * e2y + z * e2z) / d, my, hy, degree, C, &sL[t][n1]);
-      const double w = (double)sp0[k].w;
-      for (int a = 0; a <= degree; ++a) sL[t][a] *= w;  // w L_a(xi): one FMA per proxy below
+      const double rd = 1.0 / (x * ux + y * uy + z * uz);
+      const float uxi = (float)(((x * e1x + y * e1y + z * e1z) * rd - mx) * ihx);
+      const float ueta = (float)(((x * e2x + y * e2y + z * e2z) * rd - my) * ihy);
+      basisF(uxi, degree, sT, sBw, sp0[k].w, &sL[t][0]);  // w L_a(xi): one FMA per proxy below
+      basisF(ueta, degree, sT, sBw, 1.f, &sL[t][n1]);
     }
     __syncthreads();
-    if (t < P) {
+    if (t < P) {  // products of two floats are exact in FP64; the sum runs in FP64
       const int m = min(kUpThreads, k1 - c0);
-      for (int j = 0; j < m; ++j) q = fma(sL[j][ia], sL[j][n1 + ib], q);
+      for (int j = 0; j < m; ++j) q = fma((double)sL[j][ia], (double)sL[j][n1 + ib], q);
     }
     __syncthreads();
   }
