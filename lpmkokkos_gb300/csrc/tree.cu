@@ -26,7 +26,6 @@ constexpr int kBlock = 256;
 constexpr int kUpThreads = 128;
 constexpr int kMaxDegree = 10;            // (n+1)^2 <= 121 proxies: one thread per proxy charge
 constexpr int kMaxNodes1D = kMaxDegree + 1;
-constexpr int kStack = 96;                // DFS stack: <= 7 depth + 8 entries for depth <= 10
 // A chart covers sources within ~37 degrees of its centre direction: an octant (54.7 degrees)
 // stretches its gnomonic chart 3x at the edge and its degree-8 interpolant then errs by 1e-5.
 constexpr double kMinChartCos = 0.8;
@@ -194,9 +193,9 @@ __device__ __forceinline__ void basisF(float u, int n, const float* t, const flo
 // the proxy charges Q_ab (one thread per proxy, sources in index order) and the proxy records
 // at sp0/sp1[ns + g (n+1)^2 + ab].
 __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, const double* __restrict__ pos,
-                                                     int degree, const Cheb C, int ns, double4* __restrict__ geom,
-                                                     int* __restrict__ approx, float4* __restrict__ sp0,
-                                                     float4* __restrict__ sp1) {
+                                                     int degree, const Cheb C, int ns, int firstNode,
+                                                     double4* __restrict__ geom, int* __restrict__ approx,
+                                                     float4* __restrict__ sp0, float4* __restrict__ sp1) {
   __shared__ double sh[kUpThreads / 32];
   __shared__ float sL[kUpThreads][2 * kMaxNodes1D];
   __shared__ float sT[kMaxNodes1D], sBw[kMaxNodes1D];
@@ -207,8 +206,10 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   const int g = blockIdx.x;
   const int2 pt = ptInds[g];
   const int n1 = degree + 1, P = n1 * n1;
-  if (pt.y == 0) {
-    if (threadIdx.x == 0) { geom[g] = make_double4(0, 0, 0, -1.0); approx[g] = 0; }
+  if (pt.y == 0 || g < firstNode) {
+    // empty; or the root and the octants, whose sources span more than any chart allows (their
+    // geometry would only ever open them, so they are opened unconditionally: infinite radius)
+    if (threadIdx.x == 0) { geom[g] = make_double4(0, 0, 0, pt.y == 0 ? -1.0 : INFINITY); approx[g] = 0; }
     return;
   }
   const int k0 = pt.x, k1 = pt.x + pt.y;
@@ -261,7 +262,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   const double ihx = 1.0 / hx, ihy = 1.0 / hy;
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
-  double q = 0.0;
+  double q = 0.0;  // FP64 total of the per-chunk compensated FP32 sums
   for (int c0 = k0; c0 < k1; c0 += kUpThreads) {
     const int k = c0 + t;
     if (k < k1) {
@@ -273,9 +274,16 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
       basisF(ueta, degree, sT, sBw, 1.f, &sL[t][n1]);
     }
     __syncthreads();
-    if (t < P) {  // products of two floats are exact in FP64; the sum runs in FP64
+    if (t < P) {  // Kahan-compensated FP32 over the chunk (the FP32 pipe; FP64 is 1/64 of it)
       const int m = min(kUpThreads, k1 - c0);
-      for (int j = 0; j < m; ++j) q = fma((double)sL[j][ia], (double)sL[j][n1 + ib], q);
+      float h = 0.f, c = 0.f;
+      for (int j = 0; j < m; ++j) {
+        const float y = sL[j][ia] * sL[j][n1 + ib] - c;
+        const float tt = h + y;
+        c = (tt - h) - y;
+        h = tt;
+      }
+      q += (double)h - (double)c;
     }
     __syncthreads();
   }
@@ -296,75 +304,114 @@ struct Levels {
   int base[kOctreeMaxDepth + 2];
 };
 
-// Interaction lists, one warp per target tile (every lane walks the same tree; ranges are
-// written by the whole warp).  FILL = false: list length and far-field length per tile;
-// FILL = true: the flattened index list at listOff[tile], contiguous direct ranges merged.
+constexpr int kWarpStack = 4096;  // per-warp node stack: <= 256 entries per level for depth <= 10
+
+// Interaction lists, one warp per target tile, the tree walked 32 nodes at a time: each step
+// pops up to 32 stacked nodes (one per lane), tests them, places their kids on the stack and
+// their list entries in lane order (warp prefix sums), and writes each entry's index range with
+// the whole warp.  The order is a function of the data alone, so the lists are reproducible.
+// FILL = false: list length and far-field length per tile; FILL = true: the flattened index
+// list at listOff[tile], contiguous direct ranges merged.  A stack overflow (impossible for the
+// depths the tree code builds) sets *err instead of writing out of bounds.
 template <bool FILL>
-__global__ void __launch_bounds__(128) traverse(const double4* __restrict__ tileGeom, int ntiles,
-                                                const double4* __restrict__ geom, const int* __restrict__ approx,
-                                                const int2* __restrict__ ptInds, const int* __restrict__ kids,
-                                                Levels lv, int depth, double theta, int P, int ns,
-                                                int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
-                                                const int64_t* __restrict__ listOff, int* __restrict__ list) {
-  const int tile = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(32) traverse(const double4* __restrict__ tileGeom, int ntiles,
+                                               const double4* __restrict__ geom, const int* __restrict__ approx,
+                                               const int2* __restrict__ ptInds, const int* __restrict__ kids,
+                                               Levels lv, int depth, double theta, int P, int ns,
+                                               int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
+                                               const int64_t* __restrict__ listOff, int* __restrict__ list,
+                                               int* __restrict__ err) {
+  __shared__ int stack[kWarpStack];
+  const int tile = blockIdx.x;
+  const int lane = threadIdx.x;
   if (tile >= ntiles) return;
   const double4 tg = tileGeom[tile];
-  int stack[kStack];
-  int sp = 0;
-  stack[sp++] = 0;  // the root (level 0, global index 0)
+  if (lane == 0) stack[0] = 0;  // the root (level 0, global index 0)
+  __syncwarp();
+  int sp = 1;
   int64_t len = 0, far = 0;
   int64_t o = FILL ? listOff[tile] : 0;
   int rs = 0, rl = 0;  // pending direct range (FILL)
-  auto flush = [&]() {
-    for (int k = lane; k < rl; k += 32) list[o + k] = rs + k;
-    o += rl;
-    rl = 0;
-  };
-  auto direct = [&](int start, int count) {
-    len += count;
-    if (FILL) {
-      if (rl > 0 && rs + rl == start) {
-        rl += count;
-      } else {
-        flush();
-        rs = start;
-        rl = count;
+  while (sp > 0) {
+    const int n = min(32, sp);
+    const int b0 = sp - n;
+    const int g = lane < n ? stack[b0 + lane] : -1;
+    __syncwarp();
+    sp = b0;
+    int kind = 0;  // 0 nothing, 1 far, 2 direct, 3 open
+    int2 pt = make_int2(0, 0);
+    int lev = 0;
+    if (g >= 0) {
+      pt = ptInds[g];
+      if (pt.y > 0) {
+        const double4 ng = geom[g];
+        const double dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
+        const bool mac = (tg.w + ng.w) < theta * sqrt(dx * dx + dy * dy + dz * dz);
+        while (lev < depth && g >= lv.base[lev + 1]) ++lev;
+        if (mac && approx[g]) kind = 1;
+        else if (mac && pt.y <= P) kind = 2;      // well separated but smaller than its proxy set
+        else if (lev < depth) kind = 3;           // too close, or no valid chart: open the node
+        else kind = 2;                            // a leaf
       }
     }
-  };
-  while (sp > 0) {
-    const int g = stack[--sp];
-    const int2 pt = ptInds[g];
-    if (pt.y == 0) continue;
-    const double4 ng = geom[g];
-    const double dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
-    const double R = sqrt(dx * dx + dy * dy + dz * dz);
-    const bool mac = (tg.w + ng.w) < theta * R;
-    int lev = 0;
-    while (lev < depth && g >= lv.base[lev + 1]) ++lev;
-    if (mac && approx[g]) {
-      len += P;
-      far += P;
-      if (FILL) {
-        flush();
-        const int p0 = ns + g * P;
-        for (int k = lane; k < P; k += 32) list[o + k] = p0 + k;
-        o += P;
+    // kids of opened nodes onto the stack (lane order, ascending child order)
+    int nk = 0, kidv[8];
+    if (kind == 3)
+      for (int c = 0; c < 8; ++c) {
+        const int k = kids[8 * g + c];
+        if (k >= 0) kidv[nk++] = lv.base[lev + 1] + k;
       }
-    } else if (mac && pt.y <= P) {  // well separated but smaller than its proxy set
-      direct(pt.x, pt.y);
-    } else if (lev < depth) {  // too close, or no valid chart: open the node
-      for (int c = 7; c >= 0; --c) {
-        const int kid = kids[8 * g + c];
-        if (kid >= 0 && sp < kStack) stack[sp++] = lv.base[lev + 1] + kid;
+    int incl = nk;
+    for (int d = 1; d < 32; d <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, d);
+      if (lane >= d) incl += v;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    if (sp + total > kWarpStack) {  // cannot happen for depth <= 10; never write out of bounds
+      if (lane == 0) atomicExch(err, 1);
+      break;
+    }
+    for (int c = 0; c < nk; ++c) stack[sp + incl - nk + c] = kidv[c];
+    sp += total;
+    __syncwarp();
+    // list entries in lane order
+    const unsigned emit = __ballot_sync(0xffffffffu, kind == 1 || kind == 2);
+    unsigned m = emit;
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      const int kd = __shfl_sync(0xffffffffu, kind, src);
+      const int st = __shfl_sync(0xffffffffu, pt.x, src);
+      const int ct = __shfl_sync(0xffffffffu, pt.y, src);
+      const int gg = __shfl_sync(0xffffffffu, g, src);
+      if (kd == 1) {
+        len += P;
+        far += P;
+        if (FILL) {
+          for (int k = lane; k < rl; k += 32) list[o + k] = rs + k;
+          o += rl;
+          rl = 0;
+          const int p0 = ns + gg * P;
+          for (int k = lane; k < P; k += 32) list[o + k] = p0 + k;
+          o += P;
+        }
+      } else {
+        len += ct;
+        if (FILL) {
+          if (rl > 0 && rs + rl == st) {
+            rl += ct;
+          } else {
+            for (int k = lane; k < rl; k += 32) list[o + k] = rs + k;
+            o += rl;
+            rs = st;
+            rl = ct;
+          }
+        }
       }
-    } else {
-      direct(pt.x, pt.y);
     }
   }
   if (FILL) {
-    flush();
+    for (int k = lane; k < rl; k += 32) list[o + k] = rs + k;
   } else if (lane == 0) {
     lens[tile] = len;
     farLens[tile] = far;
@@ -458,8 +505,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     // 4. upward pass
     geom = grow<double4>(bGeom, nnodes, s);
     approx = grow<int>(bApprox, nnodes, s);
-    upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns, geom, approx,
-                                         tsp0, tsp1);
+    upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns,
+                                         depth >= 2 ? tree_.base[2] : nnodes, geom, approx, tsp0, tsp1);
     mark(2);
   } else {
     mark(1);
@@ -481,10 +528,11 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   Levels lv{};
   for (int l = 0; l <= tree_.depth; ++l) lv.base[l] = tree_.base[l];
   lv.base[tree_.depth + 1] = nnodes;
-  const unsigned tb = blocks((int64_t)ntiles * 32, 128);
+  int* terr = grow<int>(bErr, 1, s);
+  ck(cudaMemsetAsync(terr, 0, sizeof(int), s), "memset");
   if (ns > 0) {
-    traverse<false><<<tb, 128, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                       tp.theta, P, ns, lens, fars, nullptr, nullptr);
+    traverse<false><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
+                                          tp.theta, P, ns, lens, fars, nullptr, nullptr, terr);
   } else {
     ck(cudaMemsetAsync(lens, 0, sizeof(int64_t) * ntiles, s), "memset");
     ck(cudaMemsetAsync(fars, 0, sizeof(int64_t) * ntiles, s), "memset");
@@ -494,7 +542,10 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hFar_.resize(ntiles);
   ck(cudaMemcpyAsync(hLen_.data(), lens, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
   ck(cudaMemcpyAsync(hFar_.data(), fars, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
+  int herr = 0;
+  ck(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, s), "read-back");
   ck(cudaStreamSynchronize(s), "synchronise");
+  if (herr) fail(LPM_ERR_INTERNAL, "tree code: traversal stack overflow (octree depth %d)", tree_.depth);
   hOff_.assign((size_t)ntiles + 1, 0);
   for (int t = 0; t < ntiles; ++t) {
     hOff_[t + 1] = hOff_[t] + hLen_[t];
@@ -518,8 +569,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   ck(cudaMemcpyAsync(off, hOff_.data(), sizeof(int64_t) * (ntiles + 1), cudaMemcpyHostToDevice, s), "upload");
   ck(cudaMemcpyAsync(order, hOrder_.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, s), "upload");
   if (ns > 0)
-    traverse<true><<<tb, 128, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                      tp.theta, P, ns, nullptr, nullptr, off, list);
+    traverse<true><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
+                                         tp.theta, P, ns, nullptr, nullptr, off, list, terr);
   mark(4);
   // 7. the gathered pair kernel
   double* partial = grow<double>(bPartial, (size_t)nchunks * 5 * std::max(1, nslots), s);

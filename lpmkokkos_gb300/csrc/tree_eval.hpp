@@ -36,9 +36,9 @@ class TreeEval {
   Octree tree_;
   TreeStats stats_;
   Buf bPos, bSp0, bSp1, bInv, bSelf, bGeom, bApprox, bTileGeom, bTileSelf, bLen, bFar, bOff, bOrder, bList, bPartial,
-      bDev, bStage, bCounter;
+      bDev, bStage, bCounter, bErr;
   std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bTileSelf, &bLen,
-                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bStage, &bCounter};
+                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bStage, &bCounter, &bErr};
   SolveStage* stageDev_ = nullptr;
   // host sources of the last uploads (an evaluation synchronises before it rewrites them)
   TreeDev hDev_{};
