@@ -544,7 +544,8 @@ struct ShapeFn {
                 {(void*)pairFP32C<T, K, S, B, false, false, false>, (void*)pairFP32C<T, K, S, B, true, false, false>}}}
 // Register use of the RK4 velocity kernel (ptxas, sm_103a, paired arithmetic) sets the
 // resident CTAs per SM: 128x4 unbounded 154 regs -> 3/SM, min-blocks 4: 124 -> 4/SM;
-// 128x6 min-blocks 3: 163 -> 3/SM; 128x8 233 -> 2/SM; 64x8 min-blocks 4: 233 -> 4/SM;
+// 128x6 min-blocks 3: 163 -> 3/SM; 128x8 233 -> 2/SM; 64x8 min-blocks 4: 233 -> 4/SM; 32x8 min-blocks 8
+// (the tree code's shape) -> 8/SM;
 // 256x4 min-blocks 2: 125 -> 2/SM.  None of these spills.
 const ShapeFn kShapes[] = {
   LPM_SHAPE(128, 4, 256, 1),
@@ -553,6 +554,7 @@ const ShapeFn kShapes[] = {
   LPM_SHAPE(128, 8, 256, 1),
   LPM_SHAPE(64, 8, 256, 4),
   LPM_SHAPE(256, 4, 256, 2),
+  LPM_SHAPE(32, 8, 256, 8),
 };
 #undef LPM_SHAPE
 

@@ -65,8 +65,8 @@ struct TreeStats {
 
 cudaError_t launchTreePair(const PairShape& shape, bool psi, bool precise, bool rcpApprox, const TreeDev* dev,
                            int nitems, int* counter, int grid, cudaStream_t s);
-// The tree kernel's launch shape: 64 threads x 8 targets (512-target tiles), 4 CTAs per SM.
-inline constexpr PairShape kTreeShape{64, 8, 256, 4};
+// The tree kernel's launch shape: 32 threads x 8 targets (256-target tiles), 8 CTAs per SM.
+inline constexpr PairShape kTreeShape{32, 8, 256, 8};
 bool treePairShapeSupported(const PairShape& shape);
 
 }  // namespace lpm
