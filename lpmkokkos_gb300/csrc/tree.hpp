@@ -14,7 +14,8 @@
 // ~R away (the usual tree-code regime).
 //
 // Clusters are the nodes of the reference's Morton octree (octree.hpp) over the stage positions
-// of the sources; target batches are the pair kernel's target tiles.  A tile takes a cluster
+// of the sources; target batches ("tiles") are runs of at most 256 target slots of the plan's
+// Morton order that stay inside one level-3 Morton cell.  A tile takes a cluster
 // as far field when (r_tile + r_node) < theta |c_tile - c_node| and the node has more than
 // (n+1)^2 sources and a valid chart; otherwise it recurses into the kids, or takes the node's
 // sources directly at a leaf or when the node is accepted but too small to approximate.
