@@ -986,6 +986,8 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     B.shape = shapeFor(ctx, B.prec, false);
     B.rk4 = true;
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
+    if (flags & LPM_BVE_TREECODE)
+      fail(LPM_ERR_NOT_SUPPORTED, "ensemble_create: the tree code runs single solves (lpm_bve_rk4_step) only");
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
     auto ioOf = [](const lpm_bve_state* st) {

@@ -874,6 +874,8 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     const unsigned flags = opts ? opts->flags : LPM_BVE_FP32C;
     const double eps = opts ? opts->eps : 0.0;
     if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "server: eps must be finite and >= 0");
+    if (flags & LPM_BVE_TREECODE)
+      fail(LPM_ERR_NOT_SUPPORTED, "server: the tree code runs single solves (lpm_bve_rk4_step) only");
     S->flags = flags;
     S->prec = (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64;
     S->shape = S->prec == Precision::FP32C ? kDefaultFP32C : kFP64Shape;

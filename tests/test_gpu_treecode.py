@@ -151,3 +151,50 @@ def test_invalid(ctx):
         ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED | P.TREECODE)
     assert "FP32C" in str(e.value)
     ctx.set_treecode()
+
+
+def test_regularised_kernel(tctx):
+    """eps > 0 (the regularised kernel of the benchmark spec; absent from the reference)."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 0, 6)
+    rf, pf = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED | P.PSI, eps=0.01)
+    tf, qf = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE | P.PSI, eps=0.01)
+    torch.cuda.synchronize()
+    assert max(_rel(tf[leaf], rf[leaf]), _rel(qf[leaf], pf[leaf])) <= TOL
+
+
+@pytest.mark.parametrize("extra", [P.SKIP_MASKED_TARGETS, P.RENORM, P.RK4_FIX_QUIRK])
+def test_rk4_flags_with_tree(tctx, extra):
+    """The RK4 options combine with the tree code as with the direct sum (3 steps, icos L5)."""
+    ctx = tctx
+    a, _, leaf = _sphere(ctx, 0, 5)
+    b, _, _ = _sphere(ctx, 0, 5)
+    ctx.rk4_step(a.state(), 0.005, OMEGA, 3, flags=P.FP64 | extra)
+    ctx.rk4_step(b.state(), 0.005, OMEGA, 3, flags=P.FP32C | P.TREECODE | extra)
+    torch.cuda.synchronize()
+    errs = [_rel(b.physVerts, a.physVerts), _rel(b.velocityVerts, a.velocityVerts),
+            _rel(b.physFaces[leaf], a.physFaces[leaf]), _rel(b.relVortFaces[leaf], a.relVortFaces[leaf])]
+    assert max(errs) <= TOL, errs
+
+
+def test_cubed_sphere_rk4_including_parents(tctx):
+    """On the cubed sphere a masked parent sits on its children's shared corner (not on a leaf):
+    its velocity is finite, and the tree code must get it right too."""
+    ctx = tctx
+    a, _, _ = _sphere(ctx, 1, 5)
+    b, _, _ = _sphere(ctx, 1, 5)
+    ctx.rk4_step(a.state(), 0.005, OMEGA, 3, flags=P.FP64)
+    ctx.rk4_step(b.state(), 0.005, OMEGA, 3, flags=P.FP32C | P.TREECODE)
+    torch.cuda.synchronize()
+    assert torch.isfinite(a.velocityFaces).all()
+    errs = [_rel(b.velocityFaces, a.velocityFaces), _rel(b.physFaces, a.physFaces), _rel(b.velocityVerts, a.velocityVerts)]
+    assert max(errs) <= TOL, errs
+
+
+def test_ensemble_and_server_refuse_the_tree_code(ctx):
+    s, _, _ = _sphere(ctx, 0, 2)
+    with pytest.raises(RuntimeError) as e:
+        ctx.ensemble([s.state()], flags=P.FP32C | P.TREECODE)
+    assert "single solves" in str(e.value)
+    with pytest.raises(RuntimeError):
+        bve.Server(flags=P.FP32C | P.TREECODE)
