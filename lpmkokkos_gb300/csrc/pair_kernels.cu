@@ -412,6 +412,7 @@ template <int NTH, int K, int ST, int MINB, bool PSI, bool PRECISE, bool NEWTON>
 __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict__ dev, int nitems,
                                                  int* __restrict__ counter) {
   static_assert(ST % kSub == 0, "source tile must be a multiple of the sub-block");
+  static_assert(ST % NTH == 0, "each thread stages ST / NTH sources");
   constexpr int P = K / 2;
   __shared__ float4 sXY[ST];
   __shared__ float4 sZW[ST];
@@ -452,16 +453,34 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
     const int64_t l1 = part + 1 == S.nchunks ? tl : tl * (part + 1) / S.nchunks / kSub * kSub;
     const int64_t off = S.listOff[tile] + l0;
     const int64_t len = l1 - l0;
+    // The list indices of a block are loaded one block ahead (into registers, while the
+    // previous block computes), so staging waits only for the records they point to.
+    constexpr int kPer = ST / NTH;
+    int nextId[kPer];
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int64_t q = threadIdx.x + i * NTH;
+      nextId[i] = q < len ? S.list[off + q] : INT_MIN;
+    }
     for (int64_t b0 = 0; b0 < len; b0 += ST) {
       const int nsrc = (int)min((int64_t)ST, (len - b0 + kSub - 1) / kSub * kSub);
       int hit = 0;
-      for (int j = threadIdx.x; j < nsrc; j += NTH) {
-        const bool live = b0 + j < len;
-        const int id = live ? S.list[off + b0 + j] : INT_MIN;
-        hit |= live && id >= ts.x && id <= ts.y;
-        stageSource<K, PRECISE>(j, live, live ? S.sp0[id] : float4{}, live ? S.sp1[id] : float4{}, tt, sXY, sZW, sD,
-                                sLXY, sLZ);
-        sId[j] = id;
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int j = threadIdx.x + i * NTH;
+        if (j < nsrc) {
+          const int id = nextId[i];
+          const bool live = id != INT_MIN;
+          hit |= live && id >= ts.x && id <= ts.y;
+          stageSource<K, PRECISE>(j, live, live ? S.sp0[id] : float4{}, live ? S.sp1[id] : float4{}, tt, sXY, sZW,
+                                  sD, sLXY, sLZ);
+          sId[j] = id;
+        }
+      }
+#pragma unroll
+      for (int i = 0; i < kPer; ++i) {
+        const int64_t q = b0 + ST + threadIdx.x + i * NTH;
+        nextId[i] = q < len ? S.list[off + q] : INT_MIN;
       }
       if (__syncthreads_or(hit))
         fp32cTile<K, PSI, true, PRECISE, NEWTON, true>(T, nsrc, 0, sId, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
