@@ -198,3 +198,30 @@ def test_ensemble_and_server_refuse_the_tree_code(ctx):
     assert "single solves" in str(e.value)
     with pytest.raises(RuntimeError):
         bve.Server(flags=P.FP32C | P.TREECODE)
+
+
+@pytest.mark.parametrize("seed,level", [(0, 0), (0, 1), (1, 0), (1, 2)])
+def test_tiny_meshes(tctx, seed, level):
+    """Octree depth 1, clusters smaller than a proxy set: everything is summed directly."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, seed, level)
+    r, _ = ctx.velocity(s.physVerts, *src, flags=P.FP64)
+    t, _ = ctx.velocity(s.physVerts, *src, flags=P.FP32C | P.MESH_TARGETS | P.TREECODE)
+    torch.cuda.synchronize()
+    assert _rel(t, r) <= TOL
+    assert ctx.tree_stats()["far_pairs"] == 0
+
+
+def test_no_sources_and_ragged_targets(tctx):
+    """Every face masked: no sources, zero velocity; 1,001 distinct targets (not a tile multiple)."""
+    ctx = tctx
+    s, _, _ = _sphere(ctx, 0, 3)
+    all_masked = torch.ones_like(s.faces_mask)
+    x = torch.nn.functional.normalize(torch.randn(1001, 3, dtype=torch.float64, device="cuda"), dim=1)
+    t, _ = ctx.velocity(x, s.physFaces, s.relVortFaces, s.faces_area, all_masked, flags=P.FP32C | P.TREECODE)
+    torch.cuda.synchronize()
+    assert torch.equal(t, torch.zeros_like(t))
+    r, _ = ctx.velocity(x, s.physFaces, s.relVortFaces, s.faces_area, s.faces_mask, flags=P.FP64)
+    t, _ = ctx.velocity(x, s.physFaces, s.relVortFaces, s.faces_area, s.faces_mask, flags=P.FP32C | P.TREECODE)
+    torch.cuda.synchronize()
+    assert _rel(t, r) <= TOL
