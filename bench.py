@@ -114,7 +114,7 @@ def parse():
     ap.add_argument("--kinds", choices=["both", "icos"], default="both", help="c4: mesh seeds")
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     ap.add_argument("--no-tree", action="store_true",
-                    help="c2/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
+                    help="c2/c3/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
     ap.add_argument("--tree-only", action="store_true",
                     help="c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
     return ap.parse_args()
@@ -538,6 +538,7 @@ def run_ensemble(args, rank, world, local_rank):
     t_init = time.time() - t0
     dts = [courant_dt(sk, lv) for sk, lv in picks]
     oms = [2 * math.pi] * len(picks)
+    initial = [clone_sphere(bve, s) for s in spheres] if not args.no_tree else None
     ens = ctx.ensemble([s.state() for s in spheres], flags=P.FP32C)
     info = ens.info()
     ens.step(dts, oms, max(1, args.warmup))
@@ -569,9 +570,23 @@ def run_ensemble(args, rank, world, local_rank):
         "gpu_launches": 13 * args.steps, "init_s": t_init, "all_vertex_velocities_finite": finite,
         "clocks": clocks,
     }
+    ens.close()
+    if initial is not None:
+        # the same ensemble with the tree code (each solve its own octree and lists; an
+        # approximation outside the reference, beside the direct numbers), from the initial states
+        tens = ctx.ensemble([s.state() for s in initial], flags=P.FP32C | P.TREECODE)
+        tens.step(dts, oms, 1)
+        torch.cuda.synchronize()
+        el_t = max_over_ranks(_timed_region(torch, stream, lambda: tens.step(dts, oms, 1), args.steps, flush), world, dev)
+        tens.close()
+        out["treecode"] = {"ensemble_rk4_steps_per_s": whole_job_rate(world, args.steps, el_t),
+                           "ms_per_step": el_t / args.steps,
+                           "speedup_vs_direct_ensemble": whole_job_rate(world, args.steps, el_t) / steps_per_s,
+                           "params": {"degree": 8, "theta": 0.6, "leaf_points": 512},
+                           "note": "one tree-code evaluation per solve, launched one solve after another"}
+        del initial
     if rank == 0:
         print(json.dumps(out), flush=True)
-    ens.close()
     ctx.close()
 
 

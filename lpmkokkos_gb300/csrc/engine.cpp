@@ -351,9 +351,20 @@ void refreshTables(Batch& B, cudaStream_t s) {
 // One evaluation of the direct sums for every solve of the batch.
 void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s) {
   LPM_CUDA(launchPrep(B.stageDev, B.prepMap, B.nPrepBlocks, prepStage, B.prec, B.counter, s));
-  if (B.treeMode) {  // tree code: octree, lists and the gathered pair kernel, then the same epilogue
-    B.tree->evaluate(*B.solves[0], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
-    LPM_CUDA(launchEpilogue(B.tree->stageDev(), B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
+  if (B.treeMode) {  // tree code: per solve octree, lists and gathered pair kernel; one epilogue
+    const size_t n = B.solves.size();
+    B.treeStageHost.resize(n);
+    for (size_t m = 0; m < n; ++m) {
+      TreeEval& T = *B.trees[m];
+      T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
+      SolveStage st = B.solves[m]->stage;
+      st.partial = T.partial();
+      st.nchunks = T.nchunks();
+      B.treeStageHost[m] = st;
+    }
+    // (the next evaluation's first octree build synchronises before this host table changes)
+    LPM_CUDA(cudaMemcpyAsync(B.treeStageDev, B.treeStageHost.data(), n * sizeof(SolveStage), cudaMemcpyHostToDevice, s));
+    LPM_CUDA(launchEpilogue(B.treeStageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
     return;
   }
   cudaEvent_t e0 = nullptr, e1 = nullptr;
@@ -549,13 +560,16 @@ void bindIO(Batch& B, size_t m, const ParticleIO& io, double dt, double omega, c
   (void)s;
 }
 
-// Switches a single-solve batch between the direct sum and the tree code for this call.
+// Switches a batch (one solve or an ensemble) between the direct sum and the tree code.
 void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree) {
   B.treeMode = tree;
   if (!tree) return;
-  if (!B.tree) B.tree = std::make_shared<TreeEval>();
+  if (B.trees.empty()) {
+    for (size_t m = 0; m < B.solves.size(); ++m) B.trees.push_back(std::make_shared<TreeEval>());
+    B.treeStageDev = B.mem.alloc<SolveStage>(B.solves.size());
+  }
   B.treeParams = ctx->treeParams;
-  ctx->lastTree = B.tree;
+  ctx->lastTree = B.trees.back();
 }
 
 }  // namespace
@@ -983,11 +997,11 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     E->batch = std::make_unique<Batch>();
     Batch& B = *E->batch;
     B.prec = precOf(flags);
-    B.shape = shapeFor(ctx, B.prec, false);
+    const bool tree = flags & LPM_BVE_TREECODE;
+    if (tree && B.prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "ensemble_create: the tree code needs LPM_BVE_FP32C");
+    B.shape = shapeFor(ctx, B.prec, tree);
     B.rk4 = true;
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
-    if (flags & LPM_BVE_TREECODE)
-      fail(LPM_ERR_NOT_SUPPORTED, "ensemble_create: the tree code runs single solves (lpm_bve_rk4_step) only");
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
     auto ioOf = [](const lpm_bve_state* st) {
@@ -1003,7 +1017,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
       io.barea = st->farea;
       return io;
     };
-    if (B.prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0) {
+    if (!tree && B.prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0) {
       int big = 0;  // tune on the solve with the most pairs: it dominates the launch
       for (int m = 1; m < nsolves; ++m)
         if ((states[m].nverts + states[m].nfaces) * states[m].nfaces >
@@ -1069,7 +1083,9 @@ int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* O
     if (changed) refreshTables(B, s);
     const bool quirk = !(E->flags & LPM_BVE_RK4_FIX_QUIRK);
     const bool renorm = E->flags & LPM_BVE_RENORM;
-    if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer) {
+    const bool tree = E->flags & LPM_BVE_TREECODE;
+    useTree(ctx, B, tree);
+    if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // tree steps read sizes back: no capture
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
       B.timer = nullptr;

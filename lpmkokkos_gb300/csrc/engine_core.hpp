@@ -204,8 +204,11 @@ struct Batch {
   int4* prepMap = nullptr;
   int4* slotMap = nullptr;
   int* counter = nullptr;
-  // tree code (LPM_BVE_TREECODE): evaluation state, created on first use
-  std::shared_ptr<TreeEval> tree;
+  // tree code (LPM_BVE_TREECODE): one evaluation state per solve, created on first use, and the
+  // epilogue's stage table pointing at their partial sums
+  std::vector<std::shared_ptr<TreeEval>> trees;
+  SolveStage* treeStageDev = nullptr;
+  std::vector<SolveStage> treeStageHost;
   bool treeMode = false;
   TreeParams treeParams;
   int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)

@@ -593,13 +593,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hd.eps2 = Pl.eps2;
   TreeDev* dd = grow<TreeDev>(bDev, 1, s);
   ck(cudaMemcpyAsync(dd, &hd, sizeof(hd), cudaMemcpyHostToDevice, s), "upload");
-  SolveStage& st = hStage_;
-  st = Pl.stage;
-  st.partial = partial;
-  st.nchunks = nchunks;
-  SolveStage* sd = grow<SolveStage>(bStage, 1, s);
-  ck(cudaMemcpyAsync(sd, &st, sizeof(st), cudaMemcpyHostToDevice, s), "upload");
-  stageDev_ = sd;
+  partial_ = partial;
+  nchunks_ = nchunks;
   int* counter = grow<int>(bCounter, 1, s);
   ck(cudaMemsetAsync(counter, 0, sizeof(int), s), "memset");
   cudaEvent_t e0 = nullptr, e1 = nullptr;

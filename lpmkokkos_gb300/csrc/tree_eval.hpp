@@ -9,13 +9,14 @@ namespace lpm {
 
 class TreeEval {
  public:
-  // One evaluation for the single solve P: builds the source octree over the stage positions
-  // the prep kernel wrote, the proxies and the per-tile index lists, and runs the gathered pair
-  // kernel into this object's one-chunk partial buffer.  The epilogue then reads stageDev().
+  // One evaluation for the solve P: builds the source octree over the stage positions the prep
+  // kernel wrote, the proxies and the per-tile index lists, and runs the gathered pair kernel
+  // into this object's partial buffer ([nchunks()][ncomp][slot]), which the epilogue then sums.
   // Synchronises `s` (octree level sizes, list lengths).
   void evaluate(SolvePlan& P, const TreeParams& tp, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
                 int slots, PairTimer* timer, cudaStream_t s);
-  const SolveStage* stageDev() const { return stageDev_; }
+  double* partial() const { return partial_; }
+  int nchunks() const { return nchunks_; }
   const TreeStats& stats() const { return stats_; }
 
  private:
@@ -36,13 +37,13 @@ class TreeEval {
   Octree tree_;
   TreeStats stats_;
   Buf bPos, bSp0, bSp1, bInv, bSelf, bGeom, bApprox, bTileGeom, bTileSelf, bLen, bFar, bOff, bOrder, bList, bPartial,
-      bDev, bStage, bCounter, bErr;
+      bDev, bCounter, bErr;
   std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bTileSelf, &bLen,
-                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bStage, &bCounter, &bErr};
-  SolveStage* stageDev_ = nullptr;
-  // host sources of the last uploads (an evaluation synchronises before it rewrites them)
+                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bCounter, &bErr};
+  double* partial_ = nullptr;
+  int nchunks_ = 1;
+  // host source of the last upload (an evaluation synchronises before it rewrites it)
   TreeDev hDev_{};
-  SolveStage hStage_{};
   std::vector<int64_t> hLen_, hFar_, hOff_;
   std::vector<int2> hTiles_;
   const int2* tilesOf_ = nullptr;  // plan whose tile sizes hTiles_ holds

@@ -191,11 +191,27 @@ def test_cubed_sphere_rk4_including_parents(tctx):
     assert max(errs) <= TOL, errs
 
 
-def test_ensemble_and_server_refuse_the_tree_code(ctx):
-    s, _, _ = _sphere(ctx, 0, 2)
-    with pytest.raises(RuntimeError) as e:
-        ctx.ensemble([s.state()], flags=P.FP32C | P.TREECODE)
-    assert "single solves" in str(e.value)
+def test_ensemble_with_the_tree_code(tctx):
+    """An ensemble of uneven solves with the tree code: each solve bit-identical to its own
+    single-solve tree-code run, and within the bar of its FP64 direct run."""
+    ctx = tctx
+    specs = [(0, 4), (1, 5), (0, 6)]
+    ens = [_sphere(ctx, *sp) for sp in specs]
+    alone = [_sphere(ctx, *sp) for sp in specs]
+    ref = [_sphere(ctx, *sp) for sp in specs]
+    e = ctx.ensemble([t[0].state() for t in ens], flags=P.FP32C | P.TREECODE)
+    e.step([0.005] * 3, [OMEGA] * 3, 2)
+    for (a, _, leaf), (r, _, _) in zip(alone, ref):
+        ctx.rk4_step(a.state(), 0.005, OMEGA, 2, flags=P.FP32C | P.TREECODE)
+        ctx.rk4_step(r.state(), 0.005, OMEGA, 2, flags=P.FP64)
+    torch.cuda.synchronize()
+    for (x, _, leaf), (a, _, _), (r, _, _) in zip(ens, alone, ref):
+        assert torch.equal(x.physVerts, a.physVerts) and torch.equal(x.velocityFaces[leaf], a.velocityFaces[leaf])
+        assert _rel(x.velocityVerts, r.velocityVerts) <= TOL and _rel(x.physFaces[leaf], r.physFaces[leaf]) <= TOL
+    e.close()
+
+
+def test_server_refuses_the_tree_code(ctx):
     with pytest.raises(RuntimeError):
         bve.Server(flags=P.FP32C | P.TREECODE)
 
