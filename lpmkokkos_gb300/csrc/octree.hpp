@@ -66,11 +66,4 @@ class Octree {
   bool registered_ = false;
 };
 
-// Level of global node index g.
-inline int octreeLevelOf(const Octree& t, int64_t g) {
-  int l = 0;
-  while (l < t.depth && g >= t.base[l + 1]) ++l;
-  return l;
-}
-
 }  // namespace lpm

@@ -11,8 +11,6 @@
 
 #include "tree_eval.hpp"
 
-#include <cub/cub.cuh>
-
 #include <algorithm>
 #include <cfloat>
 #include <climits>

@@ -151,3 +151,23 @@ def test_face_connectivity_reproduces_areas(native, seed):
     leaf = m["fmask"] == 0  # a divided parent passes its area to its children (area 0)
     assert np.abs(area[leaf] - m["farea"][leaf]).max() <= 1e-12 * m["farea"].max()
     assert (m["farea"][~leaf] == 0).all()
+
+
+def test_octree_and_tree_code_argument_checks(native):
+    """The octree and tree-code entry points reject bad arguments before touching the device."""
+    from lpmkokkos_gb300 import _lib as L
+    lib = L.lib()
+    h = ctypes.c_void_p()
+    x = (ctypes.c_double * 12)()
+    ptr = ctypes.cast(x, ctypes.c_void_p).value
+    for args in ((None, 3, 1, 4, 3), (ptr, 3, 1, 0, 3), (ptr, 3, 1, 4, 0), (ptr, 3, 1, 4, 11), (ptr, -3, 1, 4, 3)):
+        xp, si, sc, n, d = args
+        assert lib.lpm_octree_build(xp, si, sc, n, d, 1, ctypes.byref(h), None) == L.LPM_ERR_INVALID_ARGUMENT
+        assert not h.value
+    assert lib.lpm_octree_build(ptr, 3, 1, 4, 3, 1, None, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_octree_info(None, None, None, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_octree_arrays(None, *([None] * 8)) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_octree_destroy(None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_bve_ctx_set_treecode(None, 8, 0.6, 512) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_bve_ctx_tree_stats(None, None, None, None, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_sphere_tangency(ptr, 3, 1, ptr, 3, 1, -1, ptr, None) == L.LPM_ERR_INVALID_ARGUMENT
