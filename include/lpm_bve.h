@@ -197,8 +197,10 @@ int lpm_sphere_tangency(const double* x, int64_t x_si, int64_t x_sc, const doubl
 /* Tree-code parameters of the context (LPM_BVE_TREECODE): interpolation degree n per chart
  * axis (2..10; (n+1)^2 proxies per cluster), opening parameter theta (0 < theta < 1: a cluster
  * is far from a target tile when r_tile + r_cluster < theta * distance), and the mean sources per
- * octree leaf that set the octree depth.  Defaults 8, 0.6, 512. */
-int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points);
+ * octree leaf that set the octree depth, and min_pairs: a solve whose evaluation has fewer target x
+ * source pairs keeps the direct sum (the tree's fixed costs exceed its savings below ~1e9 pairs; in
+ * an ensemble the small solves share one direct launch).  Defaults 8, 0.6, 512, 1e9. */
+int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points, double min_pairs);
 /* Statistics of the context's last tree-code evaluation: octree depth and node count, far-field
  * clusters taken over all tiles, target x source pairs evaluated (direct + proxy), and -- with
  * timing enabled (lpm_bve_ctx_set_timing) -- phase_ms[3] = milliseconds of the octree build, the

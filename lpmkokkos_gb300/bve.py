@@ -312,9 +312,10 @@ class Context:
         t, k, s, b = shape if shape else (0, 0, 0, 0)
         L.check(self._lib.lpm_bve_ctx_set_shape(self.handle, t, k, s, b), self.handle)
 
-    def set_treecode(self, degree: int = 8, theta: float = 0.6, leaf_points: int = 512):
-        """Tree-code parameters for calls with flags & TREECODE (include/lpm_bve.h)."""
-        L.check(self._lib.lpm_bve_ctx_set_treecode(self.handle, degree, theta, leaf_points), self.handle)
+    def set_treecode(self, degree: int = 8, theta: float = 0.6, leaf_points: int = 512, min_pairs: float = 1e9):
+        """Tree-code parameters for calls with flags & TREECODE (include/lpm_bve.h); solves with
+        fewer than min_pairs target x source pairs keep the direct sum."""
+        L.check(self._lib.lpm_bve_ctx_set_treecode(self.handle, degree, theta, leaf_points, min_pairs), self.handle)
 
     def tree_stats(self) -> dict:
         """Octree depth and nodes, far clusters and pairs of the last tree-code evaluation."""

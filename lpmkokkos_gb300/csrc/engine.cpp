@@ -354,12 +354,20 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
   if (B.treeMode) {  // tree code: per solve octree, lists and gathered pair kernel; one epilogue
     const size_t n = B.solves.size();
     B.treeStageHost.resize(n);
+    // solves below the size threshold: one persistent direct launch over their work items
+    if (B.nDirectItems > 0)
+      LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.directItems, B.nDirectItems,
+                          B.counter, std::min(B.nDirectItems, B.slots), s));
     for (size_t m = 0; m < n; ++m) {
       TreeEval& T = *B.trees[m];
-      T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
       SolveStage st = B.solves[m]->stage;
-      st.partial = T.partial();
-      st.nchunks = T.nchunks();
+      if (B.treeDirect[m]) {
+        T.markDirect(*B.solves[m]);
+      } else {
+        T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
+        st.partial = T.partial();
+        st.nchunks = T.nchunks();
+      }
       B.treeStageHost[m] = st;
     }
     // (the next evaluation's first octree build synchronises before this host table changes)
@@ -561,7 +569,7 @@ void bindIO(Batch& B, size_t m, const ParticleIO& io, double dt, double omega, c
 }
 
 // Switches a batch (one solve or an ensemble) between the direct sum and the tree code.
-void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree) {
+void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree, cudaStream_t s) {
   B.treeMode = tree;
   if (!tree) return;
   if (B.trees.empty()) {
@@ -570,6 +578,34 @@ void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree) {
   }
   B.treeParams = ctx->treeParams;
   ctx->lastTree = B.trees.back();
+  if (B.treeDirectFor == B.treeParams.minPairs) return;
+  // solves too small for the tree code keep the direct sum: their work items, longest first
+  B.treeDirectFor = B.treeParams.minPairs;
+  B.treeDirect.assign(B.solves.size(), 0);
+  std::vector<WorkItem> items;
+  for (size_t m = 0; m < B.solves.size(); ++m) {
+    const SolvePlan& P = *B.solves[m];
+    if ((double)P.nslots * P.ns >= B.treeParams.minPairs) continue;
+    B.treeDirect[m] = 1;
+    for (int t = 0; t < P.ntiles; ++t)
+      for (int c = 0; c < P.nchunks; ++c) {
+        WorkItem w{};
+        w.solve = (int)m;
+        w.tile = t;
+        w.s0 = std::min(P.ns, c * P.chunkLen);
+        w.s1 = std::min(P.ns, (c + 1) * P.chunkLen);
+        w.chunk = c;
+        items.push_back(w);
+      }
+  }
+  std::stable_sort(items.begin(), items.end(), [&](const WorkItem& a, const WorkItem& b) {
+    return (int64_t)(a.s1 - a.s0) * B.solves[a.solve]->tileSize > (int64_t)(b.s1 - b.s0) * B.solves[b.solve]->tileSize;
+  });
+  B.directMem.release();
+  B.nDirectItems = (int)items.size();
+  B.directItems = B.nDirectItems ? B.directMem.alloc<WorkItem>(items.size()) : nullptr;
+  upload(B.directItems, items, s);
+  LPM_CUDA(cudaStreamSynchronize(s));  // the host vector goes out of scope
 }
 
 }  // namespace
@@ -712,15 +748,16 @@ int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches
   return LPM_OK;
 }
 
-int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points) {
+int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points, double min_pairs) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
-  if (degree < 2 || degree > 10 || !(theta > 0.0 && theta < 1.0) || leaf_points < 1) {
-    ctx->err = "set_treecode: degree 2..10, theta in (0, 1), leaf_points >= 1";
+  if (degree < 2 || degree > 10 || !(theta > 0.0 && theta < 1.0) || leaf_points < 1 || !(min_pairs >= 0.0)) {
+    ctx->err = "set_treecode: degree 2..10, theta in (0, 1), leaf_points >= 1, min_pairs >= 0";
     return LPM_ERR_INVALID_ARGUMENT;
   }
   ctx->treeParams.degree = degree;
   ctx->treeParams.theta = theta;
   ctx->treeParams.leafPoints = leaf_points;
+  ctx->treeParams.minPairs = min_pairs;
   return LPM_OK;
 }
 
@@ -803,7 +840,7 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     // Distinct targets are arbitrary points unless the caller says they are mesh points.
     B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
-    useTree(ctx, B, tree);
+    useTree(ctx, B, tree, s);
     bool changed = false;
     bindIO(B, 0, io, 0.0, 0.0, s, changed);
     if (changed) refreshTables(B, s);
@@ -865,7 +902,7 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const bool renorm = flags & LPM_BVE_RENORM;
     const bool rcp = flags & LPM_BVE_RCP_APPROX;
     B.rcpApprox = rcp;
-    useTree(ctx, B, tree);
+    useTree(ctx, B, tree, s);
     if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // the tree build reads sizes back: no capture
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
@@ -1084,7 +1121,7 @@ int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* O
     const bool quirk = !(E->flags & LPM_BVE_RK4_FIX_QUIRK);
     const bool renorm = E->flags & LPM_BVE_RENORM;
     const bool tree = E->flags & LPM_BVE_TREECODE;
-    useTree(ctx, B, tree);
+    useTree(ctx, B, tree, s);
     if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // tree steps read sizes back: no capture
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);

@@ -209,6 +209,11 @@ struct Batch {
   std::vector<std::shared_ptr<TreeEval>> trees;
   SolveStage* treeStageDev = nullptr;
   std::vector<SolveStage> treeStageHost;
+  std::vector<char> treeDirect;        // per solve: below TreeParams::minPairs, direct sum
+  double treeDirectFor = -1.0;         // minPairs the subset below was built for
+  WorkItem* directItems = nullptr;     // pair-kernel items of the direct solves
+  int nDirectItems = 0;
+  DeviceArena directMem;
   bool treeMode = false;
   TreeParams treeParams;
   int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)

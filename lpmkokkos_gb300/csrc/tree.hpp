@@ -36,6 +36,7 @@ struct TreeParams {
   int degree = 8;          // interpolation degree n per chart axis: (n+1)^2 proxies per cluster
   double theta = 0.6;      // opening parameter of the acceptance test
   int leafPoints = 512;    // target mean sources per octree leaf (sets the octree depth)
+  double minPairs = 1e9;   // solves with fewer target x source pairs use the direct sum
 };
 
 // Device description of one tree evaluation for the gathered pair kernel.

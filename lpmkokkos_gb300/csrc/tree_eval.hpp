@@ -15,6 +15,11 @@ class TreeEval {
   // Synchronises `s` (octree level sizes, list lengths).
   void evaluate(SolvePlan& P, const TreeParams& tp, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
                 int slots, PairTimer* timer, cudaStream_t s);
+  // Records that this solve's evaluation used the direct sum (smaller than TreeParams::minPairs).
+  void markDirect(const SolvePlan& P) {
+    stats_ = TreeStats{};
+    stats_.pairs = stats_.directPairs = (double)P.nslots * P.ns;
+  }
   double* partial() const { return partial_; }
   int nchunks() const { return nchunks_; }
   const TreeStats& stats() const { return stats_; }

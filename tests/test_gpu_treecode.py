@@ -35,7 +35,7 @@ def _sphere(ctx, seed, level):
 
 @pytest.fixture
 def tctx(ctx):
-    ctx.set_treecode()  # defaults
+    ctx.set_treecode(min_pairs=0)  # default parameters, the tree code at every size
     yield ctx
     ctx.set_treecode()
 
@@ -75,7 +75,7 @@ def test_all_direct_limit(tctx):
     within FP32C rounding."""
     ctx = tctx
     s, src, leaf = _sphere(ctx, 1, 4)
-    ctx.set_treecode(8, 0.01, 512)
+    ctx.set_treecode(8, 0.01, 512, 0)
     t, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
     r, _ = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED)
     torch.cuda.synchronize()
@@ -143,7 +143,7 @@ def test_level8_against_fp32c_direct(tctx):
 
 
 def test_invalid(ctx):
-    for args in ((1, 0.6, 512), (11, 0.6, 512), (8, 0.0, 512), (8, 1.0, 512), (8, 0.6, 0)):
+    for args in ((1, 0.6, 512), (11, 0.6, 512), (8, 0.0, 512), (8, 1.0, 512), (8, 0.6, 0), (8, 0.6, 512, -1.0)):
         with pytest.raises(RuntimeError):
             ctx.set_treecode(*args)
     s, src, _ = _sphere(ctx, 0, 2)
@@ -241,3 +241,26 @@ def test_no_sources_and_ragged_targets(tctx):
     t, _ = ctx.velocity(x, s.physFaces, s.relVortFaces, s.faces_area, s.faces_mask, flags=P.FP32C | P.TREECODE)
     torch.cuda.synchronize()
     assert _rel(t, r) <= TOL
+
+
+def test_size_threshold_and_hybrid_ensemble(ctx):
+    """Below min_pairs a solve keeps the direct sum: a TREECODE call on icosahedral level 5
+    (7.7e8 pairs < 1e9) equals the direct FP32C sum of a plan with the tree's launch shape, and in an
+    ensemble the small solves share one direct launch while the large one takes the tree code --
+    every solve bit-identical to its own single-solve TREECODE run."""
+    ctx.set_treecode()  # min_pairs 1e9
+    specs = [(0, 4), (1, 5), (0, 5), (0, 6)]
+    ens = [_sphere(ctx, *sp) for sp in specs]
+    alone = [_sphere(ctx, *sp) for sp in specs]
+    e = ctx.ensemble([t[0].state() for t in ens], flags=P.FP32C | P.TREECODE)
+    e.step([0.005] * 4, [OMEGA] * 4, 2)
+    kinds = []
+    for a, _, _ in alone:
+        ctx.rk4_step(a.state(), 0.005, OMEGA, 2, flags=P.FP32C | P.TREECODE)
+        torch.cuda.synchronize()
+        kinds.append(ctx.tree_stats()["far_pairs"] > 0)
+    torch.cuda.synchronize()
+    assert kinds == [False, False, False, True], kinds
+    for (x, _, leaf), (a, _, _) in zip(ens, alone):
+        assert torch.equal(x.physVerts, a.physVerts) and torch.equal(x.velocityFaces[leaf], a.velocityFaces[leaf])
+    e.close()

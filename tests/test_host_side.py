@@ -168,6 +168,6 @@ def test_octree_and_tree_code_argument_checks(native):
     assert lib.lpm_octree_info(None, None, None, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_octree_arrays(None, *([None] * 8)) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_octree_destroy(None) == L.LPM_ERR_INVALID_ARGUMENT
-    assert lib.lpm_bve_ctx_set_treecode(None, 8, 0.6, 512) == L.LPM_ERR_INVALID_ARGUMENT
+    assert lib.lpm_bve_ctx_set_treecode(None, 8, 0.6, 512, 0.0) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_bve_ctx_tree_stats(None, None, None, None, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_sphere_tangency(ptr, 3, 1, ptr, 3, 1, -1, ptr, None) == L.LPM_ERR_INVALID_ARGUMENT
