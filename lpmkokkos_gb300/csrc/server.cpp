@@ -208,7 +208,13 @@ struct lpm_bve_server {
   std::vector<double> latencies;
   std::map<std::tuple<int, int, int>, std::shared_ptr<const MeshHost>> meshes;  // prep thread only
   std::deque<std::tuple<int, int, int>> meshOrder;
-  std::thread prepT, gpuT;
+  // tree code (LPM_BVE_TREECODE): requests of at least minPairs pairs per evaluation go to the
+  // tree thread, which runs them one at a time through the single-solve path on its own stream
+  bool tree = false;
+  double treeMinPairs = 1e9;
+  std::deque<Req*> treeQueue;  // under mu
+  std::condition_variable cvTree;
+  std::thread prepT, gpuT, treeT;
 };
 
 namespace lpm {
@@ -581,6 +587,118 @@ std::map<int, int> shareSlots(const std::map<int, SizeClass>& classes, int slots
   return grid;
 }
 
+// The tree thread: each request it is handed runs alone through the library's single-solve path
+// (lpm_bve_velocity / lpm_bve_rk4_step with LPM_BVE_TREECODE) on this thread's context and
+// stream -- device initial vorticity as on the gpu thread, the initial velocity, the steps, the
+// copy back -- so its result depends on nothing but the request.  Its kernels share the GPU
+// with the size classes' persistent grids (they take the slots the classes leave).
+void treeRequest(lpm_bve_server* S, lpm_bve_ctx* ctx, cudaStream_t ts, Req* r) {
+  const MeshHost& M = *r->mesh;
+  r->nv = M.nv;
+  r->nf = M.nf;
+  const Layout L(M.nv, M.nf);
+  DeviceArena mem;
+  mem.streamOrdered(ts, ts, S->pool);
+  char* dev = mem.alloc<char>(L.bytes);
+  LPM_CUDA(cudaMemcpyAsync(dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, ts));
+  double* d = reinterpret_cast<double*>(dev);
+  auto check = [&](int rc) {
+    if (rc != LPM_OK) fail(rc, "%s", lpm_bve_last_error(ctx));
+  };
+  if (!S->hostIc)
+    for (const auto& part : {std::make_pair(L.vx, L.vzeta), std::make_pair(L.fx, L.fzeta)}) {
+      const int64_t n = part.first == L.vx ? M.nv : M.nf;
+      check(lpm_ic_rh54_gaussians_device(d + part.first, n, 3, 1, r->gc.data(), r->ga.data(), r->r.n_gaussians,
+                                         r->r.gauss_width, d + part.second, (lpm_stream_t)ts));
+    }
+  const uint8_t* mask = reinterpret_cast<const uint8_t*>(dev + L.maskByte);
+  {
+    std::lock_guard<std::mutex> lk(S->mu);
+    r->state = LPM_REQ_RUNNING;
+    r->tStart = Clock::now();
+    r->pairsPerEval = (double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl;
+    S->st.pairs += r->pairsPerEval;
+  }
+  const unsigned fl = S->flags;  // FP32C | TREECODE and the RK4 options
+  lpm_points tv{d + L.vx, M.nv, 3, 1};
+  lpm_sources src{{d + L.fx, M.nf, 3, 1}, d + L.fzeta, d + L.farea, mask};
+  check(lpm_bve_velocity(ctx, &tv, &src, d + L.vvel, 3, 1, nullptr, LPM_BVE_FP32C | LPM_BVE_MESH_TARGETS | LPM_BVE_TREECODE,
+                         S->eps, (lpm_stream_t)ts));
+  check(lpm_bve_velocity(ctx, nullptr, &src, d + L.fvel, 3, 1, nullptr,
+                         LPM_BVE_FP32C | LPM_BVE_COLLOCATED | LPM_BVE_TREECODE | (fl & LPM_BVE_SKIP_MASKED_TARGETS),
+                         S->eps, (lpm_stream_t)ts));
+  lpm_bve_state st{};
+  st.nverts = M.nv;
+  st.nfaces = M.nf;
+  st.vx = d + L.vx; st.vx_stride_i = 3; st.vx_stride_c = 1;
+  st.vzeta = d + L.vzeta;
+  st.vvel = d + L.vvel; st.vvel_stride_i = 3; st.vvel_stride_c = 1;
+  st.fx = d + L.fx; st.fx_stride_i = 3; st.fx_stride_c = 1;
+  st.fzeta = d + L.fzeta;
+  st.fvel = d + L.fvel; st.fvel_stride_i = 3; st.fvel_stride_c = 1;
+  st.farea = d + L.farea;
+  st.fmask = mask;
+  check(lpm_bve_rk4_step(ctx, &st, r->r.dt, r->r.omega, r->r.nsteps, fl, S->eps, (lpm_stream_t)ts));
+  check(lpm_bve_plan_invalidate(ctx));  // the next request's arrays reuse this memory
+  LPM_CUDA(cudaMemcpyAsync(r->host, dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, ts));
+  mem.release();
+  LPM_CUDA(cudaStreamSynchronize(ts));
+  std::lock_guard<std::mutex> lk(S->mu);
+  if (r->state != LPM_REQ_RUNNING) return;
+  r->state = LPM_REQ_DONE;
+  r->tDone = Clock::now();
+  S->reserved -= r->est;
+  S->inflight -= 1;
+  S->st.completed += 1;
+  S->st.solve_steps += r->r.nsteps;
+  S->latencies.push_back(seconds(r->tSubmit, r->tDone));
+  S->cvDone.notify_all();
+  S->cvPrep.notify_all();
+}
+
+void treeLoop(lpm_bve_server* S) {
+  cudaSetDevice(S->dev.device);
+  lpm_bve_ctx* ctx = nullptr;
+  cudaStream_t ts = nullptr;
+  std::string setupErr;
+  lpm_bve_opts o{S->dev.device, 0, 0};
+  if (lpm_bve_ctx_create(&ctx, &o) != LPM_OK || lpm_bve_ctx_set_treecode(ctx, 8, 0.6, 512, 0.0) != LPM_OK ||
+      cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking) != cudaSuccess)
+    setupErr = "tree thread: no context or stream";
+  for (;;) {
+    Req* r = nullptr;
+    {
+      std::unique_lock<std::mutex> lk(S->mu);
+      S->cvTree.wait(lk, [&] { return S->stop || !S->treeQueue.empty(); });
+      if (S->stop) {
+        for (Req* q : S->treeQueue) failLocked(S, q, "server destroyed before the request ran");
+        S->treeQueue.clear();
+        break;
+      }
+      r = S->treeQueue.front();
+      S->treeQueue.pop_front();
+    }
+    try {
+      if (!setupErr.empty()) fail(LPM_ERR_INTERNAL, "%s", setupErr.c_str());
+      treeRequest(S, ctx, ts, r);
+    } catch (const Error& e) {
+      if (ts) cudaStreamSynchronize(ts);
+      std::lock_guard<std::mutex> lk(S->mu);
+      failLocked(S, r, "tree code: " + e.msg);
+    } catch (const std::exception& e) {
+      if (ts) cudaStreamSynchronize(ts);
+      std::lock_guard<std::mutex> lk(S->mu);
+      failLocked(S, r, "tree code: " + fromStd(e).msg);
+    }
+    r->mesh.reset();
+  }
+  if (ts) {
+    cudaStreamSynchronize(ts);
+    cudaStreamDestroy(ts);
+  }
+  if (ctx) lpm_bve_ctx_destroy(ctx);
+}
+
 void gpuLoop(lpm_bve_server* S) {
   cudaSetDevice(S->dev.device);
   std::map<int, SizeClass> classes;  // key: size class
@@ -629,6 +747,13 @@ void gpuLoop(lpm_bve_server* S) {
         failLocked(S, r, msg);
       };
       for (Req* r : joiners) {
+        if (S->tree && (double)(r->mesh->nv + (S->skip ? r->mesh->nl : r->mesh->nf)) * (double)r->mesh->nl >=
+                           S->treeMinPairs) {
+          std::lock_guard<std::mutex> lk(S->mu);  // large enough for the tree code: the tree thread
+          S->treeQueue.push_back(r);
+          S->cvTree.notify_one();
+          continue;
+        }
         try {
           setupSolve(S, r);
           ok.push_back(r);
@@ -874,8 +999,9 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     const unsigned flags = opts ? opts->flags : LPM_BVE_FP32C;
     const double eps = opts ? opts->eps : 0.0;
     if (!(eps >= 0.0) || !std::isfinite(eps)) fail(LPM_ERR_INVALID_ARGUMENT, "server: eps must be finite and >= 0");
-    if (flags & LPM_BVE_TREECODE)
-      fail(LPM_ERR_NOT_SUPPORTED, "server: the tree code runs single solves (lpm_bve_rk4_step) only");
+    if ((flags & LPM_BVE_TREECODE) && !(flags & LPM_BVE_FP32C))
+      fail(LPM_ERR_NOT_SUPPORTED, "server: the tree code needs LPM_BVE_FP32C");
+    S->tree = flags & LPM_BVE_TREECODE;
     S->flags = flags;
     S->prec = (flags & LPM_BVE_FP32C) ? Precision::FP32C : Precision::FP64;
     S->shape = S->prec == Precision::FP32C ? kDefaultFP32C : kFP64Shape;
@@ -915,6 +1041,7 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
   try {
     raw->prepT = std::thread(prepLoop, raw);
     raw->gpuT = std::thread(gpuLoop, raw);
+    if (raw->tree) raw->treeT = std::thread(treeLoop, raw);
   } catch (const std::exception& e) {  // no thread: stop and join the one that started
     std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.what());
     lpm_bve_server_destroy(raw);
@@ -1159,9 +1286,11 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
     S->stop = true;
   }
   S->cvPrep.notify_all();
+  S->cvTree.notify_all();
   wakeGpu(S);
   if (S->prepT.joinable()) S->prepT.join();
   if (S->gpuT.joinable()) S->gpuT.join();
+  if (S->treeT.joinable()) S->treeT.join();
   cudaSetDevice(S->dev.device);
   for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);

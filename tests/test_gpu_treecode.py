@@ -211,9 +211,33 @@ def test_ensemble_with_the_tree_code(tctx):
     e.close()
 
 
-def test_server_refuses_the_tree_code(ctx):
-    with pytest.raises(RuntimeError):
-        bve.Server(flags=P.FP32C | P.TREECODE)
+def test_server_with_the_tree_code(ctx):
+    """A server created with LPM_BVE_TREECODE: the icosahedral level-6 request (1.2e10 pairs per
+    evaluation, above min_pairs) runs on the tree thread, the small ones in the batched direct
+    classes.  Every result equals the same request's result alone, bit for bit, and the tree
+    request is within the bar of an FP64 single solve."""
+    big = (0, 6, 901)
+    small = [(0, 3, 902), (1, 4, 903), (1, 3, 904)]
+
+    def run(specs):
+        with bve.Server(0, flags=P.FP32C | P.TREECODE, host_ic=True) as srv:
+            ids = [srv.submit(sk, lv, 0.0025, 3, ic_seed=seed, n_gaussians=3, gauss_width=0.1)
+                   for sk, lv, seed in specs]
+            for i in ids:
+                assert srv.wait(i, 300.0)
+            return [srv.result(i) for i in ids]
+
+    mix = run([small[0], big, small[1], small[2]])
+    alone = run([big]) + run(small)
+    for got, want in zip([mix[1], mix[0], mix[2], mix[3]], alone):
+        for k in ("vx", "vvel", "fx", "fvel", "vzeta", "fzeta"):
+            assert np.array_equal(got[k], want[k], equal_nan=True), k
+    s = bve.BVESphere(0, 6)
+    s.init_vorticity(bve.rh54_gaussians(901, 3, 0.1), ctx, flags=P.FP64)
+    ctx.rk4_step(s.state(), 0.0025, OMEGA, 3, flags=P.FP64)
+    torch.cuda.synchronize()
+    ref = s.velocityVerts.cpu().numpy()
+    assert np.linalg.norm(mix[1]["vvel"] - ref) <= TOL * np.linalg.norm(ref)
 
 
 @pytest.mark.parametrize("seed,level", [(0, 0), (0, 1), (1, 0), (1, 2)])
