@@ -115,6 +115,9 @@ def parse():
     ap.add_argument("--autotune", action="store_true", help="let the library time launch shapes first")
     ap.add_argument("--no-tree", action="store_true",
                     help="c2/c3/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
+    ap.add_argument("--tree", action="store_true",
+                    help="c4: a server with LPM_BVE_TREECODE (requests of >= 1e9 pairs per evaluation run on "
+                         "its tree-code thread)")
     ap.add_argument("--tree-only", action="store_true",
                     help="c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
     return ap.parse_args()
@@ -785,7 +788,8 @@ def run_server(args, rank, world, local_rank):
     arrivals = np.cumsum(gaps) - gaps[0]
     specs = [dict(seed=int(k), level=int(lv), dt=courant_dt(int(k), int(lv)), nsteps=args.req_steps,
                   ic_seed=SEED_BASE + 4 + i) for i, (k, lv) in enumerate(zip(kinds, lvls))]
-    srv = bve.Server(local_rank, flags=P.FP32C)
+    sflags = P.FP32C | (P.TREECODE if args.tree else 0)
+    srv = bve.Server(local_rank, flags=sflags)
     # warm-up: one zero-step request per mesh (fills the host mesh/plan cache, loads kernels)
     meshes = sorted({(s["seed"], s["level"]) for s in specs})
     warm = [srv.submit(seed=k, level=lv, dt=0.01, nsteps=0) for k, lv in meshes]
@@ -827,7 +831,7 @@ def run_server(args, rank, world, local_rank):
     mixed = [srv.result(ids[i]) for i in check]
     srv.close()
     same = True
-    with bve.Server(local_rank, flags=P.FP32C) as alone:
+    with bve.Server(local_rank, flags=sflags) as alone:
         for i, got in zip(check, mixed):
             rid = alone.submit(**specs[i])
             assert alone.wait(rid, 600.0)
@@ -861,7 +865,7 @@ def run_server(args, rank, world, local_rank):
         "config": {"workload": f"{n} requests, Poisson arrivals at {rate:.4g}/s, {kinds_desc} levels "
                                f"{lo}-{hi} (weights {', '.join(f'{v:.3g}' for v in weights)}), "
                                f"{args.req_steps} RK4 steps each, dt at the level-4 Courant number, FP32C "
-                               f"(seed {SEED_BASE + 4})",
+                               f"(seed {SEED_BASE + 4})" + ("; tree-code server" if args.tree else ""),
                    "levels": {str(lv): int((lvls == lv).sum()) for lv in levels},
                    "expected_service_s": exp_service, "offered_utilisation": rate * exp_service},
         "latency_s": {"p50": nearest(0.5), "p99": nearest(0.99), "max": float(lat.max()),
