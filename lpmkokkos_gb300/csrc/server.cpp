@@ -19,6 +19,10 @@
 //              queued behind a burst of steps, or a new request, wakes it.
 // A host function queued on a request's lane behind its copy-back marks it done, returns its
 // budget reservation and wakes waiters and the admission loop.
+// With LPM_BVE_TREECODE a third thread, tree, takes the requests of at least 1e9 pairs per
+// evaluation from the gpu thread and runs them one at a time through the library's single-solve
+// tree-code path on its own context and stream (the tree code reads sizes back between kernels,
+// so it cannot live in the classes' captured steps).
 // A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
 // summation order depend on nothing but its own mesh and the launch shape, fixed per server.
 
