@@ -19,9 +19,9 @@
 //              queued behind a burst of steps, or a new request, wakes it.
 // A host function queued on a request's lane behind its copy-back marks it done, returns its
 // budget reservation and wakes waiters and the admission loop.
-// With LPM_BVE_TREECODE a third thread, tree, takes the requests of at least 1e9 pairs per
-// evaluation from the gpu thread and runs them one at a time through the library's single-solve
-// tree-code path on its own context and stream (the tree code reads sizes back between kernels,
+// With LPM_BVE_TREECODE two more threads, tree, take the requests of at least 1e9 pairs per
+// evaluation from the gpu thread and run them (one each at a time) through the library's
+// single-solve tree-code path on their own contexts and streams (the tree code reads sizes back between kernels,
 // so it cannot live in the classes' captured steps).
 // A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
 // summation order depend on nothing but its own mesh and the launch shape, fixed per server.
@@ -218,7 +218,8 @@ struct lpm_bve_server {
   double treeMinPairs = 1e9;
   std::deque<Req*> treeQueue;  // under mu
   std::condition_variable cvTree;
-  std::thread prepT, gpuT, treeT;
+  std::thread prepT, gpuT;
+  std::vector<std::thread> treeT;
 };
 
 namespace lpm {
@@ -1045,7 +1046,10 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
   try {
     raw->prepT = std::thread(prepLoop, raw);
     raw->gpuT = std::thread(gpuLoop, raw);
-    if (raw->tree) raw->treeT = std::thread(treeLoop, raw);
+    // two tree threads: a large request need not wait for another's whole run, only share its
+    // kernels (each thread has its own context and stream)
+    if (raw->tree)
+      for (int k = 0; k < 2; ++k) raw->treeT.emplace_back(treeLoop, raw);
   } catch (const std::exception& e) {  // no thread: stop and join the one that started
     std::fprintf(stderr, "lpm_bve_server_create: %s\n", e.what());
     lpm_bve_server_destroy(raw);
@@ -1294,7 +1298,8 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
   wakeGpu(S);
   if (S->prepT.joinable()) S->prepT.join();
   if (S->gpuT.joinable()) S->gpuT.join();
-  if (S->treeT.joinable()) S->treeT.join();
+  for (auto& t : S->treeT)
+    if (t.joinable()) t.join();
   cudaSetDevice(S->dev.device);
   for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);
