@@ -406,8 +406,8 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
 // The tree code's gathered pair kernel: persistent CTAs take target tiles (longest index
 // lists first); each tile walks its flattened list of sorted-source and proxy indices
 // (tree.hpp), staging up to ST gathered records at a time.  Only the last block of a list is
-// padded (to the sub-block of 64).  The self-pair check runs on blocks that hold a source of
-// the tile's own self range.  One FP64 partial chunk per target.
+// padded (to the sub-block of 64).  The self-pair check runs only on blocks that hold the source
+// of one of the tile's own targets.  One FP64 partial chunk per target.
 template <int NTH, int K, int ST, int MINB, bool PSI, bool PRECISE, bool NEWTON>
 __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict__ dev, int nitems,
                                                  int* __restrict__ counter) {
@@ -446,7 +446,6 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
       hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
       hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
     }
-    const int2 ts = S.tileSelf[tile];
     // part `part` of the tile's list: [l0, l1), cut at multiples of the sub-block
     const int64_t tl = S.listOff[tile + 1] - S.listOff[tile];
     const int64_t l0 = tl * part / S.nchunks / kSub * kSub;
@@ -471,7 +470,10 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
         if (j < nsrc) {
           const int id = nextId[i];
           const bool live = id != INT_MIN;
-          hit |= live && id >= ts.x && id <= ts.y;
+          if (live && id < S.ns) {  // a source of one of this tile's own targets: check self pairs
+            const int sl = S.srcSlot[id];
+            hit |= sl >= tile0 && sl < tile0 + tcount;
+          }
           stageSource<K, PRECISE>(j, live, live ? S.sp0[id] : float4{}, live ? S.sp1[id] : float4{}, tt, sXY, sZW,
                                   sD, sLXY, sLZ);
           sId[j] = id;

@@ -54,17 +54,6 @@ __device__ __forceinline__ double blockMax(double v, double* sh) {
   for (int w = 0; w < NT / 32; ++w) t = fmax(t, sh[w]);
   return t;
 }
-template <int NT>
-__device__ __forceinline__ int blockMinI(int v, int* sh) {
-  for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_down_sync(0xffffffffu, v, o));
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
-  __syncthreads();
-  int t = INT_MAX;
-  for (int w = 0; w < NT / 32; ++w) t = min(t, sh[w]);
-  return t;
-}
-
 __global__ void srcPositions(const float4* __restrict__ sp0, const float4* __restrict__ sp1, int ns,
                              double* __restrict__ pos) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -76,13 +65,15 @@ __global__ void srcPositions(const float4* __restrict__ sp0, const float4* __res
 }
 
 __global__ void gatherSources(const int* __restrict__ orig, const float4* __restrict__ sp0,
-                              const float4* __restrict__ sp1, int ns, float4* __restrict__ tsp0,
-                              float4* __restrict__ tsp1, int* __restrict__ inv) {
+                              const float4* __restrict__ sp1, const int* __restrict__ srcSlot, int ns,
+                              float4* __restrict__ tsp0, float4* __restrict__ tsp1, int* __restrict__ inv,
+                              int* __restrict__ tslot) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= ns) return;
   const int o = orig[k];
   tsp0[k] = sp0[o];
   tsp1[k] = sp1[o];
+  tslot[k] = srcSlot[o];
   inv[o] = k;
 }
 
@@ -94,43 +85,34 @@ __global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__
   out[t] = s >= 0 ? inv[s] : -1;
 }
 
-// Centroid and radius of each target tile over its vertices and leaf faces, and the tile's
-// range of self indices in key order.  Masked parent faces do not shape the tile: on the
-// icosahedral mesh a parent's centre is its middle child's, its velocity is singular in the
-// reference's formula, and after a step it runs away (its bounding sphere would then admit no
-// far field).  Parents are still evaluated with their tile's list; a cubed-sphere parent sits on
-// its children's shared corner, inside the tile.
+// Centroid and radius of each target tile over its vertices and leaf faces.  Masked parent
+// faces do not shape the tile: on the icosahedral mesh a parent's centre is its middle child's,
+// its velocity is singular in the reference's formula, and after a step it runs away (its
+// bounding sphere would then admit no far field).  Parents are still evaluated with their tile's
+// list; a cubed-sphere parent sits on its children's shared corner, inside the tile.
 __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
                                                        const int2* __restrict__ tiles, const int* __restrict__ perm,
                                                        int64_t na, const uint8_t* __restrict__ mask,
-                                                       const int* __restrict__ selfSorted, double4* __restrict__ geom,
-                                                       int2* __restrict__ tileSelf) {
+                                                       double4* __restrict__ geom) {
   __shared__ double sh[kBlock / 32];
-  __shared__ int shi[kBlock / 32];
   const int2 tr = tiles[blockIdx.x];
   const int t0 = tr.x, cnt = tr.y;
+  auto shapes = [&](int slot, double x, double y, double z) {
+    const int id = perm[slot];
+    return sane(x, y, z) && !(mask && id >= na && mask[id - na]);
+  };
   double sx = 0, sy = 0, sz = 0, sc = 0;
-  int smin = INT_MAX, smax = INT_MIN;
   for (int q = threadIdx.x; q < cnt; q += kBlock) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
-    const int id = perm[slot];
-    const bool shape = sane(x, y, z) && !(mask && id >= na && mask[id - na]);
-    if (shape) { sx += x; sy += y; sz += z; sc += 1.0; }
-    const int s = selfSorted[slot];
-    if (s >= 0) { smin = min(smin, s); smax = max(smax, s); }
+    if (shapes(slot, x, y, z)) { sx += x; sy += y; sz += z; sc += 1.0; }
   }
   sx = blockSum<kBlock>(sx, sh);
   sy = blockSum<kBlock>(sy, sh);
   sz = blockSum<kBlock>(sz, sh);
   sc = blockSum<kBlock>(sc, sh);
-  smin = blockMinI<kBlock>(smin, shi);
-  smax = -blockMinI<kBlock>(smax == INT_MIN ? INT_MAX : -smax, shi);
   if (sc == 0.0) {
-    if (threadIdx.x == 0) {
-      geom[blockIdx.x] = make_double4(0, 0, 0, INFINITY);
-      tileSelf[blockIdx.x] = make_int2(smin, smin == INT_MAX ? -1 : smax);
-    }
+    if (threadIdx.x == 0) geom[blockIdx.x] = make_double4(0, 0, 0, INFINITY);
     return;
   }
   const double cx = sx / sc, cy = sy / sc, cz = sz / sc;
@@ -138,15 +120,10 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
   for (int q = threadIdx.x; q < cnt; q += kBlock) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
-    const int id = perm[slot];
-    if (sane(x, y, z) && !(mask && id >= na && mask[id - na]))
-      r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
+    if (shapes(slot, x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
   }
   r2 = blockMax<kBlock>(r2, sh);
-  if (threadIdx.x == 0) {
-    geom[blockIdx.x] = make_double4(cx, cy, cz, sqrt(r2));
-    tileSelf[blockIdx.x] = make_int2(smin, smin == INT_MAX ? -1 : smax);
-  }
+  if (threadIdx.x == 0) geom[blockIdx.x] = make_double4(cx, cy, cz, sqrt(r2));
 }
 
 // Chebyshev points of the second kind t_a = cos(pi a / n) and their barycentric weights.
@@ -477,6 +454,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   mark(0);
 
   const int* selfSorted = nullptr;
+  int* tslot = nullptr;
   int nnodes = 0;
   float4* tsp0 = nullptr;
   float4* tsp1 = nullptr;
@@ -496,7 +474,9 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     tsp0 = grow<float4>(bSp0, nrec, s);
     tsp1 = grow<float4>(bSp1, nrec, s);
     int* inv = grow<int>(bInv, ns, s);
-    gatherSources<<<blocks(ns), kBlock, 0, s>>>(tree_.origIds, Pl.stage.sp0, Pl.stage.sp1, ns, tsp0, tsp1, inv);
+    tslot = grow<int>(bSlot, ns, s);
+    gatherSources<<<blocks(ns), kBlock, 0, s>>>(tree_.origIds, Pl.stage.sp0, Pl.stage.sp1, Pl.stage.srcSlot, ns, tsp0,
+                                                tsp1, inv, tslot);
     int* ss = grow<int>(bSelf, nslots, s);
     sortedSelf<<<blocks(nslots), kBlock, 0, s>>>(Pl.dev.self, inv, nslots, ss);
     selfSorted = ss;
@@ -514,12 +494,11 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     selfSorted = ss;
     tsp0 = grow<float4>(bSp0, 1, s);
     tsp1 = grow<float4>(bSp1, 1, s);
+    tslot = grow<int>(bSlot, 1, s);
   }
   // 5. tiles
   double4* tgeom = grow<double4>(bTileGeom, ntiles, s);
-  int2* tself = grow<int2>(bTileSelf, ntiles, s);
-  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask,
-                                         selfSorted, tgeom, tself);
+  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
   // 6. interaction lists: lengths, offsets and launch order on the host, then the indices
   int64_t* lens = grow<int64_t>(bLen, ntiles, s);
   int64_t* fars = grow<int64_t>(bFar, ntiles, s);
@@ -579,7 +558,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hd.sp1 = tsp1;
   hd.self = selfSorted;
   hd.tiles = Pl.treeTiles;
-  hd.tileSelf = tself;
+  hd.srcSlot = tslot;
   hd.tileCentre = Pl.treeCentres;
   hd.listOff = off;
   hd.list = list;
@@ -588,6 +567,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hd.nslots = nslots;
   hd.ntiles = ntiles;
   hd.nchunks = nchunks;
+  hd.ns = ns;
   hd.eps2 = Pl.eps2;
   TreeDev* dd = grow<TreeDev>(bDev, 1, s);
   ck(cudaMemcpyAsync(dd, &hd, sizeof(hd), cudaMemcpyHostToDevice, s), "upload");

@@ -45,14 +45,14 @@ struct TreeDev {
   const float4* sp0;       // [ns + nprox] sorted sources, then proxies: (x_hi, y_hi, z_hi, w)
   const float4* sp1;       // (x_lo, y_lo, z_lo, D)
   const int* self;         // [nslots] sorted index of the same particle, -1 if none
+  const int* srcSlot;      // [ns] slot of the same particle as sorted source k, -1 if none
   const int2* tiles;       // [ntiles] {first slot, count} (runs inside one level-3 Morton cell)
-  const int2* tileSelf;    // [ntiles] min/max of self over the tile (INT_MAX, -1 if none)
   const int* tileCentre;   // [ntiles] centre slot of the tile (as in the direct kernel)
   const int64_t* listOff;  // [ntiles + 1] offsets into list
   const int* list;         // flattened per-tile source indices into sp0/sp1
   const int* order;        // [ntiles * nchunks] work items (tile * nchunks + part), longest first
   double* partial;         // [nchunks][ncomp][nslots]: part c of every tile's list sums into chunk c
-  int nslots, ntiles, nchunks;
+  int nslots, ntiles, nchunks, ns;
   double eps2;
 };
 

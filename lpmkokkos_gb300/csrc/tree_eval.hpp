@@ -41,10 +41,10 @@ class TreeEval {
  private:
   Octree tree_;
   TreeStats stats_;
-  Buf bPos, bSp0, bSp1, bInv, bSelf, bGeom, bApprox, bTileGeom, bTileSelf, bLen, bFar, bOff, bOrder, bList, bPartial,
-      bDev, bCounter, bErr;
-  std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bTileSelf, &bLen,
-                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bCounter, &bErr};
+  Buf bPos, bSp0, bSp1, bInv, bSelf, bGeom, bApprox, bTileGeom, bLen, bFar, bOff, bOrder, bList, bPartial,
+      bDev, bCounter, bErr, bSlot;
+  std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bLen,
+                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bCounter, &bErr, &bSlot};
   double* partial_ = nullptr;
   int nchunks_ = 1;
   // host source of the last upload (an evaluation synchronises before it rewrites it)
