@@ -51,7 +51,6 @@ class TreeEval {
   TreeDev hDev_{};
   std::vector<int64_t> hLen_, hFar_, hOff_;
   std::vector<int2> hTiles_;
-  const int2* tilesOf_ = nullptr;  // plan whose tile sizes hTiles_ holds
   std::vector<int> hOrder_;
 };
 
