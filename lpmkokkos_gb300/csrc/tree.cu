@@ -437,10 +437,6 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   if (!(tp.theta > 0.0 && tp.theta < 1.0)) fail(LPM_ERR_INVALID_ARGUMENT, "tree code: theta must be in (0, 1)");
   if (!treePairShapeSupported(shape)) fail(LPM_ERR_NOT_SUPPORTED, "tree code: plan built for another launch shape");
   const int ns = Pl.ns, nslots = Pl.nslots, ntiles = Pl.nTreeTiles;
-  // tile sizes, for the pair statistics (read with the list lengths; a rebuilt plan may reuse the
-  // address of an old one, so nothing is cached across evaluations)
-  hTiles_.resize(ntiles);
-  ck(cudaMemcpyAsync(hTiles_.data(), Pl.treeTiles, sizeof(int2) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
   const int P = (tp.degree + 1) * (tp.degree + 1);
   stats_ = TreeStats{};
   // phase timing (with the context's timer): events at the phase boundaries, read at the sync
@@ -516,6 +512,9 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   mark(3);
   hLen_.resize(ntiles);
   hFar_.resize(ntiles);
+  // tile sizes, for the pair statistics (read every time: a rebuilt plan may reuse an old address)
+  hTiles_.resize(ntiles);
+  ck(cudaMemcpyAsync(hTiles_.data(), Pl.treeTiles, sizeof(int2) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
   ck(cudaMemcpyAsync(hLen_.data(), lens, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
   ck(cudaMemcpyAsync(hFar_.data(), fars, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
   int herr = 0;
