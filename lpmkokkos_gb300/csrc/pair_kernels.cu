@@ -46,6 +46,18 @@ __device__ __forceinline__ float lg2Approx(float x) {
   return r;
 }
 
+// Asynchronous global -> shared copies (cp.async, cached in L1 and L2), in commit groups.
+__device__ __forceinline__ void cpAsync16(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsync4(void* smem, const void* gmem) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Kahan step: add v into the compensated pair (h, c); the represented value is h - c.
 __device__ __forceinline__ void kahanAdd(float& h, float& c, float v) {
   const float y = v - c;
@@ -405,7 +417,8 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
 
 // The tree code's gathered pair kernel: persistent CTAs take target tiles (longest index
 // lists first); each tile walks its flattened list of sorted-source and proxy indices
-// (tree.hpp), staging up to ST gathered records at a time.  Only the last block of a list is
+// (tree.hpp), staging up to ST gathered records at a time; the gathered records of the next
+// block are in flight (cp.async) while a block computes.  Only the last block of a list is
 // padded (to the sub-block of 64).  The self-pair check runs only on blocks that hold the source
 // of one of the tile's own targets.  One FP64 partial chunk per target.
 template <int NTH, int K, int ST, int MINB, bool PSI, bool PRECISE, bool NEWTON>
@@ -420,12 +433,36 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
   __shared__ float4 sLXY[PRECISE ? ST : 1];
   __shared__ float2 sLZ[PRECISE ? ST : 1];
   __shared__ int sId[ST];
+  // Raw records of the next block, fetched by cp.async while the current block computes.  Slot j
+  // is written and read back only by the lane that stages source j, so the lane's own wait is
+  // the only synchronisation these buffers need.
+  __shared__ __align__(16) float4 sRaw0[ST];
+  __shared__ __align__(16) float4 sRaw1[ST];
+  __shared__ int sRawSlot[ST];
+  __shared__ int sRawId[ST];
   __shared__ int sItem;
   __shared__ int sCentre;
   SourceTile<PRECISE> T;
   T.xy = sXY; T.zw = sZW; T.d = sD;
   if constexpr (PRECISE) { T.lxy = sLXY; T.lz = sLZ; }
   const TreeDev& S = *dev;
+  constexpr int kPer = ST / NTH;
+  // Starts the copies of one block's records (ids[i]: list entry of slot threadIdx.x + i NTH,
+  // INT_MIN past the end) and records the ids beside them.
+  auto fetch = [&](const int (&ids)[kPer]) {
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int j = threadIdx.x + i * NTH;
+      const int id = ids[i];
+      sRawId[j] = id;
+      if (id != INT_MIN) {
+        cpAsync16(&sRaw0[j], S.sp0 + id);
+        cpAsync16(&sRaw1[j], S.sp1 + id);
+        if (id < S.ns) cpAsync4(&sRawSlot[j], S.srcSlot + id);
+      }
+    }
+    cpAsyncCommit();
+  };
 
   for (;;) {
     if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
@@ -452,39 +489,48 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
     const int64_t l1 = part + 1 == S.nchunks ? tl : tl * (part + 1) / S.nchunks / kSub * kSub;
     const int64_t off = S.listOff[tile] + l0;
     const int64_t len = l1 - l0;
-    // The list indices of a block are loaded one block ahead (into registers, while the
-    // previous block computes), so staging waits only for the records they point to.
-    constexpr int kPer = ST / NTH;
+    // Pipeline: the records of block b + 1 are copied (cp.async) and the list indices of block
+    // b + 2 loaded into registers while block b computes; staging then reads shared memory only.
     int nextId[kPer];
 #pragma unroll
     for (int i = 0; i < kPer; ++i) {
       const int64_t q = threadIdx.x + i * NTH;
       nextId[i] = q < len ? S.list[off + q] : INT_MIN;
     }
+    fetch(nextId);
+#pragma unroll
+    for (int i = 0; i < kPer; ++i) {
+      const int64_t q = ST + threadIdx.x + i * NTH;
+      nextId[i] = q < len ? S.list[off + q] : INT_MIN;
+    }
     for (int64_t b0 = 0; b0 < len; b0 += ST) {
       const int nsrc = (int)min((int64_t)ST, (len - b0 + kSub - 1) / kSub * kSub);
+      cpAsyncWaitAll();  // this lane's copies of block b
       int hit = 0;
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
         const int j = threadIdx.x + i * NTH;
         if (j < nsrc) {
-          const int id = nextId[i];
+          const int id = sRawId[j];
           const bool live = id != INT_MIN;
           if (live && id < S.ns) {  // a source of one of this tile's own targets: check self pairs
-            const int sl = S.srcSlot[id];
+            const int sl = sRawSlot[j];
             hit |= sl >= tile0 && sl < tile0 + tcount;
           }
-          stageSource<K, PRECISE>(j, live, live ? S.sp0[id] : float4{}, live ? S.sp1[id] : float4{}, tt, sXY, sZW,
+          stageSource<K, PRECISE>(j, live, live ? sRaw0[j] : float4{}, live ? sRaw1[j] : float4{}, tt, sXY, sZW,
                                   sD, sLXY, sLZ);
           sId[j] = id;
         }
       }
+      // (the barrier also orders this block's raw reads before the copies that refill the slots)
+      const int anyHit = __syncthreads_or(hit);
+      fetch(nextId);  // block b + 1 (no copies past the end of the list)
 #pragma unroll
       for (int i = 0; i < kPer; ++i) {
-        const int64_t q = b0 + ST + threadIdx.x + i * NTH;
+        const int64_t q = b0 + 2 * ST + threadIdx.x + i * NTH;
         nextId[i] = q < len ? S.list[off + q] : INT_MIN;
       }
-      if (__syncthreads_or(hit))
+      if (anyHit)
         fp32cTile<K, PSI, true, PRECISE, NEWTON, true>(T, nsrc, 0, sId, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
                                                        tt.C, tt.self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
       else
@@ -492,6 +538,7 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
                                                         tt.C, tt.self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
       __syncthreads();
     }
+    cpAsyncWaitAll();  // none are pending (the last fetch is past the list end); kept for safety
     writePartials<NTH, K, PSI>(S.partial + (size_t)part * (PSI ? 5 : 3) * n, n, tile0, tcount, hx, hy, hz, cx, cy, cz,
                                hp, cp, hw, cw);
     (void)P;
@@ -630,6 +677,19 @@ cudaError_t launchTreePair(const PairShape& shape, bool psi, bool precise, bool 
     fn = psi ? (void*)treeFP32C<T, K, ST, B, true, false, false> : (void*)treeFP32C<T, K, ST, B, false, false, false>;
   else
     fn = psi ? (void*)treeFP32C<T, K, ST, B, true, false, true> : (void*)treeFP32C<T, K, ST, B, false, false, true>;
+  // 8 CTAs of ~22 KB static shared memory each need the shared-memory-heavy carveout (once).
+  static const cudaError_t carve = [] {
+    void* all[] = {(void*)treeFP32C<T, K, ST, B, true, true, true>,   (void*)treeFP32C<T, K, ST, B, false, true, true>,
+                   (void*)treeFP32C<T, K, ST, B, true, false, false>, (void*)treeFP32C<T, K, ST, B, false, false, false>,
+                   (void*)treeFP32C<T, K, ST, B, true, false, true>,  (void*)treeFP32C<T, K, ST, B, false, false, true>};
+    for (void* f : all) {
+      const cudaError_t e =
+          cudaFuncSetAttribute(f, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  }();
+  if (carve != cudaSuccess) return carve;
   void* args[] = {(void*)&dev, (void*)&nitems, (void*)&counter};
   return cudaLaunchKernel(fn, dim3(grid), dim3(T), args, 0, s);
 }
