@@ -206,34 +206,44 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
     e1x /= e1n; e1y /= e1n; e1z /= e1n;
     e2x = uy * e1z - uz * e1y; e2y = uz * e1x - ux * e1z; e2z = ux * e1y - uy * e1x;
   }
-  double r2 = 0.0, dmin = DBL_MAX, xmin = DBL_MAX, xmax = -DBL_MAX, ymin = DBL_MAX, ymax = -DBL_MAX;
+  // Radius, chart test and chart extents in FP32 (FP64 runs at 1/64 of the FP32 rate): the radius
+  // only enters the acceptance test and the extents only bound the interpolation interval, so
+  // ~1e-7 absolute errors are absorbed by the margins below.  The charges keep FP64 chart
+  // coordinates.
+  const float fcx = (float)cx, fcy = (float)cy, fcz = (float)cz;
+  const float fux = (float)ux, fuy = (float)uy, fuz = (float)uz;
+  const float f1x = (float)e1x, f1y = (float)e1y, f1z = (float)e1z, f2x = (float)e2x, f2y = (float)e2y, f2z = (float)e2z;
+  float r2 = 0.f, dmin = FLT_MAX, xmin = FLT_MAX, xmax = -FLT_MAX, ymin = FLT_MAX, ymax = -FLT_MAX;
   for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) {
-    const double x = pos[3 * k], y = pos[3 * k + 1], z = pos[3 * k + 2];
-    r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
+    const float x = (float)pos[3 * k], y = (float)pos[3 * k + 1], z = (float)pos[3 * k + 2];
+    r2 = fmaxf(r2, (x - fcx) * (x - fcx) + (y - fcy) * (y - fcy) + (z - fcz) * (z - fcz));
     if (cand) {
-      const double d = x * ux + y * uy + z * uz;
-      dmin = fmin(dmin, d);
-      if (d > 0.0) {
-        const double rd = 1.0 / d;
-        const double xi = (x * e1x + y * e1y + z * e1z) * rd, eta = (x * e2x + y * e2y + z * e2z) * rd;
-        xmin = fmin(xmin, xi); xmax = fmax(xmax, xi); ymin = fmin(ymin, eta); ymax = fmax(ymax, eta);
+      const float d = x * fux + y * fuy + z * fuz;
+      dmin = fminf(dmin, d);
+      if (d > 0.f) {
+        const float rd = __frcp_rn(d);
+        const float xi = (x * f1x + y * f1y + z * f1z) * rd, eta = (x * f2x + y * f2y + z * f2z) * rd;
+        xmin = fminf(xmin, xi); xmax = fmaxf(xmax, xi); ymin = fminf(ymin, eta); ymax = fmaxf(ymax, eta);
       }
     }
   }
-  r2 = blockMax<kUpThreads>(r2, sh);
-  dmin = -blockMax<kUpThreads>(-dmin, sh);
-  xmin = -blockMax<kUpThreads>(-xmin, sh);
-  xmax = blockMax<kUpThreads>(xmax, sh);
-  ymin = -blockMax<kUpThreads>(-ymin, sh);
-  ymax = blockMax<kUpThreads>(ymax, sh);
-  const bool valid = cand && dmin >= kMinChartCos && xmax > xmin && ymax > ymin;
+  const double rad = sqrt(blockMax<kUpThreads>((double)r2, sh)) + 1e-6;  // covers the FP32 rounding
+  const double dlo = -blockMax<kUpThreads>(-(double)dmin, sh);
+  double xlo = -blockMax<kUpThreads>(-(double)xmin, sh);
+  double xhi = blockMax<kUpThreads>((double)xmax, sh);
+  double ylo = -blockMax<kUpThreads>(-(double)ymin, sh);
+  double yhi = blockMax<kUpThreads>((double)ymax, sh);
+  const bool valid = cand && dlo >= kMinChartCos && xhi > xlo && yhi > ylo;
   if (threadIdx.x == 0) {
-    geom[g] = make_double4(cx, cy, cz, sqrt(r2));
+    geom[g] = make_double4(cx, cy, cz, rad);
     approx[g] = valid ? 1 : 0;
   }
   if (!valid) return;
-  const double mx = 0.5 * (xmin + xmax), hx = 0.5 * (xmax - xmin);
-  const double my = 0.5 * (ymin + ymax), hy = 0.5 * (ymax - ymin);
+  // widen the rectangle by the FP32 error of the extents (|xi|, |eta| <= 0.75 on a valid chart)
+  constexpr double kPad = 1e-6;
+  xlo -= kPad; xhi += kPad; ylo -= kPad; yhi += kPad;
+  const double mx = 0.5 * (xlo + xhi), hx = 0.5 * (xhi - xlo);
+  const double my = 0.5 * (ylo + yhi), hy = 0.5 * (yhi - ylo);
   const double ihx = 1.0 / hx, ihy = 1.0 / hy;
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
