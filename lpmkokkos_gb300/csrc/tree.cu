@@ -541,13 +541,22 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   }
   stats_.directPairs = stats_.pairs - stats_.farPairs;
   // Work items: each tile's list in `nchunks` parts (enough items for ~8 waves of CTAs), each
-  // part with its own partial chunk; longest parts first.
+  // part with its own partial chunk; tiles by descending list length (ties by tile index), a
+  // tile's parts in order.  One sort of packed 64-bit keys over the tiles: the host part of an
+  // evaluation is on its critical path.
   const int nchunks = std::max(1, std::min(16, (8 * std::max(1, slots) + ntiles - 1) / std::max(1, ntiles)));
   const int nitems = ntiles * nchunks;
+  hKey_.resize(ntiles);
+  for (int t = 0; t < ntiles; ++t) {
+    const uint64_t l = (uint64_t)std::min<int64_t>(hLen_[t], INT32_MAX);
+    hKey_[t] = ((uint64_t)INT32_MAX - l) << 32 | (uint32_t)t;
+  }
+  std::sort(hKey_.begin(), hKey_.end());
   hOrder_.resize(nitems);
-  std::iota(hOrder_.begin(), hOrder_.end(), 0);
-  std::stable_sort(hOrder_.begin(), hOrder_.end(),
-                   [&](int a, int b) { return hLen_[a / nchunks] > hLen_[b / nchunks]; });
+  for (int i = 0; i < ntiles; ++i) {
+    const int t = (int)(uint32_t)hKey_[i];
+    for (int p = 0; p < nchunks; ++p) hOrder_[(size_t)i * nchunks + p] = t * nchunks + p;
+  }
   int64_t* off = grow<int64_t>(bOff, (size_t)ntiles + 1, s);
   int* order = grow<int>(bOrder, nitems, s);
   int* list = grow<int>(bList, (size_t)std::max<int64_t>(1, hOff_[ntiles]), s);

@@ -52,6 +52,7 @@ class TreeEval {
   std::vector<int64_t> hLen_, hFar_, hOff_;
   std::vector<int2> hTiles_;
   std::vector<int> hOrder_;
+  std::vector<uint64_t> hKey_;  // tiles by descending list length (then tile index), for the order
 };
 
 // Octree depth whose leaves hold about `leafPoints` of n points on the sphere: the nonempty
