@@ -208,8 +208,8 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   }
   // Radius, chart test and chart extents in FP32 (FP64 runs at 1/64 of the FP32 rate): the radius
   // only enters the acceptance test and the extents only bound the interpolation interval, so
-  // ~1e-7 absolute errors are absorbed by the margins below.  The charges keep FP64 chart
-  // coordinates.
+  // ~1e-7 absolute errors are absorbed by the margins below.  The charges take their chart
+  // coordinates from each source's FP64 offset to the chart centre (below).
   const float fcx = (float)cx, fcy = (float)cy, fcz = (float)cz;
   const float fux = (float)ux, fuy = (float)uy, fuz = (float)uz;
   const float f1x = (float)e1x, f1y = (float)e1y, f1z = (float)e1z, f2x = (float)e2x, f2y = (float)e2y, f2z = (float)e2z;
@@ -244,17 +244,20 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   xlo -= kPad; xhi += kPad; ylo -= kPad; yhi += kPad;
   const double mx = 0.5 * (xlo + xhi), hx = 0.5 * (xhi - xlo);
   const double my = 0.5 * (ylo + yhi), hy = 0.5 * (yhi - ylo);
-  const double ihx = 1.0 / hx, ihy = 1.0 / hy;
+  const float fmx = (float)mx, fmy = (float)my, fihx = (float)(1.0 / hx), fihy = (float)(1.0 / hy);
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
   double q = 0.0;  // FP64 total of the per-chunk compensated FP32 sums
   for (int c0 = k0; c0 < k1; c0 += kUpThreads) {
     const int k = c0 + t;
     if (k < k1) {
-      const double x = pos[3 * k], y = pos[3 * k + 1], z = pos[3 * k + 2];
-      const double rd = 1.0 / (x * ux + y * uy + z * uz);
-      const float uxi = (float)(((x * e1x + y * e1y + z * e1z) * rd - mx) * ihx);
-      const float ueta = (float)(((x * e2x + y * e2y + z * e2z) * rd - my) * ihy);
+      // chart coordinates from the offset d = x - c^ (FP64 difference, then FP32): x.c^ = 1 + d.c^
+      // and x.e = d.e for the tangent directions, so every FP32 product is of the offset's size
+      // and the coordinates carry ~1e-7 of it, not of |x|
+      const float dx = (float)(pos[3 * k] - ux), dy = (float)(pos[3 * k + 1] - uy), dz = (float)(pos[3 * k + 2] - uz);
+      const float rd = __frcp_rn(1.f + (dx * fux + dy * fuy + dz * fuz));
+      const float uxi = ((dx * f1x + dy * f1y + dz * f1z) * rd - fmx) * fihx;
+      const float ueta = ((dx * f2x + dy * f2y + dz * f2z) * rd - fmy) * fihy;
       basisF(uxi, degree, sT, sBw, sp0[k].w, &sL[t][0]);  // w L_a(xi): one FMA per proxy below
       basisF(ueta, degree, sT, sBw, 1.f, &sL[t][n1]);
     }
