@@ -354,7 +354,7 @@ Octree::~Octree() {
 }
 
 void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int maxDepth, bool neighbors,
-                   cudaStream_t s) {
+                   cudaStream_t s, bool hostBox) {
   if (maxDepth < 1 || maxDepth > kOctreeMaxDepth) fail(LPM_ERR_INVALID_ARGUMENT, "octree depth must be 1..%d", kOctreeMaxDepth);
   if (npts <= 0 || npts > INT32_MAX) fail(LPM_ERR_INVALID_ARGUMENT, "octree: 1..2^31-1 points");
   std::call_once(g_tablesOnce, [] {
@@ -491,8 +491,10 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
     if (neighbors)
       check(cudaMemcpyAsync(nbrs + 27 * b, bLevNbrs[l].p, 27 * m * sizeof(int), cudaMemcpyDeviceToDevice, s), "copy");
   }
-  check(cudaMemcpyAsync(box, dbx, sizeof(box), cudaMemcpyDeviceToHost, s), "read-back");
-  check(cudaStreamSynchronize(s), "synchronise");
+  if (hostBox) {
+    check(cudaMemcpyAsync(box, dbx, sizeof(box), cudaMemcpyDeviceToHost, s), "read-back");
+    check(cudaStreamSynchronize(s), "synchronise");
+  }
   check(cudaGetLastError(), "launch");
 }
 

@@ -31,7 +31,10 @@ class Octree {
 
   // Builds the tree of n points x[i*si + c*sc] (device) with leaves at `depth`.  Reads the level
   // sizes back (synchronises `s`); buffers are reused by later builds when large enough.
-  void build(const double* x, int64_t si, int64_t sc, int64_t n, int depth, bool neighbors, cudaStream_t s);
+  // hostBox = false leaves `box` stale and returns with the last copies still queued on `s`
+  // (for a caller that reads only device arrays and synchronises later).
+  void build(const double* x, int64_t si, int64_t sc, int64_t n, int depth, bool neighbors, cudaStream_t s,
+             bool hostBox = true);
 
   int depth = 0;
   int64_t n = 0, nnodes = 0;

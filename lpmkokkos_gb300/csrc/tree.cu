@@ -93,7 +93,7 @@ __global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__
 __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
                                                        const int2* __restrict__ tiles, const int* __restrict__ perm,
                                                        int64_t na, const uint8_t* __restrict__ mask,
-                                                       double4* __restrict__ geom) {
+                                                       double4_32a* __restrict__ geom) {
   __shared__ double sh[kBlock / 32];
   const int2 tr = tiles[blockIdx.x];
   const int t0 = tr.x, cnt = tr.y;
@@ -112,7 +112,7 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
   sz = blockSum<kBlock>(sz, sh);
   sc = blockSum<kBlock>(sc, sh);
   if (sc == 0.0) {
-    if (threadIdx.x == 0) geom[blockIdx.x] = make_double4(0, 0, 0, INFINITY);
+    if (threadIdx.x == 0) geom[blockIdx.x] = make_double4_32a(0, 0, 0, INFINITY);
     return;
   }
   const double cx = sx / sc, cy = sy / sc, cz = sz / sc;
@@ -123,7 +123,7 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
     if (shapes(slot, x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
   }
   r2 = blockMax<kBlock>(r2, sh);
-  if (threadIdx.x == 0) geom[blockIdx.x] = make_double4(cx, cy, cz, sqrt(r2));
+  if (threadIdx.x == 0) geom[blockIdx.x] = make_double4_32a(cx, cy, cz, sqrt(r2));
 }
 
 // Chebyshev points of the second kind t_a = cos(pi a / n) and their barycentric weights.
@@ -169,7 +169,7 @@ __device__ __forceinline__ void basisF(float u, int n, const float* t, const flo
 // at sp0/sp1[ns + g (n+1)^2 + ab].
 __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, const double* __restrict__ pos,
                                                      int degree, const Cheb C, int ns, int firstNode,
-                                                     double4* __restrict__ geom, int* __restrict__ approx,
+                                                     double4_32a* __restrict__ geom, int* __restrict__ approx,
                                                      float4* __restrict__ sp0, float4* __restrict__ sp1) {
   __shared__ double sh[kUpThreads / 32];
   __shared__ float sL[kUpThreads][2 * kMaxNodes1D];
@@ -184,7 +184,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   if (pt.y == 0 || g < firstNode) {
     // empty; or the root and the octants, whose sources span more than any chart allows (their
     // geometry would only ever open them, so they are opened unconditionally: infinite radius)
-    if (threadIdx.x == 0) { geom[g] = make_double4(0, 0, 0, pt.y == 0 ? -1.0 : INFINITY); approx[g] = 0; }
+    if (threadIdx.x == 0) { geom[g] = make_double4_32a(0, 0, 0, pt.y == 0 ? -1.0 : INFINITY); approx[g] = 0; }
     return;
   }
   const int k0 = pt.x, k1 = pt.x + pt.y;
@@ -235,7 +235,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   double yhi = blockMax<kUpThreads>((double)ymax, sh);
   const bool valid = cand && dlo >= kMinChartCos && xhi > xlo && yhi > ylo;
   if (threadIdx.x == 0) {
-    geom[g] = make_double4(cx, cy, cz, rad);
+    geom[g] = make_double4_32a(cx, cy, cz, rad);
     approx[g] = valid ? 1 : 0;
   }
   if (!valid) return;
@@ -302,8 +302,8 @@ constexpr int kWarpStack = 4096;  // per-warp node stack: <= 256 entries per lev
 // list at listOff[tile], contiguous direct ranges merged.  A stack overflow (impossible for the
 // depths the tree code builds) sets *err instead of writing out of bounds.
 template <bool FILL>
-__global__ void __launch_bounds__(32) traverse(const double4* __restrict__ tileGeom, int ntiles,
-                                               const double4* __restrict__ geom, const int* __restrict__ approx,
+__global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ tileGeom, int ntiles,
+                                               const double4_32a* __restrict__ geom, const int* __restrict__ approx,
                                                const int2* __restrict__ ptInds, const int* __restrict__ kids,
                                                Levels lv, int depth, double theta, int P, int ns,
                                                int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(32) traverse(const double4* __restrict__ tileG
   const int tile = blockIdx.x;
   const int lane = threadIdx.x;
   if (tile >= ntiles) return;
-  const double4 tg = tileGeom[tile];
+  const double4_32a tg = tileGeom[tile];
   if (lane == 0) stack[0] = 0;  // the root (level 0, global index 0)
   __syncwarp();
   int sp = 1;
@@ -332,7 +332,7 @@ __global__ void __launch_bounds__(32) traverse(const double4* __restrict__ tileG
     if (g >= 0) {
       pt = ptInds[g];
       if (pt.y > 0) {
-        const double4 ng = geom[g];
+        const double4_32a ng = geom[g];
         const double dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
         const bool mac = (tg.w + ng.w) < theta * sqrt(dx * dx + dy * dy + dz * dz);
         while (lev < depth && g >= lv.base[lev + 1]) ++lev;
@@ -466,14 +466,14 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   int nnodes = 0;
   float4* tsp0 = nullptr;
   float4* tsp1 = nullptr;
-  double4* geom = nullptr;
+  double4_32a* geom = nullptr;
   int* approx = nullptr;
   if (ns > 0) {
     // 1-3. octree over the stage positions, sources in key order
     double* pos = grow<double>(bPos, 3 * (size_t)ns, s);
     srcPositions<<<blocks(ns), kBlock, 0, s>>>(Pl.stage.sp0, Pl.stage.sp1, ns, pos);
     const int depth = treeDepthFor(ns, tp.leafPoints);
-    tree_.build(pos, 3, 1, ns, depth, false, s);
+    tree_.build(pos, 3, 1, ns, depth, false, s, /*hostBox=*/false);  // the next sync: the list lengths
     mark(1);
     nnodes = (int)tree_.nnodes;
     stats_.depth = depth;
@@ -489,7 +489,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     sortedSelf<<<blocks(nslots), kBlock, 0, s>>>(Pl.dev.self, inv, nslots, ss);
     selfSorted = ss;
     // 4. upward pass
-    geom = grow<double4>(bGeom, nnodes, s);
+    geom = grow<double4_32a>(bGeom, nnodes, s);
     approx = grow<int>(bApprox, nnodes, s);
     upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns,
                                          depth >= 2 ? tree_.base[2] : nnodes, geom, approx, tsp0, tsp1);
@@ -505,7 +505,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     tslot = grow<int>(bSlot, 1, s);
   }
   // 5. tiles
-  double4* tgeom = grow<double4>(bTileGeom, ntiles, s);
+  double4_32a* tgeom = grow<double4_32a>(bTileGeom, ntiles, s);
   tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
   // 6. interaction lists: lengths, offsets and launch order on the host, then the indices
   int64_t* lens = grow<int64_t>(bLen, ntiles, s);
