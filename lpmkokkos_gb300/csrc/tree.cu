@@ -86,9 +86,9 @@ __global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__
 }
 
 // Centroid and radius of each target tile over its vertices and leaf faces.  Masked parent
-// faces do not shape the tile: on the icosahedral mesh a parent's centre is its middle child's,
-// its velocity is singular in the reference's formula, and after a step it runs away (its
-// bounding sphere would then admit no far field).  Parents are still evaluated with their tile's
+// faces do not shape the tile: on the icosahedral mesh a parent's centre lies within ~1e-6 of its
+// middle child's, its velocity is near-singular in the reference's formula, and after a step it
+// runs away (its bounding sphere would then admit no far field).  Parents are still evaluated with their tile's
 // list; a cubed-sphere parent sits on its children's shared corner, inside the tile.
 __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
                                                        const int2* __restrict__ tiles, const int* __restrict__ perm,

@@ -4,8 +4,9 @@ The tree code is an approximation outside the reference: far source clusters act
 chart-interpolated proxies (lpmkokkos_gb300/csrc/tree.hpp).  Its bar is the FP32C bar --
 relative L2 <= 1e-6 against the FP64 direct sum -- at the default parameters (degree 8,
 theta 0.6, 512 sources per leaf; measured 8e-8 at icosahedral levels 6-7 and 1.2e-7 at level 8).
-Masked icosahedral parents coincide with a leaf and are NaN in every path, so comparisons take
-vertices and leaf faces."""
+Masked icosahedral parents lie within ~1e-6 of a leaf, so their velocities are dominated by that
+near-singular pair in every path (some inf/NaN).  Comparisons therefore take vertices and leaf
+faces."""
 import math
 
 import numpy as np
