@@ -171,3 +171,27 @@ def test_octree_and_tree_code_argument_checks(native):
     assert lib.lpm_bve_ctx_set_treecode(None, 8, 0.6, 512, 0.0) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_bve_ctx_tree_stats(None, None, None, None, None, None, None, None) == L.LPM_ERR_INVALID_ARGUMENT
     assert lib.lpm_sphere_tangency(ptr, 3, 1, ptr, 3, 1, -1, ptr, None) == L.LPM_ERR_INVALID_ARGUMENT
+
+
+def _integration_index():
+    """Function names of the integration notes' entry-point index; a cell's `_suffix` entries
+    share the first name's prefix (`lpm_octree_build`, `_info` -> lpm_octree_info)."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    section = text.split("## 9. Entry-point index", 1)[1]
+    names = set()
+    for line in section.splitlines():
+        if not line.startswith("| `"):
+            continue
+        cell = line.split("|")[1]
+        entries = re.findall(r"`([a-z0-9_]+)`", cell)
+        prefix = entries[0].rsplit("_", 1)[0]
+        for e in entries:
+            names.add(prefix + e if e.startswith("_") else e)
+    return names
+
+
+def test_integration_index_lists_every_declared_function():
+    declared = _declared_functions()
+    listed = _integration_index()
+    assert not declared - listed, sorted(declared - listed)
+    assert not listed - declared, sorted(listed - declared)
