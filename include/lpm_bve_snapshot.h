@@ -9,8 +9,10 @@
  *     matches the uninterrupted run to the rounding of the summation order);
  *   - a legacy VTK PolyData file (vertices as points, leaf faces as polygons, relative vorticity
  *     and velocity as point and cell data, face area) that VTK readers and ParaView open.
- * Arrays may live on the device or the host (copies use cudaMemcpyDefault); every call
- * synchronises `stream`.  Errors return a negative status and print a message on stderr.
+ * Arrays may live on the device or the host.  Device and managed arrays are copied on `stream`,
+ * host arrays with memcpy.  Every call synchronises `stream` when a CUDA device is present; with
+ * host arrays the calls also work without one (stream NULL), e.g. for post-processing.
+ * Errors return a negative status and print a message on stderr.
  */
 #ifndef LPM_BVE_SNAPSHOT_H
 #define LPM_BVE_SNAPSHOT_H

@@ -203,11 +203,19 @@ def mesh_face_verts(seed: int, level: int) -> np.ndarray:
 # ----------------------------------------------------------------------------------------
 # snapshots and VTK output (include/lpm_bve_snapshot.h)
 # ----------------------------------------------------------------------------------------
+def _state_stream(state: "BVEState", stream) -> ctypes.c_void_p:
+    """The stream of a snapshot call: the caller's, else the current one for device state, else
+    none (a state of host tensors needs no device)."""
+    if stream is None and not state.vx.is_cuda:
+        return ctypes.c_void_p(None)
+    return _stream(stream)
+
+
 def snapshot_write(path: str, state: "BVEState", seed: int, level: int, t: float = 0.0, dt: float = 0.0,
                    omega: float = 2 * PI, stream=None):
     st = state.c_struct()
     L.check(L.lib().lpm_bve_snapshot_write(path.encode(), ctypes.byref(st), seed, level, t, dt, omega,
-                                           _stream(stream)))
+                                           _state_stream(state, stream)))
 
 
 def snapshot_info(path: str) -> dict:
@@ -223,13 +231,14 @@ def snapshot_read(path: str, state: "BVEState", stream=None) -> float:
     """Restores positions, vorticity and velocity into `state`; returns the snapshot's time."""
     st = state.c_struct()
     t = ctypes.c_double()
-    L.check(L.lib().lpm_bve_snapshot_read(path.encode(), ctypes.byref(st), ctypes.byref(t), _stream(stream)))
+    L.check(L.lib().lpm_bve_snapshot_read(path.encode(), ctypes.byref(st), ctypes.byref(t),
+                                          _state_stream(state, stream)))
     return t.value
 
 
 def vtk_write(path: str, state: "BVEState", seed: int, level: int, stream=None):
     st = state.c_struct()
-    L.check(L.lib().lpm_bve_vtk_write(path.encode(), ctypes.byref(st), seed, level, _stream(stream)))
+    L.check(L.lib().lpm_bve_vtk_write(path.encode(), ctypes.byref(st), seed, level, _state_stream(state, stream)))
 
 
 # ----------------------------------------------------------------------------------------
@@ -237,7 +246,8 @@ def vtk_write(path: str, state: "BVEState", seed: int, level: int, stream=None):
 # ----------------------------------------------------------------------------------------
 @dataclass
 class BVEState:
-    """Device arrays of one solve (the arguments of BVERK4::advance_timestep)."""
+    """Device arrays of one solve (the arguments of BVERK4::advance_timestep).  Snapshot and VTK
+    calls also take a state of host tensors."""
     vx: torch.Tensor
     vzeta: torch.Tensor
     vvel: torch.Tensor

@@ -54,14 +54,47 @@ struct File {
   }
 };
 
-// Device (or host: the copies use cudaMemcpyDefault) strided n x 3 array -> host row-major.
+// True for device or managed memory; false for host memory and whenever no CUDA device is
+// present (the attribute query then fails and its error is cleared).
+bool cudaOwned(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+bool haveDevice() {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return false;
+  }
+  return n > 0;
+}
+
+// Copies between the caller's arrays and host buffers.  Device or managed memory goes through
+// `s`; host-only copies use memcpy (no device needed), after synchronising `s` when a device
+// exists, so work queued on `s` into pinned host arrays is complete first.
+void copyBytes(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return;
+  if (cudaOwned(dst) || cudaOwned(src)) {
+    LPM_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDefault, s));
+    LPM_CUDA(cudaStreamSynchronize(s));
+    return;
+  }
+  if (haveDevice()) LPM_CUDA(cudaStreamSynchronize(s));
+  std::memcpy(dst, src, bytes);
+}
+
+// Strided n x 3 array (device or host) -> host row-major.
 std::vector<double> fetchVec(const double* p, int64_t n, int64_t si, int64_t sc, cudaStream_t s) {
   std::vector<double> out(3 * (size_t)n);
   if (n == 0) return out;
   const int64_t span = (n - 1) * si + 2 * sc + 1;
   std::vector<double> raw((size_t)span);
-  LPM_CUDA(cudaMemcpyAsync(raw.data(), p, sizeof(double) * span, cudaMemcpyDefault, s));
-  LPM_CUDA(cudaStreamSynchronize(s));
+  copyBytes(raw.data(), p, sizeof(double) * span, s);
   for (int64_t i = 0; i < n; ++i)
     for (int c = 0; c < 3; ++c) out[3 * i + c] = raw[(size_t)(i * si + c * sc)];
   return out;
@@ -70,10 +103,7 @@ std::vector<double> fetchVec(const double* p, int64_t n, int64_t si, int64_t sc,
 template <typename T>
 std::vector<T> fetchScalar(const T* p, int64_t n, cudaStream_t s) {
   std::vector<T> out((size_t)n);
-  if (n > 0) {
-    LPM_CUDA(cudaMemcpyAsync(out.data(), p, sizeof(T) * n, cudaMemcpyDefault, s));
-    LPM_CUDA(cudaStreamSynchronize(s));
-  }
+  if (n > 0) copyBytes(out.data(), p, sizeof(T) * n, s);
   return out;
 }
 
@@ -82,25 +112,20 @@ std::vector<T> fetchScalar(const T* p, int64_t n, cudaStream_t s) {
 void storeVec(double* p, const std::vector<double>& v, int64_t n, int64_t si, int64_t sc, cudaStream_t s) {
   if (n == 0) return;
   if (si == 3 && sc == 1) {
-    LPM_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(double) * 3 * n, cudaMemcpyDefault, s));
-    LPM_CUDA(cudaStreamSynchronize(s));
+    copyBytes(p, v.data(), sizeof(double) * 3 * n, s);
     return;
   }
   const int64_t span = (n - 1) * si + 2 * sc + 1;
   std::vector<double> raw((size_t)span);
-  LPM_CUDA(cudaMemcpyAsync(raw.data(), p, sizeof(double) * span, cudaMemcpyDefault, s));
-  LPM_CUDA(cudaStreamSynchronize(s));
+  copyBytes(raw.data(), p, sizeof(double) * span, s);
   for (int64_t i = 0; i < n; ++i)
     for (int c = 0; c < 3; ++c) raw[(size_t)(i * si + c * sc)] = v[3 * i + c];
-  LPM_CUDA(cudaMemcpyAsync(p, raw.data(), sizeof(double) * span, cudaMemcpyDefault, s));
-  LPM_CUDA(cudaStreamSynchronize(s));
+  copyBytes(p, raw.data(), sizeof(double) * span, s);
 }
 
 template <typename T>
 void storeScalar(T* p, const std::vector<T>& v, cudaStream_t s) {
-  if (v.empty()) return;
-  LPM_CUDA(cudaMemcpyAsync(p, v.data(), sizeof(T) * v.size(), cudaMemcpyDefault, s));
-  LPM_CUDA(cudaStreamSynchronize(s));
+  if (!v.empty()) copyBytes(p, v.data(), sizeof(T) * v.size(), s);
 }
 
 void checkState(const lpm_bve_state* st) {

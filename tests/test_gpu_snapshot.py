@@ -19,6 +19,7 @@ import torch
 import lpmkokkos_gb300 as P
 from lpmkokkos_gb300 import _lib as L
 from lpmkokkos_gb300 import bve
+from vtk_reader import read_vtk_sections
 
 pytestmark = pytest.mark.gpu
 
@@ -111,49 +112,12 @@ def test_snapshot_of_another_mesh_is_refused(ctx, tmp_path):
         bve.snapshot_info(str(bad))
 
 
-def _read_vtk_sections(raw):
-    """Splits a legacy binary VTK PolyData file into (keyword line, payload bytes) records."""
-    out, pos = [], 0
-    header = []
-    for _ in range(4):
-        end = raw.index(b"\n", pos)
-        header.append(raw[pos:end].decode())
-        pos = end + 1
-    sizes = {"double": 8, "int": 4}
-    while pos < len(raw):
-        while pos < len(raw) and raw[pos:pos + 1] == b"\n":
-            pos += 1
-        if pos >= len(raw):
-            break
-        end = raw.index(b"\n", pos)
-        line = raw[pos:end].decode()
-        pos = end + 1
-        parts = line.split()
-        if parts[0] == "POINTS":
-            n = int(parts[1]) * 3 * sizes[parts[2]]
-        elif parts[0] == "POLYGONS":
-            n = int(parts[2]) * 4
-        elif parts[0] in ("POINT_DATA", "CELL_DATA"):
-            out.append((line, b"")); count = int(parts[1]); continue
-        elif parts[0] == "SCALARS":
-            end = raw.index(b"\n", pos); pos = end + 1          # LOOKUP_TABLE line
-            n = count * 8
-        elif parts[0] == "VECTORS":
-            n = count * 3 * 8
-        else:
-            raise AssertionError(line)
-        out.append((line, raw[pos:pos + n]))
-        assert len(raw[pos:pos + n]) == n, line
-        pos += n
-    return header, out
-
-
 @pytest.mark.parametrize("seed", [0, 1])
 def test_vtk_file_layout(ctx, tmp_path, seed):
     a = _sphere(ctx, seed, 3, P.FP64)
     path = tmp_path / "a.vtk"
     bve.vtk_write(str(path), a.state(), seed, 3)
-    header, secs = _read_vtk_sections(path.read_bytes())
+    header, secs = read_vtk_sections(path.read_bytes())
     assert header[0].startswith("# vtk DataFile") and header[2] == "BINARY" and header[3] == "DATASET POLYDATA"
     kinds = [s[0].split()[0] for s in secs]
     assert kinds == ["POINTS", "POLYGONS", "POINT_DATA", "SCALARS", "VECTORS", "CELL_DATA", "SCALARS", "SCALARS",
