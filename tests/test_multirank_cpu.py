@@ -55,3 +55,26 @@ def test_reference_arm_nonzero_ranks_do_nothing(capsys, monkeypatch):
     monkeypatch.setenv("WORLD_SIZE", "2")
     bench.main()
     assert capsys.readouterr().out == ""
+
+
+def test_reference_arm_json_line(capsys, monkeypatch):
+    """The reference arm's line (CPU oracle, small mesh): the GPU arm's metric, unit and workload,
+    a cpu_baseline describing the run and an e2e block with no host-device traffic."""
+    import json
+
+    import bench
+    monkeypatch.setattr("sys.argv", ["bench.py", "--impl", "reference", "--level", "3", "--steps", "1",
+                                     "--warmup", "0"])
+    monkeypatch.delenv("RANK", raising=False)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    bench.main()
+    lines = [line for line in capsys.readouterr().out.splitlines() if line.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "RK4 steps/s" and d["unit"] == "steps/s"
+    assert d["higher_is_better"] is True and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 0
+    assert d["value"] > 0 and d["ms_per_step"] == pytest.approx(1000.0 / d["value"])
+    assert d["config"]["workload"] == bench.workload_desc(3)
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert d["e2e"] == {"value": d["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
