@@ -872,6 +872,8 @@ def run_server(args, rank, world, local_rank):
                       "mean_wait": float(waits.mean())},
         "latency_by_level": by_level,
         "solve_steps_per_s": solve_steps / wall, "computed_pairs_per_s": pairs / wall,
+        **({"computed_pairs_note": "tree-code requests count the direct-sum pairs their evaluations replace"}
+           if args.tree else {}),
         "server_iterations": st["steps_run"] - base["steps_run"], "max_running": st["max_running_seen"],
         "wall_s": wall, "mix_equals_alone": bool(same), "clocks": clocks,
         "serial_fp64_gpu": {"pairs_per_s": r64, "seconds": serial64, "requests_per_s": n / serial64,

@@ -51,7 +51,8 @@ typedef struct {
   int64_t submitted, completed, failed, cancelled, running, queued;
   int64_t steps_run;          /* RK4 steps launched over size classes (one step of one class) */
   int64_t solve_steps;        /* sum over solves of RK4 steps taken */
-  double pairs;               /* target-source pairs evaluated (incl. masked-parent targets) */
+  double pairs;               /* target-source pairs evaluated (incl. masked-parent targets);
+                                 a tree-code request counts the direct-sum pairs it replaces */
   double busy_s;              /* wall time with at least one solve running */
   size_t reserved_bytes, budget_bytes;
   int max_running_seen;

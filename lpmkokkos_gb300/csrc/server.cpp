@@ -656,6 +656,7 @@ void treeRequest(lpm_bve_server* S, lpm_bve_ctx* ctx, cudaStream_t ts, Req* r) {
   S->inflight -= 1;
   S->st.completed += 1;
   S->st.solve_steps += r->r.nsteps;
+  S->st.pairs += 4.0 * r->r.nsteps * r->pairsPerEval;  // the direct-sum pairs the steps replace
   S->latencies.push_back(seconds(r->tSubmit, r->tDone));
   S->cvDone.notify_all();
   S->cvPrep.notify_all();
@@ -688,10 +689,12 @@ void treeLoop(lpm_bve_server* S) {
       treeRequest(S, ctx, ts, r);
     } catch (const Error& e) {
       if (ts) cudaStreamSynchronize(ts);
+      if (ctx) lpm_bve_plan_invalidate(ctx);  // plans of the failed request's (reused) arrays
       std::lock_guard<std::mutex> lk(S->mu);
       failLocked(S, r, "tree code: " + e.msg);
     } catch (const std::exception& e) {
       if (ts) cudaStreamSynchronize(ts);
+      if (ctx) lpm_bve_plan_invalidate(ctx);
       std::lock_guard<std::mutex> lk(S->mu);
       failLocked(S, r, "tree code: " + fromStd(e).msg);
     }
