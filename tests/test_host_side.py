@@ -195,3 +195,21 @@ def test_integration_index_lists_every_declared_function():
     listed = _integration_index()
     assert not declared - listed, sorted(declared - listed)
     assert not listed - declared, sorted(listed - declared)
+
+
+@pytest.mark.parametrize("level", [2, 4, 7, 8])
+def test_bench_work_units_match_the_mesh(native, level):
+    """The benchmark's work units: its closed-form mesh sizes equal the library's counts, the
+    algorithmic pairs per evaluation are (vertices + leaves) x leaves (3.933e7 at icosahedral
+    level 4, 1.611e11 at 7, 2.577e12 at 8), and the computed pairs add the masked-parent targets."""
+    import bench
+    from lpmkokkos_gb300 import bve
+    nv, nall, nl = bench.mesh_sizes(level)
+    assert (nv, nall, nl) == bve.mesh_counts(0, level)
+    alg = (nv + nl) * nl
+    quoted = {4: 3.933e7, 7: 1.611e11, 8: 2.577e12}
+    if level in quoted:
+        assert alg == pytest.approx(quoted[level], rel=5e-4)
+    assert bench.computed_pairs(0, level) == (nv + nall) * nl
+    cnv, cnall, cnl = bve.mesh_counts(1, level)
+    assert bench.computed_pairs(1, level) == (cnv + cnall) * cnl
