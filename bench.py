@@ -1,25 +1,35 @@
 #!/usr/bin/env python
-"""Benchmark of the GB300 BVE path: RK4 steps/s on one solve at icosahedral level 7.
+"""Benchmark of the GB300 BVE path: RK4 steps/s of one solve at icosahedral level 8.
 
-Workload (the single-solve configuration the headline metric is quoted on): icosahedral
-level 7 (163,842 vertices; 436,900 faces of which 327,680 leaves are the sources), RH54
-relative vorticity plus 3 seeded Gaussian vortices (amplitude U(-2,2), width 0.1 rad),
-Omega = 2 pi, eps = 0, dt = 0.00125 (0.01 at level 4, halved per level).  A step is one
-RK4 step (four direct-sum evaluations over every vertex and face target).  Synthetic data
-generated on the host; nothing is downloaded.
+Default workload (the largest single-GPU configuration of the headline metric): icosahedral
+level 8 -- 655,362 vertices; 1,747,620 faces of which 1,310,720 leaves are the sources -- RH54
+relative vorticity plus 8 seeded Gaussian vortices (amplitude U(-2,2), width 0.1 rad),
+Omega = 2 pi, eps = 0.01, dt = 0.000625 (0.01 at level 4, halved per level), RK4 steps, then
+the stream function and velocity at every vertex and face.  A step is one RK4 step: four
+direct-sum evaluations over every vertex and face target (2,403,+ targets x 1,310,720 sources).
+Synthetic data generated on the host; nothing is downloaded.  ``--config c2`` runs the
+level-7 single solve (RH54 + 3 vortices, eps 0) the same way; it is also reported as a
+secondary leg of the default line.
 
 Printed JSON line (rank 0):
-  value      RK4 steps/s, whole job, device-resident inputs, graph-replayed steps
-  e2e        the same through lpm_bve_rk4_step with the state copied host->device before
-             and device->host after every step (pinned buffers)
-  roofline   pair kernel: algorithmic pairs per launch / CUDA-event launch time, against
-             the FP32 FMA-pipe peak (13 FMA-pipe lane-ops per pair)
-  cpu_baseline  the CPU oracle (OpenMP restatement of the reference path) on the host cores
-  fp64_gpu   the plain FP64 GPU path on a sample of targets, and FP32C-vs-FP64 error there
+  value        RK4 steps/s, whole job, device-resident state, graph-replayed steps
+  e2e          the same through lpm_bve_rk4_step with the state copied host->device before and
+               device->host after every step (pinned buffers)
+  roofline     pair kernel: algorithmic pairs per launch / CUDA-event launch time, against the
+               FP32 FMA-pipe peak (13 FMA-pipe lane-ops per pair)
+  psi_pass     the closing stream-function + velocity evaluation at every target
+  oracle_parity  FP32C and plain-FP64 GPU results against the CPU oracle on 4,096 + 4,096
+               sampled vertex / leaf-face targets summed over all sources, initial and final state
+  fp64_gpu     the plain FP64 GPU path: its pair rate on a target sample at this level, and a full
+               FP64 RK4 step at level 6 timed beside a sample there (the sample's validity)
+  cpu_baseline the CPU oracle (OpenMP restatement of the reference path) on the host cores
+  c2_level7    the level-7 single solve: steps/s and its pair kernel's roofline fraction
 
---impl reference times the reference's CPU path (the oracle port; the reference itself
-cannot be built here) on the same workload, each step a bounded sample of targets.
-Under torchrun (N > 1) every rank advances its own replica of the solve ("scaling": "weak").
+--impl reference times the reference's CPU path (the oracle port; the reference itself cannot
+be built here) on the same workload and config: each step is one evaluation over a bounded
+random sample of targets, extrapolated to a full RK4 step, and one full evaluation at level 6 is
+timed beside a sample there.  Under torchrun (N > 1) every rank advances its own replica of the
+solve ("scaling": "weak").
 """
 from __future__ import annotations
 
@@ -30,6 +40,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -37,7 +48,13 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 SEED_BASE = 20261203
-WORKLOAD = dict(seed_kind=0, level=7, ngauss=3, width=0.1, omega=2 * math.pi, eps=0.0, ic_seed=SEED_BASE + 1)
+# single-solve workloads: c2 = icosahedral level 7, c5 = icosahedral level 8 (the default)
+WORKLOADS = {
+    "c2": dict(seed_kind=0, level=7, ngauss=3, width=0.1, omega=2 * math.pi, eps=0.0, ic_seed=SEED_BASE + 1,
+               psi_pass=False),
+    "c5": dict(seed_kind=0, level=8, ngauss=8, width=0.1, omega=2 * math.pi, eps=0.01, ic_seed=SEED_BASE + 5,
+               psi_pass=True),
+}
 
 
 def time_step(level: int) -> float:
@@ -46,6 +63,8 @@ def time_step(level: int) -> float:
     A fixed dt = 0.01 at level 7 moves stage positions ~2 mesh spacings off the sphere, where
     the reference's 1 - x.y denominator crosses zero for nearest neighbours."""
     return 0.01 * 2.0 ** (4 - level)
+
+
 OPS_PER_PAIR = 13  # FP32 FMA-pipe lane operations per velocity pair in the FP32C kernel
 # DRAM bytes per pair-kernel launch per particle (target + source): ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one level-6 launch, 6.91 MB for 150,182 targets + 81,920 sources
@@ -85,25 +104,28 @@ def hbm_line(traffic_bytes, launch_ms):
             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peak else None}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--level", type=int, default=WORKLOAD["level"])
     ap.add_argument("--prec", choices=["fp32c", "fp64"], default="fp32c")
-    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--e2e-steps", type=int, default=0,
+                    help="RK4 steps of the end-to-end pass (0: half of --steps, at least 3)")
     ap.add_argument("--err-steps", type=int, default=0,
-                    help="c2: also advance an FP64 trajectory beside an FP32C one for this many steps and report "
+                    help="c2/c5: also advance an FP64 trajectory beside an FP32C one for this many steps and report "
                          "the per-step velocity/vorticity errors (device norms; FP64 is ~150x slower)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-parity", action="store_true", help="skip the sampled-target oracle comparison")
+    ap.add_argument("--no-secondary", action="store_true", help="c5: skip the level-7 secondary leg")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
-    ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c2",
-                    help="c2: single solve icos L7 (default, the headline); c3: 64-solve uneven ensemble; "
-                         "c4: continuous-batching server under Poisson arrivals; "
-                         "c5: icos L8, eps 0.01, 8 vortices, then the stream function at all targets")
+    ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c5",
+                    help="c5: icos L8, eps 0.01, 8 vortices, RK4 steps then the stream function at all targets "
+                         "(default, the headline); c2: single solve icos L7; c3: 64-solve uneven ensemble; "
+                         "c4: continuous-batching server under Poisson arrivals")
+    ap.add_argument("--level", type=int, default=0, help="c2/c5: override the mesh level (0: the config's)")
     ap.add_argument("--requests", type=int, default=96, help="c4: number of requests")
     ap.add_argument("--rate", type=float, default=8.0, help="c4: mean arrivals per second (0: set by --util)")
     ap.add_argument("--util", type=float, default=0.7, help="c4 with --rate 0: target device utilisation")
@@ -119,8 +141,8 @@ def parse():
                     help="c4: a server with LPM_BVE_TREECODE (requests of >= 1e9 pairs per evaluation run on "
                          "its tree-code thread)")
     ap.add_argument("--tree-only", action="store_true",
-                    help="c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
-    return ap.parse_args()
+                    help="c2/c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
+    return ap.parse_args(argv)
 
 
 def max_over_ranks(x: float, world: int, device=None) -> float:
@@ -139,10 +161,18 @@ def whole_job_rate(world: int, units_per_rank: int, max_elapsed_ms: float) -> fl
     return world * units_per_rank / (max_elapsed_ms * 1e-3)
 
 
-def workload_desc(level):
-    w = dict(WORKLOAD, level=level)
-    return (f"icosahedral level {level}, RH54 + {w['ngauss']} Gaussian vortices (seed {w['ic_seed']}, "
-            f"amp U(-2,2), width {w['width']}), eps {w['eps']}, dt {time_step(level):g}, Omega 2pi")
+def workload(config: str, level: int = 0) -> dict:
+    w = dict(WORKLOADS[config])
+    if level:
+        w["level"] = level
+    w["dt"] = time_step(w["level"])
+    return w
+
+
+def workload_desc(w: dict) -> str:
+    return (f"icosahedral level {w['level']}, RH54 + {w['ngauss']} Gaussian vortices (seed {w['ic_seed']}, "
+            f"amp U(-2,2), width {w['width']}), eps {w['eps']}, dt {w['dt']:g}, Omega 2pi"
+            + ("; stream function and velocity at every target after the steps" if w["psi_pass"] else ""))
 
 
 def mesh_sizes(level):
@@ -150,6 +180,16 @@ def mesh_sizes(level):
     nl = 20 * 4 ** level
     nall = 20 * (4 ** (level + 1) - 1) // 3
     return nv, nall, nl
+
+
+def bench_config(w: dict, world: int) -> dict:
+    """The `config` object of the line: identical in this arm and in the reference arm."""
+    nv, nall, nl = mesh_sizes(w["level"])
+    return {"workload": workload_desc(w), "targets": nv + nall, "sources": nl, "vertices": nv, "faces": nall,
+            "pairs_per_eval_algorithmic": (nv + nl) * nl, "pairs_per_eval_computed": (nv + nall) * nl,
+            "evals_per_step": 4, "eps": w["eps"], "dt": w["dt"],
+            "l2": "256 MiB buffer written between steps (inside the timed region)",
+            "parallelism": f"replicas x{world}"}
 
 
 # ------------------------------------------------------------------------------------------
@@ -166,19 +206,20 @@ def gpu_uuid(local_rank):
 
 
 class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms into a temporary file while a
+    timed region runs; stop() summarises them."""
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_id: str | None):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            fd, self.path = tempfile.mkstemp(prefix="lpm_clocks_", suffix=".csv")
+            self.fh = os.fdopen(fd, "w")
             cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
             if gpu_id:
                 cmd += ["-i", gpu_id]
-            self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(cmd, stdout=self.fh, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -194,7 +235,10 @@ class ClockSampler:
         self.fh.close()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        with open(self.path) as fh:
+            lines = fh.readlines()
+        os.unlink(self.path)
+        for line in lines:
             parts = [p.strip() for p in line.split(",")]
             if len(parts) < 9:
                 continue
@@ -214,6 +258,10 @@ class ClockSampler:
 # ------------------------------------------------------------------------------------------
 # our arm
 # ------------------------------------------------------------------------------------------
+def _events(torch):
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
 def run_ours(args, rank, world, local_rank):
     import numpy as np
     import torch
@@ -227,15 +275,18 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     ctx = bve.Context(local_rank, autotune=args.autotune)
     prec = P.FP32C if args.prec == "fp32c" else P.FP64
-    w = dict(WORKLOAD, level=args.level, dt=time_step(args.level))
-    nv, nall, nl = mesh_sizes(args.level)
+    w = workload(args.config, args.level)
+    level, eps = w["level"], w["eps"]
+    nv, nall, nl = mesh_sizes(level)
 
     t0 = time.time()
-    sphere = bve.BVESphere(w["seed_kind"], args.level, omega=w["omega"], layout="left", device=dev)
+    sphere = bve.BVESphere(w["seed_kind"], level, omega=w["omega"], layout="left", device=dev)
     ic = bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"])
-    sphere.init_vorticity(ic, ctx, flags=prec, eps=w["eps"])
+    sphere.init_vorticity(ic, ctx, flags=prec, eps=eps)
     torch.cuda.synchronize()
     t_init = time.time() - t0
+    if args.tree_only:
+        return tree_only(args, P, bve, torch, ctx, sphere, w, local_rank)
     s0 = clone_sphere(bve, sphere) if not args.no_tree and prec == P.FP32C and rank == 0 else None
     st = sphere.state()
 
@@ -249,9 +300,14 @@ def run_ours(args, rank, world, local_rank):
     # FP32 FMA-pipe peak at the current clock (roofline denominator)
     fma_peak_lane_ops, probes = fma_peak(P, local_rank)
 
+    # parity of the initial state (FP32C from init_vorticity, FP64 at the sampled targets)
+    parity = {}
+    if not args.no_parity and rank == 0:
+        parity["initial"] = oracle_parity(ctx, P, torch, np, sphere, w, prec, solve=False)
+
     # warm-up: builds the plan and captures the step graph
     t0 = time.time()
-    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=prec, eps=w["eps"])
+    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=prec, eps=eps)
     torch.cuda.synchronize()
     t_warm = time.time() - t0
 
@@ -264,11 +320,11 @@ def run_ours(args, rank, world, local_rank):
             ctx.timing(reset=True)
         barrier()
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(torch)
         e0.record(stream)
         for _ in range(nsteps):
             flush.zero_()
-            ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=w["eps"])
+            ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=eps)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -280,18 +336,20 @@ def run_ours(args, rank, world, local_rank):
         return el, pair
 
     sampler = ClockSampler(gpu_uuid(local_rank))
-    # 1) instrumented pass: per-launch CUDA events around the pair kernel (direct launches)
-    el_instr, (pair_ms, pair_n) = timed(args.steps, True)
-    # 2) headline pass: graph-replayed steps (the product's default path)
+    # 1) headline pass: graph-replayed steps (the product's default path)
     el_graph, _ = timed(args.steps, False)
+    # 2) instrumented pass: per-launch CUDA events around the pair kernel (direct launches)
+    n_instr = max(1, min(args.steps, 2))
+    el_instr, (pair_ms, pair_n) = timed(n_instr, True)
     clocks = sampler.stop()
     el_graph_max = rank_max(el_graph)
     el_instr_max = rank_max(el_instr)
 
     ms_per_step = el_graph_max / args.steps
     value = whole_job_rate(world, args.steps, el_graph_max)
-    pairs_alg = (nv + nl) * nl                 # algorithmic pairs per evaluation
-    pairs_done = (nv + nall) * nl              # computed (masked parents are targets too)
+    cfg = bench_config(w, world)
+    pairs_alg = cfg["pairs_per_eval_algorithmic"]
+    pairs_done = cfg["pairs_per_eval_computed"]
     pair_avg_ms = pair_ms / max(1, pair_n)
     achieved = pairs_alg / (pair_avg_ms * 1e-3) / 1e9
     peak_at_probe = fma_peak_lane_ops / OPS_PER_PAIR / 1e9
@@ -299,6 +357,7 @@ def run_ours(args, rank, world, local_rank):
     peak_nominal = sms * 128 * 2070e6 / OPS_PER_PAIR / 1e9
 
     # 3) end to end through the public API with host buffers
+    e2e_steps = args.e2e_steps if args.e2e_steps > 0 else max(3, args.steps // 2)
     names = ("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")
     host = {n: torch.empty(getattr(st, n).shape, dtype=torch.float64, pin_memory=True) for n in names}
     for n in names:
@@ -306,19 +365,20 @@ def run_ours(args, rank, world, local_rank):
     torch.cuda.synchronize()
     bytes_step = sum(host[n].numel() * 8 for n in names)
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+    e0, e1 = _events(torch)
     e0.record(stream)
-    for _ in range(args.e2e_steps):
+    for _ in range(e2e_steps):
         for n in names:
             getattr(st, n).copy_(host[n], non_blocking=True)
-        ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=w["eps"])
+        ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=eps)
         for n in names:
             host[n].copy_(getattr(st, n), non_blocking=True)
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
     el_e2e = rank_max(e0.elapsed_time(e1))
-    e2e_value = whole_job_rate(world, args.e2e_steps, el_e2e)
+    e2e_value = whole_job_rate(world, e2e_steps, el_e2e)
+    steps_done = max(1, args.warmup) + args.steps + n_instr + e2e_steps
 
     out = {
         "metric": "RK4 steps/s",
@@ -333,16 +393,9 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": "f32c" if prec == P.FP32C else "f64",
         "data": "synthetic (seeded RH54 + Gaussian vortices on a generated icosahedral mesh)",
-        "config": {
-            "workload": workload_desc(args.level),
-            "targets": nv + nall, "sources": nl, "vertices": nv, "faces": nall,
-            "pairs_per_eval_algorithmic": pairs_alg, "pairs_per_eval_computed": pairs_done,
-            "evals_per_step": 4,
-            "l2": "256 MiB buffer written between steps (inside the timed region)",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": cfg,
         "pair_interactions_per_s": world * 4 * pairs_alg / (ms_per_step * 1e-3),
-        "instrumented_ms_per_step": el_instr_max / args.steps,
+        "instrumented_ms_per_step": el_instr_max / n_instr,
         "roofline": {
             "bound": "fp32_fma_pipe",
             "kernel": "pairFP32C" if prec == P.FP32C else "pairFP64",
@@ -355,6 +408,7 @@ def run_ours(args, rank, world, local_rank):
             "probes": probes,
             "peak_nominal_2070MHz": peak_nominal,
             "frac_of_nominal": achieved / peak_nominal,
+            "frac_computed_pairs": pairs_done / (pair_avg_ms * 1e-3) / 1e9 / peak_at_probe,
             "pair_launch_ms_avg": pair_avg_ms,
             "pair_launches": pair_n,
             "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
@@ -363,7 +417,7 @@ def run_ours(args, rank, world, local_rank):
             "hbm": hbm_line(TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl), pair_avg_ms),
         },
         "e2e": {"value": e2e_value, "unit": "steps/s", "h2d_bytes_per_step": bytes_step,
-                "d2h_bytes_per_step": bytes_step, "steps": args.e2e_steps},
+                "d2h_bytes_per_step": bytes_step, "steps": e2e_steps},
         "gpu_launches": 13 * args.steps,
         "init_s": t_init,
         "warmup_s": t_warm,
@@ -371,37 +425,127 @@ def run_ours(args, rank, world, local_rank):
     if clocks:
         out["clocks"] = clocks
 
-    # 4) plain FP64 GPU path and FP32C accuracy on a target sample (same state)
-    if not args.no_fp64 and rank == 0:
-        out["fp64_gpu"] = fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step)
+    # 4) the closing stream-function + velocity evaluation at every target (vertex and face
+    #    evaluations; the first call builds their two plans, the second is timed)
+    solved = False
+    if w["psi_pass"]:
+        ms = []
+        for _ in range(2):
+            e0, e1 = _events(torch)
+            e0.record(stream)
+            sphere.solve(ctx, flags=prec, eps=eps, psi=True)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(rank_max(e0.elapsed_time(e1)))
+        psi_ms = ms[1]
+        out["psi_pass"] = {"ms": psi_ms, "first_call_ms": ms[0], "pairs": pairs_done,
+                           "computed_pairs_per_s": pairs_done / (psi_ms * 1e-3),
+                           "steps_done_before": steps_done,
+                           "config5_job_s": (10 * ms_per_step + psi_ms) * 1e-3,
+                           "note": "first_call_ms includes building the vertex and face plans; config5_job_s = "
+                                   "10 timed RK4 steps + this pass"}
+        solved = True
+    # 5) parity of the final state against the oracle
+    if not args.no_parity and rank == 0:
+        parity["final"] = oracle_parity(ctx, P, torch, np, sphere, w, prec, solve=not solved)
+        parity["final"]["after_steps"] = steps_done
+        out["oracle_parity"] = parity
+        out["oracle_rel_l2"] = {"fp32c_u": max(v["fp32c"]["u_l2"] for v in parity.values()),
+                                "fp32c_psi": max(v["fp32c"]["psi_l2"] for v in parity.values()),
+                                "fp64_u_maxrel": max(v["fp64"]["u_maxrel"] for v in parity.values()),
+                                "fp64_psi_maxrel": max(v["fp64"]["psi_maxrel"] for v in parity.values())}
 
-    # 4b) the tree code beside the direct sum (approximation; not the headline)
+    # 6) plain FP64 GPU path: sample rate here, full step vs sample at level 6
+    if not args.no_fp64 and rank == 0:
+        out["fp64_gpu"] = fp64_denominators(ctx, P, bve, torch, np, sphere, w, pairs_done, ms_per_step)
+
+    # 7) the tree code beside the direct sum (approximation; not the headline)
     if s0 is not None:
-        tree = tree_leg(P, bve, torch, ctx, s0, w["dt"], w["eps"], args.steps, flush, fma_peak_lane_ops)
+        tree = tree_leg(P, bve, torch, ctx, s0, w["dt"], eps, args.steps, flush, fma_peak_lane_ops,
+                        check_steps=1 if level >= 8 else 2)
         tree["speedup_vs_direct_fp32c"] = tree["rk4_steps_per_s"] / (args.steps / (el_graph * 1e-3))
         out["treecode"] = tree
         del s0
 
-    # 5) CPU baseline (rank 0, single GPU only)
+    # 8) CPU baseline (rank 0, single GPU only)
     if not args.no_cpu_baseline and rank == 0 and world == 1:
-        out["cpu_baseline"] = cpu_baseline(sphere.state(), sphere, w, args, pairs_done)
-    # 6) per-step error of the FP32C trajectory against the FP64 one
+        out["cpu_baseline"] = cpu_baseline(sphere, args, pairs_done, eps)
+    # 9) per-step error of the FP32C trajectory against the FP64 one
     if args.err_steps > 0 and rank == 0:
-        out["per_step_error"] = per_step_error(ctx, w, args.level, args.err_steps, dev, P, bve, torch)
+        out["per_step_error"] = per_step_error(ctx, w, args.err_steps, dev, P, bve, torch)
+    # 10) the level-7 single solve as a secondary leg of the level-8 line
+    if args.config == "c5" and not args.level and not args.no_secondary and prec == P.FP32C:
+        del sphere, st, flush
+        ctx.invalidate()
+        torch.cuda.empty_cache()
+        out["c2_level7"] = secondary_leg(args, ctx, P, bve, torch, dev, world, rank_max, fma_peak_lane_ops)
     if rank == 0:
         print(json.dumps(out), flush=True)
     ctx.close()
 
 
-def per_step_error(ctx, w, level, nsteps, dev, P, bve, torch):
+def secondary_leg(args, ctx, P, bve, torch, dev, world, rank_max, lane_ops):
+    """Config 2 (icosahedral level 7, RH54 + 3 vortices, eps 0): RK4 steps/s over --steps
+    graph-replayed steps after --warmup, and its pair kernel's roofline fraction."""
+    w = workload("c2")
+    s = bve.BVESphere(w["seed_kind"], w["level"], omega=w["omega"], layout="left", device=dev)
+    s.init_vorticity(bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"]), ctx, flags=P.FP32C, eps=w["eps"])
+    st = s.state()
+    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=P.FP32C, eps=w["eps"])
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    fn = lambda: ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=P.FP32C, eps=w["eps"])  # noqa: E731
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    el = rank_max(_timed_region(torch, stream, fn, args.steps, flush))
+    ctx.set_timing(True); ctx.timing()
+    _timed_region(torch, stream, fn, 2, flush)
+    pair_ms, pair_n = ctx.timing(); ctx.set_timing(False)
+    cfg = bench_config(w, world)
+    achieved = cfg["pairs_per_eval_algorithmic"] / (pair_ms / pair_n * 1e-3)
+    peak = lane_ops / OPS_PER_PAIR
+    return {"workload": cfg["workload"], "rk4_steps_per_s": whole_job_rate(world, args.steps, el),
+            "ms_per_step": el / args.steps, "steps": args.steps,
+            "pair_launch_ms_avg": pair_ms / pair_n, "roofline_frac": achieved / peak,
+            "pairs_per_eval_algorithmic": cfg["pairs_per_eval_algorithmic"]}
+
+
+def oracle_parity(ctx, P, torch, np, sphere, w, prec, solve=True):
+    """The sphere's velocity and stream function at every target (FP32C; evaluated here when
+    `solve`, else as init_vorticity or the stream-function pass left them) and the plain FP64
+    path at the sampled targets, against the CPU oracle on 4,096 random vertices and 4,096 random
+    leaf faces summed over all sources: relative L2 for FP32C, max |e| / max |ref| for FP64
+    (oracle/sampled_parity.py, the checker)."""
+    from oracle import sampled_parity as SP
+    t0 = time.time()
+    eps = w["eps"]
+    if solve:
+        sphere.solve(ctx, flags=prec, eps=eps, psi=True)
+    torch.cuda.synchronize()
+    vidx, fidx = SP.sample_targets(sphere.mesh["nverts"], sphere.mesh["fmask"], seed=w["level"])
+    vx, fx = sphere.physVerts.cpu().numpy(), sphere.physFaces.cpu().numpy()
+    z = sphere.relVortFaces.cpu().numpy()
+    got32 = (sphere.velocityVerts.cpu().numpy()[vidx], sphere.streamFnVerts.cpu().numpy()[vidx],
+             sphere.velocityFaces.cpu().numpy()[fidx], sphere.streamFnFaces.cpu().numpy()[fidx])
+    ref = SP.oracle_at(vx, fx, z, sphere.mesh["farea"], sphere.mesh["fmask"], vidx, fidx, eps=eps)
+    got64 = SP.gpu_fp64_at(ctx, P, torch, sphere.physVerts, sphere.physFaces, sphere.relVortFaces,
+                           sphere.faces_area, sphere.faces_mask, vidx, fidx, eps=eps)
+    return {"fp32c": SP.compare(got32, ref), "fp64": SP.compare(got64, ref),
+            "sample": f"{vidx.size} random vertices + {fidx.size} random leaf faces, all "
+                      f"{int((sphere.mesh['fmask'] == 0).sum())} sources, velocity and stream function",
+            "seconds": time.time() - t0}
+
+
+def per_step_error(ctx, w, nsteps, dev, P, bve, torch):
     """FP64 and FP32C trajectories from the same initial state; after every RK4 step the
     relative l2/linf of the FP32C velocity (vertices; leaf faces, area-weighted), relative
     vorticity and face positions against FP64, reduced on the device (lpm_errnorms)."""
     ic = bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"])
-    mesh = bve.build_mesh(w["seed_kind"], level)
+    mesh = bve.build_mesh(w["seed_kind"], w["level"])
     runs = {}
     for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C)):
-        s = bve.BVESphere(w["seed_kind"], level, omega=w["omega"], device=dev, mesh=mesh)
+        s = bve.BVESphere(w["seed_kind"], w["level"], omega=w["omega"], device=dev, mesh=mesh)
         s.init_vorticity(ic, ctx, flags=flags, eps=w["eps"])
         runs[name] = s
     a, b = runs["fp64"], runs["fp32c"]
@@ -428,37 +572,68 @@ def per_step_error(ctx, w, level, nsteps, dev, P, bve, torch):
             "note": "leaf faces area-weighted, masked parent faces skipped; vertices unweighted"}
 
 
-def fp64_sample(ctx, sphere, w, P, torch, np, pairs_done, ms_per_step, eps=0.0):
-    """Plain FP64 GPU path on 8192 sampled vertex targets; FP32C error on the same targets.
-    (Vertices: a face centre given as a distinct target would coincide with its own source.)"""
-    rng = np.random.default_rng(5)
-    leaf = np.flatnonzero(sphere.mesh["fmask"] == 0)
+def _fp64_sample_rate(ctx, P, torch, np, sphere, eps, ntargets=8192, seed=5):
+    """Plain FP64 GPU pair rate on ntargets random vertex targets over all leaf sources (one
+    evaluation after its plan is built); also returns the FP32C velocity's relative L2 distance
+    from FP64 on the same targets.  (Vertices: a face centre given as a distinct target would
+    coincide with its own source.)"""
+    rng = np.random.default_rng(seed)
     pts = sphere.physVerts
-    idx = torch.from_numpy(rng.choice(pts.shape[0], 8192, replace=False)).to(pts.device)
+    idx = torch.from_numpy(rng.choice(pts.shape[0], min(ntargets, pts.shape[0]), replace=False)).to(pts.device)
     tgt = pts[idx].contiguous()
     src = (sphere.physFaces, sphere.relVortFaces, sphere.faces_area, sphere.faces_mask)
     res = {}
     for name, flags in (("fp64", P.FP64), ("fp32c", P.FP32C | P.MESH_TARGETS)):
         ctx.velocity(tgt, *src, flags=flags, eps=eps)  # plan
         torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(torch)
         e0.record()
         u, _ = ctx.velocity(tgt, *src, flags=flags, eps=eps)
         e1.record()
         torch.cuda.synchronize()
         res[name] = (u.cpu().numpy(), e0.elapsed_time(e1))
-    ns = int(leaf.size)
-    rate64 = 8192 * ns / (res["fp64"][1] * 1e-3)
-    steps64 = rate64 / (4 * pairs_done)
+    ctx.invalidate()
+    ns = int((sphere.mesh["fmask"] == 0).sum())
+    rate64 = idx.numel() * ns / (res["fp64"][1] * 1e-3)
     u64, u32 = res["fp64"][0], res["fp32c"][0]
-    err = float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
-    return {"pairs_per_s": rate64, "steps_per_s_extrapolated": steps64,
+    return rate64, float(np.linalg.norm(u32 - u64) / np.linalg.norm(u64))
+
+
+def fp64_denominators(ctx, P, bve, torch, np, sphere, w, pairs_done, ms_per_step, full_level=6):
+    """The plain FP64 GPU path (the GPU oracle of the north star's "FP32C vs FP64" target).
+    A full FP64 step at this level takes minutes (level 8: ~15 min), so its steps/s is
+    extrapolated from the pair rate on 8,192 sampled vertex targets; the extrapolation is checked
+    by one full FP64 RK4 step at level `full_level` (graph-replayed, after a warm-up step) timed
+    beside the same kind of sample at that level."""
+    rate, err32 = _fp64_sample_rate(ctx, P, torch, np, sphere, w["eps"])
+    steps64 = rate / (4 * pairs_done)
+    wf = dict(w, level=full_level, dt=time_step(full_level))
+    s = bve.BVESphere(0, full_level, omega=w["omega"], layout="left", device=sphere.physVerts.device)
+    s.init_vorticity(bve.rh54_gaussians(w["ic_seed"], w["ngauss"], w["width"]), ctx, flags=P.FP32C, eps=w["eps"])
+    st = s.state()
+    ctx.rk4_step(st, wf["dt"], w["omega"], 1, flags=P.FP64, eps=w["eps"])  # plan + captured graph
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = _events(torch)
+    e0.record(stream)
+    ctx.rk4_step(st, wf["dt"], w["omega"], 1, flags=P.FP64, eps=w["eps"])
+    e1.record(stream)
+    torch.cuda.synchronize()
+    full_ms = e0.elapsed_time(e1)
+    nv6, nall6, nl6 = mesh_sizes(full_level)
+    full_rate = 4 * (nv6 + nall6) * nl6 / (full_ms * 1e-3)
+    rate6, _ = _fp64_sample_rate(ctx, P, torch, np, s, w["eps"])
+    ctx.invalidate()
+    return {"pairs_per_s": rate, "steps_per_s_extrapolated": steps64,
             "speedup_fp32c_vs_fp64": (1000.0 / ms_per_step) / steps64,
             "sample": "velocity at 8192 random vertex targets from all leaf sources, one evaluation",
-            "fp32c_vs_fp64_velocity_rel_l2": err}
+            "fp32c_vs_fp64_velocity_rel_l2": err32,
+            "full_step_check": {"level": full_level, "fp64_rk4_step_ms": full_ms,
+                                "computed_pairs_per_s": full_rate, "sample_pairs_per_s": rate6,
+                                "sample_over_full": rate6 / full_rate}}
 
 
-def cpu_baseline(st, sphere, w, args, pairs_done):
+def cpu_baseline(sphere, args, pairs_done, eps):
     """CPU oracle on the host cores, bounded sample of the same evaluation."""
     import numpy as np
     from oracle import oracle as O
@@ -466,14 +641,14 @@ def cpu_baseline(st, sphere, w, args, pairs_done):
     vx = sphere.physVerts.cpu().numpy(); fx = sphere.physFaces.cpu().numpy()
     z = sphere.relVortFaces.cpu().numpy(); a = sphere.faces_area.cpu().numpy(); m = sphere.mesh["fmask"]
     ns = int((m == 0).sum())
-    tg = np.concatenate([vx, fx])
+    tg = np.concatenate([vx, fx[m == 0]])
     rng = np.random.default_rng(11)
     n = 256
     t = 0.0
     while True:
         sel = tg[rng.choice(tg.shape[0], n, replace=False)]
         t0 = time.time()
-        O.velocity_distinct(sel, fx, z, a, m)
+        O.velocity_distinct(sel, fx, z, a, m, eps=eps)
         t = time.time() - t0
         if t > args.cpu_seconds / 4 or n >= tg.shape[0] // 2:
             break
@@ -482,13 +657,31 @@ def cpu_baseline(st, sphere, w, args, pairs_done):
     n = min(tg.shape[0], max(n, int(n * args.cpu_seconds / max(t, 1e-3))))
     sel = tg[rng.choice(tg.shape[0], n, replace=False)]
     t0 = time.time()
-    O.velocity_distinct(sel, fx, z, a, m)
+    O.velocity_distinct(sel, fx, z, a, m, eps=eps)
     t = time.time() - t0
     rate = n * ns / t
     return {"value": rate / (4 * pairs_done), "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
             "pairs_per_s": rate,
-            "sample": f"FP64 velocity at {n} random targets from all {ns} leaf sources, {t:.1f} s, "
+            "sample": f"FP64 velocity at {n} random vertex / leaf-face points from all {ns} leaf sources, {t:.1f} s, "
                       f"extrapolated to one RK4 step (4 evaluations of {pairs_done} pairs)"}
+
+
+def tree_only(args, P, bve, torch, ctx, s, w, local_rank):
+    """--tree-only: the tree-code leg alone on this workload (profiling the tree path)."""
+    dev = s.physVerts.device
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    lane_ops, probes = fma_peak(P, local_rank)
+    sampler = ClockSampler(gpu_uuid(local_rank))
+    ctx.rk4_step(clone_sphere(bve, s).state(), w["dt"], w["omega"], max(1, args.warmup),
+                 flags=P.FP32C | P.TREECODE, eps=w["eps"])
+    tree = tree_leg(P, bve, torch, ctx, s, w["dt"], w["eps"], args.steps, flush, lane_ops, check_steps=0)
+    clocks = sampler.stop()
+    print(json.dumps({"metric": "RK4 steps/s (tree code)", "value": tree["rk4_steps_per_s"], "unit": "steps/s",
+                      "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                      "dtype": "f32c", "data": "synthetic",
+                      "config": {"workload": workload_desc(w) + "; tree code only"},
+                      "treecode": tree, "probes": probes, "clocks": clocks}), flush=True)
+    ctx.close()
 
 
 # ------------------------------------------------------------------------------------------
@@ -649,98 +842,6 @@ def tree_leg(P, bve, torch, ctx, s0, dt, eps, steps, flush, lane_ops, check_step
     }
 
 
-def run_large(args, rank, world, local_rank):
-    """Config 5: icosahedral level 8 (655,362 vertices, 1,747,620 faces, 1,310,720 sources), RH54 + 8
-    Gaussian vortices, eps = 0.01, RK4 steps, then the stream function at all targets."""
-    import numpy as np
-    import torch
-
-    import lpmkokkos_gb300 as P
-    from lpmkokkos_gb300 import bve
-    P.build()
-    torch.cuda.set_device(local_rank)
-    dev = torch.device("cuda", local_rank)
-    ctx = bve.Context(local_rank, autotune=args.autotune)
-    level, eps = 8, 0.01
-    dt = time_step(level)
-    nv, nall, nl = mesh_sizes(level)
-    t0 = time.time()
-    s = bve.BVESphere(0, level, device=dev)
-    s.init_vorticity(bve.rh54_gaussians(SEED_BASE + 5, 8), ctx, flags=P.FP32C, eps=eps)
-    torch.cuda.synchronize()
-    t_init = time.time() - t0
-    if args.tree_only:
-        flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
-        lane_ops, probes = fma_peak(P, local_rank)
-        sampler = ClockSampler(gpu_uuid(local_rank))
-        ctx.rk4_step(clone_sphere(bve, s).state(), dt, 2 * math.pi, max(1, args.warmup),
-                     flags=P.FP32C | P.TREECODE, eps=eps)
-        tree = tree_leg(P, bve, torch, ctx, s, dt, eps, args.steps, flush, lane_ops, check_steps=0)
-        clocks = sampler.stop()
-        if rank == 0:
-            print(json.dumps({"metric": "RK4 steps/s (tree code)", "value": tree["rk4_steps_per_s"],
-                              "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-                              "higher_is_better": True, "dtype": "f32c", "data": "synthetic",
-                              "config": {"workload": f"icosahedral level 8, RH54 + 8 Gaussian vortices, eps {eps}, "
-                                                     f"dt {dt:g}; tree code only"},
-                              "treecode": tree, "probes": probes, "clocks": clocks}), flush=True)
-        ctx.close()
-        return
-    s0 = clone_sphere(bve, s) if not args.no_tree else None
-    st = s.state()
-    ctx.rk4_step(st, dt, 2 * math.pi, max(1, args.warmup), flags=P.FP32C, eps=eps)
-    torch.cuda.synchronize()
-    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
-    stream = torch.cuda.current_stream()
-    ctx.set_timing(True); ctx.timing()
-    sampler = ClockSampler(gpu_uuid(local_rank))
-    el = _timed_region(torch, stream, lambda: ctx.rk4_step(st, dt, 2 * math.pi, 1, flags=P.FP32C, eps=eps),
-                       args.steps, flush)
-    clocks = sampler.stop()
-    pair_ms, pair_n = ctx.timing(); ctx.set_timing(False)
-    el = max_over_ranks(el, world, dev)
-    # stream function (and velocity) at every vertex and face
-    e0 = torch.cuda.Event(enable_timing=True); e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    s.solve(ctx, flags=P.FP32C, eps=eps, psi=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    psi_ms = e0.elapsed_time(e1)
-    lane_ops, probes = fma_peak(P, local_rank)
-    pairs_alg = (nv + nl) * nl
-    achieved = pairs_alg / (pair_ms / pair_n * 1e-3) / 1e9
-    peak = lane_ops / OPS_PER_PAIR / 1e9
-    fp64 = fp64_sample(ctx, s, dict(WORKLOAD, level=level, dt=dt), P, torch, np, (nv + nall) * nl,
-                       el / args.steps, eps=eps)
-    tree = None
-    if s0 is not None:
-        tree = tree_leg(P, bve, torch, ctx, s0, dt, eps, args.steps, flush, lane_ops)
-        tree["speedup_vs_direct_fp32c"] = tree["rk4_steps_per_s"] / whole_job_rate(1, args.steps, el)
-        tree["speedup_vs_direct_fp64_gpu"] = (tree["rk4_steps_per_s"] / fp64["steps_per_s_extrapolated"]
-                                              if fp64 and fp64.get("steps_per_s_extrapolated") else None)
-        del s0
-    out = {
-        "metric": "pair-interactions/s", "value": world * 4 * pairs_alg * args.steps / (el * 1e-3),
-        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": el / args.steps, "rk4_steps_per_s": whole_job_rate(world, args.steps, el),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32c",
-        "data": "synthetic (seeded RH54 + 8 Gaussian vortices on a generated icosahedral mesh)",
-        "config": {"workload": f"icosahedral level 8, RH54 + 8 Gaussian vortices (seed {SEED_BASE + 5}), "
-                               f"eps {eps}, dt {dt:g}, Omega 2pi; stream function at all targets after the steps",
-                   "targets": nv + nall, "sources": nl, "autotune": bool(args.autotune)},
-        "psi_and_velocity_all_targets_ms": psi_ms,
-        "roofline": {"bound": "fp32_fma_pipe", "kernel": "pairFP32C", "achieved": achieved, "peak": peak,
-                     "unit": "Gpair/s", "frac": achieved / peak, "pair_launch_ms_avg": pair_ms / pair_n,
-                     "peak_source": "FP32 FMA-pipe probe (FFMA / FFMA2, the larger) / 13 lane-ops per pair",
-                     "probes": probes, "traffic": TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl),
-                     "hbm": hbm_line(TRAFFIC_BYTES_PER_PARTICLE * (nv + nall + nl), pair_ms / pair_n)},
-        "fp64_gpu": fp64, "init_s": t_init, "clocks": clocks, "treecode": tree,
-    }
-    if rank == 0:
-        print(json.dumps(out), flush=True)
-    ctx.close()
-
-
 COMPUTED_PAIR_RATE = 2.2e12  # FP32C pairs/s incl. masked-parent targets (measured, icos L7)
 
 
@@ -855,6 +956,7 @@ def run_server(args, rank, world, local_rank):
     serial64 = sum((sp["nsteps"] * 4 + 1) * computed_pairs(sp["seed"], sp["level"]) for sp in specs) / r64
     solve_steps = st["solve_steps"] - base["solve_steps"]
     pairs = st["pairs"] - base["pairs"]
+    tree_equiv = st["tree_equiv_pairs"] - base["tree_equiv_pairs"]
     nearest = lambda q: float(np.sort(lat)[max(0, math.ceil(q * n) - 1)])  # noqa: E731
     kinds_desc = "icosahedral" if args.kinds == "icos" else "icosahedral or cubed sphere"
     out = {
@@ -872,8 +974,9 @@ def run_server(args, rank, world, local_rank):
                       "mean_wait": float(waits.mean())},
         "latency_by_level": by_level,
         "solve_steps_per_s": solve_steps / wall, "computed_pairs_per_s": pairs / wall,
-        **({"computed_pairs_note": "tree-code requests count the direct-sum pairs their evaluations replace"}
-           if args.tree else {}),
+        **({"tree_equivalent_pairs_per_s": tree_equiv / wall,
+            "tree_equivalent_pairs_note": "tree-code requests: the direct-sum pairs their evaluations replace "
+                                          "(work equivalent, not computed)"} if args.tree else {}),
         "server_iterations": st["steps_run"] - base["steps_run"], "max_running": st["max_running_seen"],
         "wall_s": wall, "mix_equals_alone": bool(same), "clocks": clocks,
         "serial_fp64_gpu": {"pairs_per_s": r64, "seconds": serial64, "requests_per_s": n / serial64,
@@ -889,44 +992,69 @@ def run_server(args, rank, world, local_rank):
 # reference arm: the reference path's CPU implementation (oracle port) on the host cores
 # ------------------------------------------------------------------------------------------
 def run_reference(args, rank, world):
+    """The reference path's CPU implementation (the oracle port: the reference needs Kokkos /
+    Trilinos, MPI and VTK, none of which exist here) on all host cores, on the same workload and
+    `config` as our arm.  A full evaluation at level 8 takes ~10 min on 16 cores, so each step is
+    one FP64 evaluation at a bounded random sample of vertex / face targets over all sources
+    (~3 s), extrapolated to a full RK4 step (4 evaluations); one full evaluation at level 6 is
+    timed beside a sample there to show the extrapolation holds."""
     if rank != 0:
         return
     import numpy as np
     from oracle import oracle as O
     O.build()
-    w = dict(WORKLOAD, level=args.level)
-    m = O.mesh(w["seed_kind"], args.level)
+    w = workload(args.config if args.config in ("c2", "c5") else "c5", args.level)
+    eps = w["eps"]
+    m = O.mesh(w["seed_kind"], w["level"])
     z = O.rh54_gaussians(m["fx"], w["ic_seed"], w["ngauss"], w["width"])
-    nv, nall, nl = mesh_sizes(args.level)
-    pairs_done = (nv + nall) * nl
+    cfg = bench_config(w, world)
+    nl, pairs_done = cfg["sources"], cfg["pairs_per_eval_computed"]
     tg = np.concatenate([m["vx"], m["fx"]])
     rng = np.random.default_rng(3)
+
+    def sample_rate(mesh, zz, targets, n):
+        sel = targets[rng.choice(targets.shape[0], n, replace=False)]
+        t0 = time.time()
+        O.velocity_distinct(sel, mesh["fx"], zz, mesh["farea"], mesh["fmask"], eps=eps)
+        return n * int((mesh["fmask"] == 0).sum()) / (time.time() - t0)
+
     # size one sample to ~3 s of CPU work
     n = 256
-    sel = tg[rng.choice(tg.shape[0], n, replace=False)]
-    t0 = time.time(); O.velocity_distinct(sel, m["fx"], z, m["farea"], m["fmask"]); t = time.time() - t0
-    n = max(256, min(tg.shape[0], int(n * 3.0 / max(t, 1e-3))))
+    r = sample_rate(m, z, tg, n)
+    n = max(256, min(tg.shape[0], int(3.0 * r / nl)))
     rates = []
     for k in range(args.warmup + args.steps):
-        sel = tg[rng.choice(tg.shape[0], n, replace=False)]
-        t0 = time.time()
-        O.velocity_distinct(sel, m["fx"], z, m["farea"], m["fmask"])
-        t = time.time() - t0
+        rk = sample_rate(m, z, tg, n)
         if k >= args.warmup:
-            rates.append(n * nl / t)
+            rates.append(rk)
     rate = statistics.median(rates)
     steps = rate / (4 * pairs_done)
-    sample = (f"each step: FP64 velocity at {n} random vertex/face targets from all {nl} leaf sources, "
+    # the extrapolation checked: one full evaluation at level 6 (or the workload's, if lower)
+    # beside a sample there
+    lf = min(6, w["level"])
+    mf = O.mesh(0, lf)
+    zf = O.rh54_gaussians(mf["fx"], w["ic_seed"], w["ngauss"], w["width"])
+    t0 = time.time()
+    O.velocity(mf["vx"], mf["fx"], zf, mf["farea"], mf["fmask"], eps=eps)
+    full_s = time.time() - t0
+    nvf, nallf, nlf = mesh_sizes(lf)
+    full_rate = (nvf + nallf) * nlf / full_s
+    tgf = np.concatenate([mf["vx"], mf["fx"]])
+    ratef = sample_rate(mf, zf, tgf, min(tgf.shape[0], max(256, int(3.0 * rate / nlf))))
+    sample = (f"each step: FP64 velocity at {n} random vertex / face targets from all {nl} leaf sources, "
               f"extrapolated to one RK4 step (4 evaluations of {pairs_done} pairs)")
     out = {
         "impl": "reference",
         "metric": "RK4 steps/s", "value": steps, "unit": "steps/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1000.0 / steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (same seeded workload)",
-        "config": {"workload": workload_desc(args.level), "targets": nv + nall, "sources": nl,
-                   "implementation": "CPU oracle: OpenMP restatement of the reference BVE path "
-                                     "(Kokkos reference not buildable: no Kokkos/Trilinos/MPI/VTK)"},
+        "config": cfg,
+        "steps_kind": "sampled evaluations (each extrapolated to one RK4 step)",
+        "implementation": "CPU oracle: OpenMP restatement of the reference BVE path (the Kokkos reference is not "
+                          "buildable here: no Kokkos/Trilinos/MPI/VTK)",
         "pair_interactions_per_s": rate,
+        "full_evaluation_check": {"level": lf, "seconds": full_s, "pairs_per_s": full_rate,
+                                  "sample_pairs_per_s": ratef, "sample_over_full": ratef / full_rate},
         "cpu_baseline": {"value": steps, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
                          "sample": sample},
         "e2e": {"value": steps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -950,7 +1078,7 @@ def main():
             torch.cuda.set_device(local_rank)
         dist.init_process_group(backend=backend)
     try:
-        {"c2": run_ours, "c3": run_ensemble, "c4": run_server, "c5": run_large}[args.config](args, rank, world, local_rank)
+        {"c2": run_ours, "c3": run_ensemble, "c4": run_server, "c5": run_ours}[args.config](args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as dist

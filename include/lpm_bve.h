@@ -15,7 +15,9 @@
  *  - Work is queued on `stream` and returns without synchronising, except the first
  *    call for a new problem geometry (new pointers, sizes, strides or mask), which
  *    builds a plan: it copies positions and the mask to the host, synchronising the
- *    stream once.  The plan is reused by later calls with the same geometry.
+ *    stream once.  The plan is reused by later calls with the same geometry: a context
+ *    keeps the plans of its four most recent lpm_bve_velocity geometries (e.g. the vertex
+ *    and the face evaluation of one mesh) and of its last lpm_bve_rk4_step state.
  *  - Every function returns LPM_OK (0) or a negative status; lpm_bve_last_error()
  *    gives the message.  One context per host thread / stream.
  */

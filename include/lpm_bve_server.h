@@ -51,11 +51,13 @@ typedef struct {
   int64_t submitted, completed, failed, cancelled, running, queued;
   int64_t steps_run;          /* RK4 steps launched over size classes (one step of one class) */
   int64_t solve_steps;        /* sum over solves of RK4 steps taken */
-  double pairs;               /* target-source pairs evaluated (incl. masked-parent targets);
-                                 a tree-code request counts the direct-sum pairs it replaces */
+  double pairs;               /* target-source pairs evaluated by the direct sum (incl. masked-parent
+                                 targets); tree-code requests are not counted here */
   double busy_s;              /* wall time with at least one solve running */
   size_t reserved_bytes, budget_bytes;
   int max_running_seen;
+  double tree_equiv_pairs;    /* tree-code requests: the direct-sum pairs their evaluations replace
+                                 (work equivalent, not work done) */
 } lpm_bve_server_counters;
 
 int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out);

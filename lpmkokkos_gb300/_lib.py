@@ -81,7 +81,8 @@ class ServerCounters(ctypes.Structure):
     _fields_ = [("submitted", c_i64), ("completed", c_i64), ("failed", c_i64), ("cancelled", c_i64),
                 ("running", c_i64), ("queued", c_i64), ("steps_run", c_i64), ("solve_steps", c_i64),
                 ("pairs", ctypes.c_double), ("busy_s", ctypes.c_double), ("reserved_bytes", ctypes.c_size_t),
-                ("budget_bytes", ctypes.c_size_t), ("max_running_seen", ctypes.c_int)]
+                ("budget_bytes", ctypes.c_size_t), ("max_running_seen", ctypes.c_int),
+                ("tree_equiv_pairs", ctypes.c_double)]
 
 
 NORMS_ABS_LINF = 1 << 0

@@ -13,6 +13,7 @@
 #include "engine.hpp"
 #include "engine_core.hpp"
 #include "tree_eval.hpp"
+#include "nvtx.hpp"
 
 #include <algorithm>
 #include <array>
@@ -349,8 +350,13 @@ void refreshTables(Batch& B, cudaStream_t s) {
 }
 
 // One evaluation of the direct sums for every solve of the batch.
-void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s) {
-  LPM_CUDA(launchPrep(B.stageDev, B.prepMap, B.nPrepBlocks, prepStage, B.prec, B.counter, s));
+void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s,
+                 const EvalNames* names) {
+  {
+    std::unique_ptr<NvtxRange> r(names ? new NvtxRange(names->prep) : nullptr);
+    LPM_CUDA(launchPrep(B.stageDev, B.prepMap, B.nPrepBlocks, prepStage, B.prec, B.counter, s));
+  }
+  std::unique_ptr<NvtxRange> pairRange(names ? new NvtxRange(names->pair) : nullptr);
   if (B.treeMode) {  // tree code: per solve octree, lists and gathered pair kernel; one epilogue
     const size_t n = B.solves.size();
     B.treeStageHost.resize(n);
@@ -370,8 +376,10 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
       }
       B.treeStageHost[m] = st;
     }
+    pairRange.reset();
     // (the next evaluation's first octree build synchronises before this host table changes)
     LPM_CUDA(cudaMemcpyAsync(B.treeStageDev, B.treeStageHost.data(), n * sizeof(SolveStage), cudaMemcpyHostToDevice, s));
+    std::unique_ptr<NvtxRange> epi(names ? new NvtxRange(names->epilogue) : nullptr);
     LPM_CUDA(launchEpilogue(B.treeStageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
     return;
   }
@@ -387,16 +395,30 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
     LPM_CUDA(cudaEventRecord(e1, s));
     B.timer->pending.emplace_back(e0, e1);
   }
+  pairRange.reset();
+  std::unique_ptr<NvtxRange> epi(names ? new NvtxRange(names->epilogue) : nullptr);
   LPM_CUDA(launchEpilogue(B.stageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
 }
 
-// One RK4 step (src/LpmBVERK4_Impl.hpp:42-130) for every solve of the batch.
+// One RK4 step (src/LpmBVERK4_Impl.hpp:42-130) for every solve of the batch, its launches named
+// after the reference's (:64-126; vertex and face work is fused into one launch here).
 void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s) {
-  enqueueEval(B, 1, 1, false, true, s);   // RK4-2: x + x_1/2
-  enqueueEval(B, 2, 2, false, true, s);   // RK4-3: x + x_2/2
-  enqueueEval(B, 3, 3, false, true, s);   // RK4-4: x + x_3
-  LPM_CUDA(launchCombine(B.stageDev, B.slotMap, B.nSlotBlocks, quirk, renorm, s));
-  enqueueEval(B, 0, 0, false, true, s);   // RK4-0: u at the new positions
+  static const EvalNames kStage[4] = {
+      {"RK4-0 positions", "RK4-0 vertex velocity + face velocity", "RK4-0 velocity out"},
+      {"RK4-2 vertex and face update (x + x1/2)", "RK4-2 vertex velocity + face velocity",
+       "RK4-2 vertex vorticity + face vorticity"},
+      {"RK4-3 vertex and face update (x + x2/2)", "RK4-3 vertex velocity + face velocity",
+       "RK4-3 vertex vorticity + face vorticity"},
+      {"RK4-4 vertex and face update (x + x3)", "RK4-4 vertex velocity + face velocity",
+       "RK4-4 vertex vorticity + face vorticity"}};
+  enqueueEval(B, 1, 1, false, true, s, &kStage[1]);   // RK4-2: x + x_1/2
+  enqueueEval(B, 2, 2, false, true, s, &kStage[2]);   // RK4-3: x + x_2/2
+  enqueueEval(B, 3, 3, false, true, s, &kStage[3]);   // RK4-4: x + x_3
+  {
+    NvtxRange r("RK4 vertex update + face update");
+    LPM_CUDA(launchCombine(B.stageDev, B.slotMap, B.nSlotBlocks, quirk, renorm, s));
+  }
+  enqueueEval(B, 0, 0, false, true, s, &kStage[0]);   // RK4-0: u at the new positions
 }
 
 }  // namespace lpm
@@ -412,8 +434,10 @@ struct lpm_bve_ctx {
   std::string err;
   cudaStream_t capture = nullptr;  // private stream for graph capture
   // cached plans
-  std::unique_ptr<lpm::Batch> velBatch;
-  lpm::Mode velMode = lpm::Mode::Distinct;
+  // velocity plans, most recently used first: BVESphere::init_vorticity and every stream-function
+  // diagnostic alternate a vertex (distinct) and a face (collocated) evaluation on the same
+  // sources, so both plans stay cached instead of being rebuilt call after call
+  std::vector<std::unique_ptr<lpm::Batch>> velPlans;
   std::unique_ptr<lpm::Batch> rkBatch;
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
   lpm::PairShape forced{0, 0, 0, 0};       // FP32C launch shape chosen by the caller (threads 0 = none)
@@ -421,6 +445,8 @@ struct lpm_bve_ctx {
   double* normScratch = nullptr;  // device: block partials + result of lpm_errnorms
   double* normHost = nullptr;     // pinned: result of lpm_errnorms
 };
+
+constexpr size_t kVelPlans = 4;  // velocity plans a context keeps
 
 struct lpm_bve_ensemble {
   lpm_bve_ctx* ctx = nullptr;
@@ -653,7 +679,7 @@ int lpm_bve_ctx_destroy(lpm_bve_ctx* ctx) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
   cudaSetDevice(ctx->dev.device);
   cudaDeviceSynchronize();
-  ctx->velBatch.reset();
+  ctx->velPlans.clear();
   ctx->rkBatch.reset();
   if (ctx->capture) cudaStreamDestroy(ctx->capture);
   if (ctx->normScratch) cudaFree(ctx->normScratch);
@@ -669,7 +695,7 @@ int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx) {
   try {
     setDevice(ctx);
     LPM_CUDA(cudaDeviceSynchronize());
-    ctx->velBatch.reset();
+    ctx->velPlans.clear();
     ctx->rkBatch.reset();
   } catch (const Error& e) {
     return handle(ctx, e);
@@ -829,14 +855,23 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     const bool skip = colloc && (flags & LPM_BVE_SKIP_MASKED_TARGETS);
     const bool tree = flags & LPM_BVE_TREECODE;
     if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "velocity: the tree code needs LPM_BVE_FP32C");
-    if (!sameGeometry(ctx, ctx->velBatch.get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
-      if (ctx->velBatch) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
-      ctx->velBatch.reset();
+    auto& plans = ctx->velPlans;
+    bool hit = false;
+    for (size_t k = 0; k < plans.size() && !hit; ++k)
+      if (sameGeometry(ctx, plans[k].get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
+        std::rotate(plans.begin(), plans.begin() + k, plans.begin() + k + 1);  // to the front
+        hit = true;
+      }
+    if (!hit) {
+      if (plans.size() >= kVelPlans) {
+        LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the plan dropped here
+        plans.pop_back();
+      }
       const bool precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
-      ctx->velBatch = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s);
-      ctx->velBatch->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
+      plans.insert(plans.begin(), makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s));
+      plans.front()->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
-    Batch& B = *ctx->velBatch;
+    Batch& B = *plans.front();
     // Distinct targets are arbitrary points unless the caller says they are mesh points.
     B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
@@ -845,7 +880,16 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     bindIO(B, 0, io, 0.0, 0.0, s, changed);
     if (changed) refreshTables(B, s);
     B.timer = ctx->timer.get();
-    enqueueEval(B, 0, 0, wantPsi, wantVel, s);
+    // the reference's functor names: BVE{Vertex,Face}{Velocity,StreamFn,Solve}
+    // (src/LpmBVEKernels.hpp:110-305)
+    static const EvalNames kVel[2][3] = {
+        {{"BVEVertexVelocity positions", "BVEVertexVelocity", "BVEVertexVelocity out"},
+         {"BVEVertexStreamFn positions", "BVEVertexStreamFn", "BVEVertexStreamFn out"},
+         {"BVEVertexSolve positions", "BVEVertexSolve", "BVEVertexSolve out"}},
+        {{"BVEFaceVelocity positions", "BVEFaceVelocity", "BVEFaceVelocity out"},
+         {"BVEFaceStreamFn positions", "BVEFaceStreamFn", "BVEFaceStreamFn out"},
+         {"BVEFaceSolve positions", "BVEFaceSolve", "BVEFaceSolve out"}}};
+    enqueueEval(B, 0, 0, wantPsi, wantVel, s, &kVel[mode == Mode::Distinct ? 0 : 1][wantPsi ? (wantVel ? 2 : 1) : 0]);
     B.timer = nullptr;
   } catch (const Error& e) {
     return handle(ctx, e);
@@ -858,6 +902,7 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
 int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, double Omega, int nsteps, unsigned flags,
                      double eps, lpm_stream_t stream) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
+  NvtxRange region("BVERK4::advance_timestep");
   try {
     setDevice(ctx);
     cudaStream_t s = (cudaStream_t)stream;
@@ -1100,6 +1145,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
 
 int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* Omega, int nsteps, lpm_stream_t stream) {
   if (!E || !E->ctx) return LPM_ERR_INVALID_ARGUMENT;
+  NvtxRange region("BVERK4::advance_timestep (ensemble)");
   lpm_bve_ctx* ctx = E->ctx;
   try {
     setDevice(ctx);

@@ -250,7 +250,10 @@ int chunkLength(int ns, int srcTile);
 // Allocates a plan's partial buffer on first use; builds items, block maps and device tables.
 void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s);
 void refreshTables(Batch& B, cudaStream_t s);
-void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s);
+struct EvalNames;
+// names: profiler range names of the evaluation's launches (nullptr: no ranges)
+void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s,
+                 const EvalNames* names = nullptr);
 void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
 
 // Snapshot file of a state held in host row-major arrays (snapshot.cpp).

@@ -313,8 +313,11 @@ int readInt(const int* d, cudaStream_t s) {
   return h;
 }
 
-std::once_flag g_tablesOnce;
-cudaError_t g_tablesErr = cudaSuccess;
+// __constant__ memory is per device: the tables are uploaded once on every device that builds
+// an octree, with that device current.
+constexpr int kMaxDevices = 64;
+std::once_flag g_tablesOnce[kMaxDevices];
+cudaError_t g_tablesErr[kMaxDevices];
 
 }  // namespace
 
@@ -357,13 +360,16 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
                    cudaStream_t s, bool hostBox) {
   if (maxDepth < 1 || maxDepth > kOctreeMaxDepth) fail(LPM_ERR_INVALID_ARGUMENT, "octree depth must be 1..%d", kOctreeMaxDepth);
   if (npts <= 0 || npts > INT32_MAX) fail(LPM_ERR_INVALID_ARGUMENT, "octree: 1..2^31-1 points");
-  std::call_once(g_tablesOnce, [] {
+  int dev = 0;
+  check(cudaGetDevice(&dev), "device query");
+  if (dev < 0 || dev >= kMaxDevices) fail(LPM_ERR_NOT_SUPPORTED, "octree: device ordinal %d >= %d", dev, kMaxDevices);
+  std::call_once(g_tablesOnce[dev], [dev] {
     signed char tp[8][27], tc[8][27];
     makeTables(tp, tc);
-    g_tablesErr = cudaMemcpyToSymbol(cParent, tp, sizeof(tp));
-    if (g_tablesErr == cudaSuccess) g_tablesErr = cudaMemcpyToSymbol(cChild, tc, sizeof(tc));
+    g_tablesErr[dev] = cudaMemcpyToSymbol(cParent, tp, sizeof(tp));
+    if (g_tablesErr[dev] == cudaSuccess) g_tablesErr[dev] = cudaMemcpyToSymbol(cChild, tc, sizeof(tc));
   });
-  check(g_tablesErr, "tables");
+  check(g_tablesErr[dev], "tables");
   depth = maxDepth;
   n = npts;
   const unsigned nb = blocksFor(n);

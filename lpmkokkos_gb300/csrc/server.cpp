@@ -622,7 +622,7 @@ void treeRequest(lpm_bve_server* S, lpm_bve_ctx* ctx, cudaStream_t ts, Req* r) {
     r->state = LPM_REQ_RUNNING;
     r->tStart = Clock::now();
     r->pairsPerEval = (double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl;
-    S->st.pairs += r->pairsPerEval;
+    S->st.tree_equiv_pairs += r->pairsPerEval;
   }
   const unsigned fl = S->flags;  // FP32C | TREECODE and the RK4 options
   lpm_points tv{d + L.vx, M.nv, 3, 1};
@@ -656,7 +656,7 @@ void treeRequest(lpm_bve_server* S, lpm_bve_ctx* ctx, cudaStream_t ts, Req* r) {
   S->inflight -= 1;
   S->st.completed += 1;
   S->st.solve_steps += r->r.nsteps;
-  S->st.pairs += 4.0 * r->r.nsteps * r->pairsPerEval;  // the direct-sum pairs the steps replace
+  S->st.tree_equiv_pairs += 4.0 * r->r.nsteps * r->pairsPerEval;  // the direct-sum pairs the steps replace
   S->latencies.push_back(seconds(r->tSubmit, r->tDone));
   S->cvDone.notify_all();
   S->cvPrep.notify_all();

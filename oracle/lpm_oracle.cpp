@@ -504,6 +504,19 @@ void oracle_velocity_distinct(const double* tx, long nt, const double* sx, const
   for (long i = 0; i < nt; ++i) reduceTarget(T[i], -1, S, zeta, area, mask, ns, e2, u + 3*i, psi ? psi + i : nullptr);
 }
 
+// Collocated sums at a subset of the faces: for each listed face index k the body of
+// BVEFaceVelocity / BVEFaceStreamFn (src/LpmBVEKernels.hpp:263-305) -- every unmasked face j
+// except j == k.  Each target of the reference's functor is independent of the others, so a
+// subset gives the same values as the full launch at those faces.
+void oracle_velocity_faces(const long* idx, long nt, const double* fx, const double* zeta, const double* area,
+                           const unsigned char* mask, long nf, double eps, double* u, double* psi) {
+  const V3* S = reinterpret_cast<const V3*>(fx);
+  const Real e2 = eps*eps;
+  #pragma omp parallel for schedule(dynamic, 16)
+  for (long i = 0; i < nt; ++i)
+    reduceTarget(S[idx[i]], idx[i], S, zeta, area, mask, nf, e2, u + 3*i, psi ? psi + i : nullptr);
+}
+
 // ---------------------------------------------------------------------------
 // RK4: BVERK4::advance_timestep (src/LpmBVERK4_Impl.hpp:42-130) with BVERK4Update (:11-39),
 // KokkosBlas::scal / update (x_k = dt*u; work = x + c*x_k) and BVEVorticityTendency

@@ -70,6 +70,8 @@ def _setup(L):
     L.oracle_mesh_free.argtypes = [ctypes.POINTER(_Mesh)]
     L.oracle_bve_velocity.argtypes = [D, ctypes.c_long, D, D, D, U, ctypes.c_long, ctypes.c_double, D, D, D, D]
     L.oracle_velocity_distinct.argtypes = [D, ctypes.c_long, D, D, D, U, ctypes.c_long, ctypes.c_double, D, D]
+    L.oracle_velocity_faces.argtypes = [ctypes.POINTER(ctypes.c_long), ctypes.c_long, D, D, D, U, ctypes.c_long,
+                                         ctypes.c_double, D, D]
     L.oracle_bve_rk4.argtypes = [D, D, D, ctypes.c_long, D, D, D, D, U, ctypes.c_long,
                                  ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                  ctypes.c_double]
@@ -148,6 +150,22 @@ def velocity_distinct(tx, sx, zeta, area, mask, eps=0.0, psi=False):
     p = np.zeros(tx.shape[0]) if psi else None
     lib().oracle_velocity_distinct(_dp(tx), tx.shape[0], _dp(sx), _dp(zeta), _dp(area), _up(mask), sx.shape[0],
                                    float(eps), _dp(u), _dp(p))
+    return (u, p) if psi else u
+
+
+def velocity_faces(idx, fx, zeta, area, mask, eps=0.0, psi=False):
+    """Collocated velocity (and stream function) at the listed faces only: face k sums every
+    unmasked face j != k (BVEFaceVelocity / BVEFaceStreamFn restricted to a target subset)."""
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    fx = np.ascontiguousarray(fx, dtype=np.float64)
+    zeta = np.ascontiguousarray(zeta, dtype=np.float64)
+    area = np.ascontiguousarray(area, dtype=np.float64)
+    mask = np.ascontiguousarray(mask, dtype=np.uint8)
+    assert idx.size == 0 or (idx.min() >= 0 and idx.max() < fx.shape[0])
+    u = np.zeros((idx.size, 3))
+    p = np.zeros(idx.size) if psi else None
+    lib().oracle_velocity_faces(idx.ctypes.data_as(ctypes.POINTER(ctypes.c_long)), idx.size, _dp(fx), _dp(zeta),
+                                _dp(area), _up(mask), fx.shape[0], float(eps), _dp(u), _dp(p))
     return (u, p) if psi else u
 
 

@@ -3,7 +3,7 @@ src/LpmOctreeLUT.hpp:70-137: ParentLUT and ChildLUT, 8 x 27 each) into
 octree_tables.json, the known answer the oracle's and the product's generated tables are
 checked against.  Reads the reference source tree, so it runs where that tree is present.
 
-Run:  python tests/golden/make_octree_tables.py [path-to-lpmKokkos]
+Run:  python tests/golden/make_octree_tables.py <path-to-lpmKokkos-checkout>
 """
 import json
 import os
@@ -21,7 +21,9 @@ def table(text, name):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_octree_tables.py <path-to-lpmKokkos-checkout>")
+    ref = sys.argv[1]
     with open(os.path.join(ref, "src", "LpmOctreeLUT.hpp")) as f:
         text = f.read()
     out = {"source": "src/LpmOctreeLUT.hpp", "ParentLUT": table(text, "ParentLUT"), "ChildLUT": table(text, "ChildLUT")}

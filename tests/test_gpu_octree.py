@@ -81,3 +81,16 @@ def test_invalid_arguments():
     for n, d in ((0, 3), (4, 0), (4, 11)):
         assert L.lib().lpm_octree_build(x.data_ptr(), 3, 1, n, d, 1, ctypes.byref(h), None) \
             == L.LPM_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.skipif(torch.cuda.device_count() < 2, reason="needs a second GPU")
+def test_neighbour_tables_on_a_second_device(oracle):
+    """The neighbour tables live in __constant__ memory, which is per device: an octree built
+    on device 1 after one on device 0 gets the same neighbour lists as the oracle."""
+    x = _source_coords(1, 5)
+    t0 = bve.Octree(torch.from_numpy(x).cuda(0), 3)
+    t0.close()
+    with torch.cuda.device(1):
+        t1 = bve.Octree(torch.from_numpy(x).cuda(1), 3)
+        _same(t1, oracle.octree(x, 3))
+        t1.close()

@@ -220,15 +220,23 @@ def test_server_with_the_tree_code(ctx):
     big = (0, 6, 901)
     small = [(0, 3, 902), (1, 4, 903), (1, 3, 904)]
 
+    counters = []
+
     def run(specs):
         with bve.Server(0, flags=P.FP32C | P.TREECODE, host_ic=True) as srv:
             ids = [srv.submit(sk, lv, 0.0025, 3, ic_seed=seed, n_gaussians=3, gauss_width=0.1)
                    for sk, lv, seed in specs]
             for i in ids:
                 assert srv.wait(i, 300.0)
+            counters.append(srv.stats())
             return [srv.result(i) for i in ids]
 
     mix = run([small[0], big, small[1], small[2]])
+    # the tree request's direct-sum-equivalent pairs are kept apart from the pairs computed
+    nv, nf, nl = bve.mesh_counts(0, 6)
+    assert counters[0]["tree_equiv_pairs"] == (1 + 4 * 3) * (nv + nf) * nl
+    direct = sum((1 + 4 * 3) * (lambda c: (c[0] + c[1]) * c[2])(bve.mesh_counts(sk, lv)) for sk, lv, _ in small)
+    assert counters[0]["pairs"] == direct
     alone = run([big]) + run(small)
     for got, want in zip([mix[1], mix[0], mix[2], mix[3]], alone):
         for k in ("vx", "vvel", "fx", "fvel", "vzeta", "fzeta"):

@@ -173,30 +173,6 @@ def test_octree_and_tree_code_argument_checks(native):
     assert lib.lpm_sphere_tangency(ptr, 3, 1, ptr, 3, 1, -1, ptr, None) == L.LPM_ERR_INVALID_ARGUMENT
 
 
-def _integration_index():
-    """Function names of the integration notes' entry-point index; a cell's `_suffix` entries
-    share the first name's prefix (`lpm_octree_build`, `_info` -> lpm_octree_info)."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    section = text.split("## 9. Entry-point index", 1)[1]
-    names = set()
-    for line in section.splitlines():
-        if not line.startswith("| `"):
-            continue
-        cell = line.split("|")[1]
-        entries = re.findall(r"`([a-z0-9_]+)`", cell)
-        prefix = entries[0].rsplit("_", 1)[0]
-        for e in entries:
-            names.add(prefix + e if e.startswith("_") else e)
-    return names
-
-
-def test_integration_index_lists_every_declared_function():
-    declared = _declared_functions()
-    listed = _integration_index()
-    assert not declared - listed, sorted(declared - listed)
-    assert not listed - declared, sorted(listed - declared)
-
-
 @pytest.mark.parametrize("level", [2, 4, 7, 8])
 def test_bench_work_units_match_the_mesh(native, level):
     """The benchmark's work units: its closed-form mesh sizes equal the library's counts, the

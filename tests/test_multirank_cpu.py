@@ -74,7 +74,11 @@ def test_reference_arm_json_line(capsys, monkeypatch):
     assert d["impl"] == "reference" and d["metric"] == "RK4 steps/s" and d["unit"] == "steps/s"
     assert d["higher_is_better"] is True and d["n_gpus"] == 1 and d["steps"] == 1 and d["warmup"] == 0
     assert d["value"] > 0 and d["ms_per_step"] == pytest.approx(1000.0 / d["value"])
-    assert d["config"]["workload"] == bench.workload_desc(3)
+    # the same config object as the GPU arm's line (level 3 instead of the default 8)
+    assert d["config"] == bench.bench_config(bench.workload("c5", 3), 1)
+    assert d["steps_kind"].startswith("sampled evaluations")
+    fc = d["full_evaluation_check"]
+    assert fc["level"] == 3 and fc["pairs_per_s"] > 0 and fc["sample_over_full"] > 0
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert d["e2e"] == {"value": d["value"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
