@@ -16,8 +16,9 @@
  *    call for a new problem geometry (new pointers, sizes, strides or mask), which
  *    builds a plan: it copies positions and the mask to the host, synchronising the
  *    stream once.  The plan is reused by later calls with the same geometry: a context
- *    keeps the plans of its four most recent lpm_bve_velocity geometries (e.g. the vertex
- *    and the face evaluation of one mesh) and of its last lpm_bve_rk4_step state.
+ *    keeps the plan of its last lpm_bve_velocity call with distinct targets, of its last
+ *    collocated call (so a mesh's vertex and face evaluations both stay planned) and of
+ *    its last lpm_bve_rk4_step state.
  *  - Every function returns LPM_OK (0) or a negative status; lpm_bve_last_error()
  *    gives the message.  One context per host thread / stream.
  */

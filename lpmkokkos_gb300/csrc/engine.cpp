@@ -434,10 +434,11 @@ struct lpm_bve_ctx {
   std::string err;
   cudaStream_t capture = nullptr;  // private stream for graph capture
   // cached plans
-  // velocity plans, most recently used first: BVESphere::init_vorticity and every stream-function
-  // diagnostic alternate a vertex (distinct) and a face (collocated) evaluation on the same
-  // sources, so both plans stay cached instead of being rebuilt call after call
-  std::vector<std::unique_ptr<lpm::Batch>> velPlans;
+  // the last velocity plan of each kind, [0] distinct targets, [1] collocated: BVESphere::
+  // init_vorticity and every stream-function diagnostic alternate a vertex (distinct) and a face
+  // (collocated) evaluation on the same sources, so both stay cached instead of being rebuilt
+  // call after call
+  std::unique_ptr<lpm::Batch> velPlans[2];
   std::unique_ptr<lpm::Batch> rkBatch;
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
   lpm::PairShape forced{0, 0, 0, 0};       // FP32C launch shape chosen by the caller (threads 0 = none)
@@ -445,8 +446,6 @@ struct lpm_bve_ctx {
   double* normScratch = nullptr;  // device: block partials + result of lpm_errnorms
   double* normHost = nullptr;     // pinned: result of lpm_errnorms
 };
-
-constexpr size_t kVelPlans = 4;  // velocity plans a context keeps
 
 struct lpm_bve_ensemble {
   lpm_bve_ctx* ctx = nullptr;
@@ -679,7 +678,7 @@ int lpm_bve_ctx_destroy(lpm_bve_ctx* ctx) {
   if (!ctx) return LPM_ERR_INVALID_ARGUMENT;
   cudaSetDevice(ctx->dev.device);
   cudaDeviceSynchronize();
-  ctx->velPlans.clear();
+  for (auto& p : ctx->velPlans) p.reset();
   ctx->rkBatch.reset();
   if (ctx->capture) cudaStreamDestroy(ctx->capture);
   if (ctx->normScratch) cudaFree(ctx->normScratch);
@@ -695,7 +694,7 @@ int lpm_bve_plan_invalidate(lpm_bve_ctx* ctx) {
   try {
     setDevice(ctx);
     LPM_CUDA(cudaDeviceSynchronize());
-    ctx->velPlans.clear();
+    for (auto& p : ctx->velPlans) p.reset();
     ctx->rkBatch.reset();
   } catch (const Error& e) {
     return handle(ctx, e);
@@ -855,23 +854,15 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     const bool skip = colloc && (flags & LPM_BVE_SKIP_MASKED_TARGETS);
     const bool tree = flags & LPM_BVE_TREECODE;
     if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "velocity: the tree code needs LPM_BVE_FP32C");
-    auto& plans = ctx->velPlans;
-    bool hit = false;
-    for (size_t k = 0; k < plans.size() && !hit; ++k)
-      if (sameGeometry(ctx, plans[k].get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
-        std::rotate(plans.begin(), plans.begin() + k, plans.begin() + k + 1);  // to the front
-        hit = true;
-      }
-    if (!hit) {
-      if (plans.size() >= kVelPlans) {
-        LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the plan dropped here
-        plans.pop_back();
-      }
+    std::unique_ptr<Batch>& plan = ctx->velPlans[colloc ? 1 : 0];
+    if (!sameGeometry(ctx, plan.get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
+      if (plan) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
+      plan.reset();
       const bool precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
-      plans.insert(plans.begin(), makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s));
-      plans.front()->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
+      plan = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s);
+      plan->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
-    Batch& B = *plans.front();
+    Batch& B = *plan;
     // Distinct targets are arbitrary points unless the caller says they are mesh points.
     B.precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;

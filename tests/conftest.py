@@ -35,3 +35,13 @@ def ctx(native):
     c = bve.Context(0)
     yield c
     c.close()
+
+
+@pytest.fixture(autouse=True)
+def _fresh_plans(request):
+    """Plans are keyed by array addresses, and torch reuses the addresses of freed tensors: the
+    session context drops its plans after every test that used it, as the C ABI asks of callers
+    that move on to an unrelated problem (lpm_bve_plan_invalidate)."""
+    yield
+    if "ctx" in request.fixturenames:
+        request.getfixturevalue("ctx").invalidate()
