@@ -120,6 +120,9 @@ def parse(argv=None):
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-parity", action="store_true", help="skip the sampled-target oracle comparison")
     ap.add_argument("--no-secondary", action="store_true", help="c5: skip the level-7 secondary leg")
+    ap.add_argument("--no-symmetric", action="store_true",
+                    help="c2/c5: steps with the plain pair kernel (LPM_BVE_NO_SYMMETRIC: every leaf pair in both "
+                         "directions) instead of the symmetric leaf kernel")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c5",
                     help="c5: icos L8, eps 0.01, 8 vortices, RK4 steps then the stream function at all targets "
@@ -275,6 +278,7 @@ def run_ours(args, rank, world, local_rank):
     dev = torch.device("cuda", local_rank)
     ctx = bve.Context(local_rank, autotune=args.autotune)
     prec = P.FP32C if args.prec == "fp32c" else P.FP64
+    sflags = prec | (P.NO_SYMMETRIC if args.no_symmetric else 0)  # RK4 step flags
     w = workload(args.config, args.level)
     level, eps = w["level"], w["eps"]
     nv, nall, nl = mesh_sizes(level)
@@ -307,7 +311,7 @@ def run_ours(args, rank, world, local_rank):
 
     # warm-up: builds the plan and captures the step graph
     t0 = time.time()
-    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=prec, eps=eps)
+    ctx.rk4_step(st, w["dt"], w["omega"], max(1, args.warmup), flags=sflags, eps=eps)
     torch.cuda.synchronize()
     t_warm = time.time() - t0
 
@@ -324,7 +328,7 @@ def run_ours(args, rank, world, local_rank):
         e0.record(stream)
         for _ in range(nsteps):
             flush.zero_()
-            ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=eps)
+            ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=sflags, eps=eps)
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
@@ -370,7 +374,7 @@ def run_ours(args, rank, world, local_rank):
     for _ in range(e2e_steps):
         for n in names:
             getattr(st, n).copy_(host[n], non_blocking=True)
-        ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=prec, eps=eps)
+        ctx.rk4_step(st, w["dt"], w["omega"], 1, flags=sflags, eps=eps)
         for n in names:
             host[n].copy_(getattr(st, n), non_blocking=True)
     e1.record(stream)

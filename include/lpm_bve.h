@@ -68,6 +68,9 @@ typedef struct CUstream_st* lpm_stream_t; /* identical to cudaStream_t; NULL = l
                                                  octree clusters far from a target tile act through
                                                  interpolated proxies (lpm_bve_ctx_set_treecode); an
                                                  approximation with its own tolerance, not in the reference */
+#define LPM_BVE_NO_SYMMETRIC        (1u << 12) /* FP32C collocated velocity()/rk4: sum every leaf-leaf pair in
+                                                 both directions with the plain direct kernel instead of once
+                                                 with the symmetric leaf kernel (same sums, other rounding) */
 
 /* ---- context ---------------------------------------------------------------- */
 typedef struct lpm_bve_ctx lpm_bve_ctx;

@@ -7,7 +7,7 @@ here (``Context``, ``BVESphere``, ``BVERK4``) mirror the reference's host interf
 """
 from ._build import build  # noqa: F401
 from ._lib import (  # noqa: F401
-    COLLOCATED, FP32C, FP64, MESH_TARGETS, NO_GRAPH, RCP_APPROX, TREECODE, NO_SORT, NO_VELOCITY, PSI, RENORM, RK4_FIX_QUIRK, SEED_CUBED,
+    COLLOCATED, FP32C, FP64, MESH_TARGETS, NO_GRAPH, NO_SYMMETRIC, RCP_APPROX, TREECODE, NO_SORT, NO_VELOCITY, PSI, RENORM, RK4_FIX_QUIRK, SEED_CUBED,
     SEED_ICOS_TRI, SKIP_MASKED_TARGETS, LpmError, lib,
 )
 

@@ -33,6 +33,7 @@ NO_SORT = 1 << 8
 MESH_TARGETS = 1 << 9
 RCP_APPROX = 1 << 10
 TREECODE = 1 << 11
+NO_SYMMETRIC = 1 << 12
 
 SEED_ICOS_TRI = 0
 SEED_CUBED = 1

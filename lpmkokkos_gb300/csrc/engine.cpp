@@ -51,7 +51,7 @@ void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc
 }
 
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
-                     cudaStream_t s) {
+                     cudaStream_t s, bool symLayout) {
   std::vector<uint8_t> hmask((size_t)io.nb, 0);
   if (mask && io.nb > 0) {
     LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)io.nb, cudaMemcpyDeviceToHost, s));
@@ -63,11 +63,11 @@ HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool 
     hb = fetchPoints(io.bx.p, io.nb, io.bx.si, io.bx.sc, s);
   }
   return prepareHostFromHost(mode, io.na, io.nb, ha.empty() ? nullptr : ha.data(), hb.empty() ? nullptr : hb.data(),
-                             hmask.data(), skipMasked, sort);
+                             hmask.data(), skipMasked, sort, symLayout);
 }
 
 HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
-                             const uint8_t* hmaskIn, bool skipMasked, bool sort) {
+                             const uint8_t* hmaskIn, bool skipMasked, bool sort, bool symLayout) {
   HostPlan H;
   H.na = na;
   H.nb = nb;
@@ -75,13 +75,15 @@ HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha
   hmask.assign((size_t)nb, 0);
   if (hmaskIn && nb > 0) std::copy(hmaskIn, hmaskIn + nb, hmask.begin());
 
-  // Target slots: particle ids (a: id = i; face f: id = na + f).
+  // Target slots: particle ids (a: id = i; face f: id = na + f).  With the symmetric layout the
+  // leaves are left out here and appended in source order below.
+  const bool sym = symLayout && sort && mode != Mode::Distinct;
   std::vector<int> ids;
   if (mode != Mode::Collocated)
     for (int64_t i = 0; i < na; ++i) ids.push_back((int)i);
   if (mode != Mode::Distinct)
     for (int64_t f = 0; f < nb; ++f)
-      if (!(skipMasked && hmask[f])) ids.push_back((int)(na + f));
+      if (!(skipMasked && hmask[f]) && !(sym && !hmask[f])) ids.push_back((int)(na + f));
   std::vector<int> srcFace;
   for (int64_t f = 0; f < nb; ++f)
     if (!hmask[f]) srcFace.push_back((int)f);
@@ -98,6 +100,13 @@ HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha
     for (size_t i = 0; i < srcFace.size(); ++i) ks[i] = {mortonKey(&hb[3 * (size_t)srcFace[i]]), srcFace[i]};
     std::sort(ks.begin(), ks.end());
     for (size_t i = 0; i < srcFace.size(); ++i) srcFace[i] = ks[i].second;
+    if (sym) {
+      H.leaf0 = (int)ids.size();
+      for (size_t i = 0; i < srcFace.size(); ++i) {
+        ids.push_back((int)(na + srcFace[i]));
+        H.slotKeys.push_back(ks[i].first);
+      }
+    }
   }
   const int nslots = (int)ids.size(), ns = (int)srcFace.size();
   std::vector<int> srcOf((size_t)nb, -1), slotOf((size_t)nb, -1);
@@ -139,11 +148,25 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
 
   P.nslots = nslots;
   P.ns = ns;
-  P.ntiles = (nslots + tileSize - 1) / tileSize;
+  P.leaf0 = H.leaf0;
+  // Target tiles of tileSize slots; with the symmetric layout a tile boundary falls at leaf0, so
+  // no tile mixes the Morton-ordered non-leaf slots with the leaves (a mixed tile would join
+  // distant parts of the sphere).
+  P.tileStart.clear();
+  for (int t = 0; t < nslots;) {
+    P.tileStart.push_back(t);
+    const int end = (H.leaf0 > 0 && t < H.leaf0) ? H.leaf0 : nslots;
+    t = std::min(end, t + tileSize);
+  }
+  P.ntiles = (int)P.tileStart.size();
+  P.tileStart.push_back(nslots);
+  std::vector<int> tileOf((size_t)nslots);
+  for (int t = 0; t < P.ntiles; ++t)
+    for (int q = P.tileStart[t]; q < P.tileStart[t + 1]; ++q) tileOf[q] = t;
   P.tileSelfHost.assign((size_t)P.ntiles, make_int2(INT_MAX, -1));
   for (int t = 0; t < nslots; ++t)
     if (self[t] >= 0) {
-      int2& r = P.tileSelfHost[t / tileSize];
+      int2& r = P.tileSelfHost[tileOf[t]];
       r.x = std::min(r.x, self[t]);
       r.y = std::max(r.y, self[t]);
     }
@@ -160,14 +183,14 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
     return mid;
   };
   std::vector<int> tileCentre((size_t)P.ntiles);
-  for (int t = 0; t < P.ntiles; ++t) tileCentre[t] = centreOf(t * tileSize, std::min(tileSize, nslots - t * tileSize));
+  for (int t = 0; t < P.ntiles; ++t) tileCentre[t] = centreOf(P.tileStart[t], P.tileStart[t + 1] - P.tileStart[t]);
   // Tree-code tiles: the same slot order cut into runs of at most tileSize slots that never
   // cross a level-3 Morton cell (a run across a cell boundary can join distant parts of the
   // sphere, and its one bounding sphere would then accept no far field).
   std::vector<int2> treeTiles;
   std::vector<int> treeCentres;
   for (int t = 0, start = 0; t <= nslots; ++t) {
-    const bool cut = t == nslots || t - start == tileSize ||
+    const bool cut = t == nslots || t - start == tileSize || (t == H.leaf0 && t > start) ||
                      (!H.slotKeys.empty() && t > start && (H.slotKeys[t] >> 21) != (H.slotKeys[start] >> 21));
     if (cut && t > start) {
       treeTiles.push_back(make_int2(start, t - start));
@@ -218,6 +241,11 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   }
   S.nslots = nslots;
   S.ns = ns;
+  S.leaf0 = H.leaf0;
+  if (H.leaf0 >= 0 && prec == Precision::FP32C) {  // reverse sums of the symmetric leaf kernel
+    S.rev = M.alloc<unsigned long long>(3 * (size_t)std::max(1, ns));
+    S.revBad = M.alloc<int>(std::max(1, ns));
+  }
 
   SolveDev& D = P.dev;
   D = SolveDev{};
@@ -232,6 +260,9 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   D.ns = ns;
   D.tileSize = tileSize;
   D.eps2 = P.eps2;
+  D.leaf0 = H.leaf0;
+  D.rev = S.rev;
+  D.revBad = S.revBad;
 }
 
 // Source chunking of one solve.  The rule depends on the solve alone (never on the other
@@ -278,6 +309,8 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
         w.s0 = std::min(P.ns, c * chunkLen);
         w.s1 = std::min(P.ns, (c + 1) * chunkLen);
         w.chunk = c;
+        w.tbeg = P.tileStart[t];
+        w.tend = P.tileStart[t + 1];
         items.push_back(w);
       }
   }
@@ -292,10 +325,37 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   B.grid = std::min(B.nitems, slots);
   B.slots = slots;
   B.itemPairs.resize(items.size());
-  for (size_t i = 0; i < items.size(); ++i) {
-    const SolvePlan& P = *B.solves[items[i].solve];
-    const int t0 = items[i].tile * B.shape.tileSize();
-    B.itemPairs[i] = (double)std::min(B.shape.tileSize(), P.nslots - t0) * (items[i].s1 - items[i].s0);
+  for (size_t i = 0; i < items.size(); ++i)
+    B.itemPairs[i] = (double)(items[i].tend - items[i].tbeg) * (items[i].s1 - items[i].s0);
+
+  // Symmetric leaf x leaf evaluation of a single solve: the direct kernel keeps the non-leaf
+  // target tiles (vertices, masked parents; slots [0, leaf0)), the symmetric kernel takes the
+  // upper triangle of leaf tiles.  Row I (leaf tile I against tiles I..NT-1) is cut into the
+  // solve's nchunks segments; segment c writes partial chunk c of tile I's slots (an empty
+  // segment writes zeros), so the epilogue's fixed-order chunk sum covers every leaf slot.
+  std::vector<WorkItem> symDirect, symItems;
+  if (B.sym) {
+    const SolvePlan& P = *B.solves[0];
+    for (const WorkItem& w : items)
+      if (w.tbeg < P.leaf0) symDirect.push_back(w);
+    const int nt = (P.ns + kSymTile - 1) / kSymTile;
+    for (int I = 0; I < nt; ++I) {
+      const int len = nt - I;
+      for (int c = 0; c < P.nchunks; ++c) {
+        WorkItem w{};
+        w.tile = I;
+        w.s0 = I + (int)((int64_t)len * c / P.nchunks);
+        w.s1 = I + (int)((int64_t)len * (c + 1) / P.nchunks);
+        w.chunk = c;
+        symItems.push_back(w);
+      }
+    }
+    std::stable_sort(symItems.begin(), symItems.end(),
+                     [](const WorkItem& a, const WorkItem& b) { return a.s1 - a.s0 > b.s1 - b.s0; });
+    B.nSymDirectItems = (int)symDirect.size();
+    B.nSymItems = (int)symItems.size();
+    B.symDirectGrid = std::min(B.nSymDirectItems, slots);
+    B.symGrid = std::min(B.nSymItems, std::max(1, dev.sms * pairSymBlocksPerSM()));
   }
 
   const int bs = stageBlockSize();
@@ -320,7 +380,13 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   B.stageDev = B.mem.alloc<SolveStage>(B.solves.size());
   B.prepMap = B.mem.alloc<int4>(prepMap.size());
   B.slotMap = B.mem.alloc<int4>(slotMap.size());
-  B.counter = B.mem.alloc<int>(1);
+  B.counter = B.mem.alloc<int>(2);
+  if (B.sym) {
+    B.symDirectItems = B.mem.alloc<WorkItem>(symDirect.size());
+    B.symItems = B.mem.alloc<WorkItem>(symItems.size());
+    upload(B.symDirectItems, symDirect, s);
+    upload(B.symItems, symItems, s);
+  }
   upload(B.items, items, s);
   upload(B.prepMap, prepMap, s);
   upload(B.slotMap, slotMap, s);
@@ -332,7 +398,7 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   }
   upload(B.solveDev, sd, s);
   upload(B.stageDev, ss, s);
-  LPM_CUDA(cudaMemsetAsync(B.counter, 0, sizeof(int), s));
+  LPM_CUDA(cudaMemsetAsync(B.counter, 0, 2 * sizeof(int), s));
   LPM_CUDA(cudaStreamSynchronize(s));  // host vectors above go out of scope
 }
 
@@ -389,15 +455,23 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
     e1 = B.timer->get();
     LPM_CUDA(cudaEventRecord(e0, s));
   }
-  LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.items, B.nitems, B.counter,
-                      B.grid, s));
+  // symmetric leaf x leaf evaluation: velocity only (the stream function keeps the plain path)
+  const bool sym = B.sym && !psi && !B.precise;
+  if (sym) {
+    LPM_CUDA(launchPair(B.prec, B.shape, false, false, B.rcpApprox, B.solveDev, B.symDirectItems, B.nSymDirectItems,
+                        B.counter, B.symDirectGrid, s));
+    LPM_CUDA(launchPairSym(B.rcpApprox, B.solveDev, B.symItems, B.nSymItems, B.counter + 1, B.symGrid, s));
+  } else {
+    LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.items, B.nitems, B.counter,
+                        B.grid, s));
+  }
   if (B.timer) {
     LPM_CUDA(cudaEventRecord(e1, s));
     B.timer->pending.emplace_back(e0, e1);
   }
   pairRange.reset();
   std::unique_ptr<NvtxRange> epi(names ? new NvtxRange(names->epilogue) : nullptr);
-  LPM_CUDA(launchEpilogue(B.stageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
+  LPM_CUDA(launchEpilogue(B.stageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s, sym));
 }
 
 // One RK4 step (src/LpmBVERK4_Impl.hpp:42-130) for every solve of the batch, its launches named
@@ -479,8 +553,9 @@ bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si &
 
 // True when a cached single-solve batch was built for the same geometry.
 bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision prec, const ParticleIO& io,
-                  const uint8_t* mask, bool skipMasked, bool sort, double eps, bool tree) {
+                  const uint8_t* mask, bool skipMasked, bool sort, double eps, bool tree, bool sym) {
   if (!B || B->solves.size() != 1) return false;
+  if ((B->solves[0]->leaf0 >= 0) != sym) return false;
   if (!(shapeFor(ctx, prec, tree) == B->shape)) return false;
   const SolvePlan& P = *B->solves[0];
   return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
@@ -493,11 +568,19 @@ bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision p
 PairShape autotune(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask,
                    bool skipMasked, bool sort, double eps, bool precise, const HostPlan& H, cudaStream_t s);
 
+// A single solve's collocated / RK4 FP32C plan takes the symmetric layout unless the caller asks
+// for the plain kernel (LPM_BVE_NO_SYMMETRIC), the tree code runs, or the targets keep their own
+// order.
+bool wantSymmetric(Mode mode, Precision prec, bool sort, bool tree, unsigned flags) {
+  return mode != Mode::Distinct && prec == Precision::FP32C && sort && !tree && !(flags & LPM_BVE_NO_SYMMETRIC);
+}
+
 std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io,
                                   const uint8_t* mask, bool skipMasked, bool sort, double eps, bool precise,
-                                  bool tree, cudaStream_t s) {
-  const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s);
+                                  bool tree, cudaStream_t s, bool sym) {
+  const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s, sym);
   auto B = std::make_unique<Batch>();
+  B->sym = H.leaf0 >= 0 && H.srcFace.size() > 0;
   B->prec = prec;
   B->shape = shapeFor(ctx, prec, tree);
   if (!tree && prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0)
@@ -509,9 +592,11 @@ std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, c
   buildSolve(*B->solves[0], mode, prec, io, mask, skipMasked, sort, eps, B->shape.tileSize(), H, s);
   finalizeBatch(*B, ctx->dev, s);
   if (ctx->verbose)
-    std::fprintf(stderr, "[lpm_bve] plan: mode=%d prec=%d slots=%d sources=%d tiles=%d chunks=%d items=%d grid=%d\n",
+    std::fprintf(stderr, "[lpm_bve] plan: mode=%d prec=%d slots=%d sources=%d tiles=%d chunks=%d items=%d grid=%d "
+                 "symmetric=%d (leaf0 %d, %d + %d items)\n",
                  (int)mode, (int)prec, B->solves[0]->nslots, B->solves[0]->ns, B->solves[0]->ntiles,
-                 B->solves[0]->nchunks, B->nitems, B->grid);
+                 B->solves[0]->nchunks, B->nitems, B->grid, (int)B->sym, B->solves[0]->leaf0, B->nSymDirectItems,
+                 B->nSymItems);
   return B;
 }
 
@@ -620,6 +705,8 @@ void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree, cudaStream_t s) {
         w.s0 = std::min(P.ns, c * P.chunkLen);
         w.s1 = std::min(P.ns, (c + 1) * P.chunkLen);
         w.chunk = c;
+        w.tbeg = P.tileStart[t];
+        w.tend = P.tileStart[t + 1];
         items.push_back(w);
       }
   }
@@ -855,11 +942,12 @@ int lpm_bve_velocity(lpm_bve_ctx* ctx, const lpm_points* tgt, const lpm_sources*
     const bool tree = flags & LPM_BVE_TREECODE;
     if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "velocity: the tree code needs LPM_BVE_FP32C");
     std::unique_ptr<Batch>& plan = ctx->velPlans[colloc ? 1 : 0];
-    if (!sameGeometry(ctx, plan.get(), mode, prec, io, src->mask, skip, sort, eps, tree)) {
+    const bool sym = wantSymmetric(mode, prec, sort, tree, flags);
+    if (!sameGeometry(ctx, plan.get(), mode, prec, io, src->mask, skip, sort, eps, tree, sym)) {
       if (plan) LPM_CUDA(cudaDeviceSynchronize());  // kernels may still read the old plan
       plan.reset();
       const bool precise = prec == Precision::FP32C && mode == Mode::Distinct && !(flags & LPM_BVE_MESH_TARGETS);
-      plan = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s);
+      plan = makeSingle(ctx, mode, prec, io, src->mask, skip, sort, eps, precise, tree, s, sym);
       plan->solves[0]->stage.io = ParticleIO{};  // force a table refresh below
     }
     Batch& B = *plan;
@@ -924,10 +1012,11 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
     const bool tree = flags & LPM_BVE_TREECODE;
     if (tree && prec != Precision::FP32C) fail(LPM_ERR_NOT_SUPPORTED, "rk4_step: the tree code needs LPM_BVE_FP32C");
-    if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps, tree)) {
+    const bool sym = wantSymmetric(Mode::RK4, prec, sort, tree, flags);
+    if (!sameGeometry(ctx, ctx->rkBatch.get(), Mode::RK4, prec, io, st->fmask, skip, sort, eps, tree, sym)) {
       if (ctx->rkBatch) LPM_CUDA(cudaDeviceSynchronize());
       ctx->rkBatch.reset();
-      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, false, tree, s);
+      ctx->rkBatch = makeSingle(ctx, Mode::RK4, prec, io, st->fmask, skip, sort, eps, false, tree, s, sym);
       ctx->rkBatch->solves[0]->stage.io = ParticleIO{};
     }
     Batch& B = *ctx->rkBatch;

@@ -37,14 +37,28 @@ struct ParticleIO {
   const double* barea = nullptr;
 };
 
-// Pair-kernel work item: one target tile against one contiguous source chunk.
+// Pair-kernel work item: one target tile against one contiguous source chunk.  In the
+// symmetric leaf kernel (pairFP32CSym) `tile` is a leaf tile I and [s0, s1) a range of leaf
+// tiles J >= I.
 struct WorkItem {
   int solve;     // index into the SolveDev table
   int tile;      // target tile within the solve
   int s0, s1;    // source range [s0, s1) within the solve
   int chunk;     // partial-sum slot (chunk index within the tile's row)
-  int pad0, pad1, pad2;
+  int tend;      // the tile's target slots are [tbeg, min(tbeg + tile size, tend))
+  int tbeg;
+  int pad;
 };
+
+// Symmetric leaf x leaf evaluation: leaf tiles of kSymTile slots (128 threads x 8 targets),
+// reverse sums accumulated in 64-bit fixed point with kSymScale units per 1 (exact, order-free
+// integer adds; a per-source flag marks contributions that are not finite or not below
+// kSymLimit, and the epilogue turns the source's result into NaN).
+constexpr int kSymThreads = 128;
+constexpr int kSymK = 8;
+constexpr int kSymTile = kSymThreads * kSymK;
+constexpr double kSymScale = 1099511627776.0;  // 2^40
+constexpr double kSymLimit = 1048576.0;        // 2^20
 
 // Device-side description of one solve for the pair kernels.
 struct SolveDev {
@@ -58,6 +72,11 @@ struct SolveDev {
   double* partial;           // [nchunks][ncomp][nslots]
   int nslots, ns, tileSize, nchunks;
   double eps2;
+  // symmetric layout: slots [leaf0, nslots) are the leaf sources 0..ns-1 in source order
+  // (leaf0 = -1: no such layout); reverse sums of the symmetric leaf kernel
+  int leaf0;
+  unsigned long long* rev;   // [3][ns] fixed point
+  int* revBad;               // [ns]
 };
 
 // Per-solve parameters for the O(N) kernels.
@@ -73,6 +92,9 @@ struct SolveStage {
   const double* partial;     // [nchunks][ncomp][nslots]
   int nslots, ns, nchunks;
   double dt, omega;
+  int leaf0;                 // symmetric layout: first leaf slot (-1: none)
+  unsigned long long* rev;   // [3][ns] fixed-point reverse sums (zeroed by prep), or null
+  int* revBad;               // [ns]
 };
 
 // Launch-shape of the FP32C pair kernel.
@@ -96,9 +118,10 @@ enum class Precision { FP64 = 0, FP32C = 1 };
 // from the stored velocity), 2 = stage-3 inputs (x + x_2/2), 3 = stage-4 inputs (x + x_3).
 cudaError_t launchPrep(const SolveStage* st, const int4* map, int nblocks, int stage, Precision prec, int* counter,
                        cudaStream_t s);
-// stageOut: 0 = no increments, 1..3 = write x_k/zeta_k of RK4 stage k+1.
+// stageOut: 0 = no increments, 1..3 = write x_k/zeta_k of RK4 stage k+1.  useRev: add the
+// symmetric kernel's reverse sums to the leaf slots.
 cudaError_t launchEpilogue(const SolveStage* st, const int4* map, int nblocks, Precision prec, bool psi,
-                           bool velocity, int stageOut, cudaStream_t s);
+                           bool velocity, int stageOut, cudaStream_t s, bool useRev = false);
 cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bool quirk, bool renorm,
                           cudaStream_t s);
 // precise: FP32C with hi/lo target-source differences (arbitrary distinct targets).
@@ -106,6 +129,10 @@ cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bo
 cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
                        const SolveDev* solves, const WorkItem* items, int nitems, int* counter, int grid,
                        cudaStream_t s);
+// Symmetric leaf x leaf kernel over `items` (see WorkItem); grid = resident CTAs.
+cudaError_t launchPairSym(bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems, int* counter,
+                          int grid, cudaStream_t s);
+int pairSymBlocksPerSM();
 int pairShapeCount();              // FP32C launch shapes compiled in
 PairShape pairShapeAt(int i);
 int stageBlockSize();

@@ -144,6 +144,8 @@ struct SolvePlan {
   int nslots = 0, ns = 0, ntiles = 0, nchunks = 1, tileSize = 1, chunkLen = 0;
   double eps2 = 0.0;
   std::vector<int2> tileSelfHost;
+  std::vector<int> tileStart;  // [ntiles + 1] first slot of each target tile (tiles never straddle leaf0)
+  int leaf0 = -1;  // symmetric layout: slots [leaf0, nslots) are the sources in source order
   // tree-code target tiles: runs of <= tileSize slots inside one level-3 Morton cell
   int nTreeTiles = 0;
   int2* treeTiles = nullptr;    // [nTreeTiles] {first slot, count}
@@ -196,6 +198,13 @@ struct Batch {
   bool precise = false;    // FP32C hi/lo differences (arbitrary distinct targets)
   bool rcpApprox = false;  // FP32C without the Newton step (LPM_BVE_RCP_APPROX)
   int nitems = 0, grid = 0, nPrepBlocks = 0, nSlotBlocks = 0;
+  // symmetric leaf x leaf evaluation (single FP32C solves with the symmetric layout): the direct
+  // kernel's items over the non-leaf slots and the symmetric kernel's items, each run with its
+  // own persistent grid and work counter (counter[0], counter[1])
+  bool sym = false;
+  WorkItem* symDirectItems = nullptr;
+  WorkItem* symItems = nullptr;
+  int nSymDirectItems = 0, nSymItems = 0, symDirectGrid = 0, symGrid = 0;
   std::vector<double> itemPairs;  // target-source pairs of each work item (host, launch order)
   DeviceArena mem;
   WorkItem* items = nullptr;
@@ -237,13 +246,17 @@ struct HostPlan {
   std::vector<uint8_t> hmask;
   std::vector<int> ids, srcFace, self, srcSlot;
   std::vector<uint32_t> slotKeys;  // Morton key of each slot (sorted plans only)
+  int leaf0 = -1;                  // symmetric layout: first leaf slot (-1: plain layout)
 };
 
+// symLayout (collocated / RK4 plans, sorted): the non-leaf target slots (vertices, masked faces)
+// first in Morton order, then every leaf in source order, so that leaf slot leaf0 + k is source
+// k -- the layout of the symmetric leaf x leaf kernel.
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
-                     cudaStream_t s);
+                     cudaStream_t s, bool symLayout = false);
 // Same from host arrays: ha (na x 3) and hb (nb x 3) row-major positions, hmask (nb bytes).
 HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
-                             const uint8_t* hmask, bool skipMasked, bool sort);
+                             const uint8_t* hmask, bool skipMasked, bool sort, bool symLayout = false);
 void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
                 bool sort, double eps, int tileSize, const HostPlan& H, cudaStream_t s);
 int chunkLength(int ns, int srcTile);

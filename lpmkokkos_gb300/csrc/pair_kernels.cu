@@ -369,8 +369,8 @@ __global__ void __launch_bounds__(NTH, MINB) pairFP32C(const SolveDev* __restric
     const WorkItem w = items[it];
     const SolveDev& S = solves[w.solve];
     const int n = S.nslots;
-    const int tile0 = w.tile * (NTH * K);
-    const int tcount = min(NTH * K, n - tile0);
+    const int tile0 = w.tbeg;
+    const int tcount = min(NTH * K, w.tend - tile0);
 
     TileTargets<K> tt;
     loadTileTargets<NTH, K, PRECISE>(S.tx, n, tile0, tcount, S.tileCentre[w.tile], S.self, S.eps2, &sCentre, tt);
@@ -545,6 +545,186 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
   }
 }
 
+// ---------------------------------------------------------------------------------------
+// Symmetric leaf x leaf sums.  Leaf faces are targets and sources at once (collocated face
+// velocity, every RK4 stage): the pair (i, j) gives source j's term on target i and source i's
+// term on target j from the same d = x_j - x_i, 2q and reciprocal.  With the plan's symmetric
+// layout (leaf target slot leaf0 + k is source k), an item takes leaf tile I (kSymTile targets,
+// 8 per thread) against the source tiles J0..J1-1, J0 >= I:
+//   * forward: source j on the thread's targets, accumulated in registers exactly as pairFP32C
+//     does (FP32 sub-block sums, Kahan-compensated, one FP64 partial per chunk);
+//   * reverse (J > I only): target i as the source of target j, s_r = W_i rn with the same
+//     rn = r (2q r - 2) (the negated Newton reciprocal).  Each thread sums its 8 targets' terms
+//     per source.  Per 32 sources a warp transposes its lanes' terms through its own shared
+//     buffer (warp-synchronous, no block barrier) and lane l sums source l over the 32 lanes;
+//     per 256 staged sources the four warps' sums meet once, are added in warp order and go to
+//     the source's 64-bit fixed-point accumulator (kSymScale units: integer adds are exact and
+//     order-free, so the result does not depend on the schedule).
+//   * the diagonal tile J = I is summed in the forward direction only, with the self pair
+//     (source index = the target's own) dropped.
+// Per unordered pair: 17 paired FMA-pipe ops + 2 MUFU for two directed pairs (13 + 1 each in
+// pairFP32C), plus ~4 FP32 adds per source and thread for the transposed reduction.
+constexpr int kSymSt = 256;              // sources staged per step
+constexpr int kSymRed = 32;              // sources per warp transpose
+constexpr int kSymWarps = kSymThreads / 32;
+constexpr int kSymPitch = 33;            // floats per transpose row (32 lanes + 1 skew)
+constexpr size_t kSymSmem = sizeof(float4) * kSymSt * 2 + sizeof(float2) * kSymSt +
+                            sizeof(float) * kSymWarps * 3 * kSymRed * kSymPitch +
+                            sizeof(float) * kSymWarps * 3 * kSymSt;
+
+template <bool NEWTON>
+__global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* __restrict__ solves,
+                                                             const WorkItem* __restrict__ items, int nitems,
+                                                             int* __restrict__ counter) {
+  constexpr int NTH = kSymThreads, K = kSymK, P = K / 2, ST = kSymSt;
+  static_assert(NTH == 128, "the cross-warp combine assumes four warps");
+  extern __shared__ __align__(16) unsigned char symSmem[];
+  float4* sXY = reinterpret_cast<float4*>(symSmem);
+  float4* sZW = sXY + ST;
+  float2* sD = reinterpret_cast<float2*>(sZW + ST);
+  float* sWarp = reinterpret_cast<float*>(sD + ST);            // [warp][3 * 32 rows][33]
+  float* sCross = sWarp + kSymWarps * 3 * kSymRed * kSymPitch; // [warp][3][ST]
+  __shared__ int sItem;
+  __shared__ int sCentre;
+  SourceTile<false> T;
+  T.xy = sXY; T.zw = sZW; T.d = sD;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* myBuf = sWarp + warp * 3 * kSymRed * kSymPitch;
+  float* myCross = sCross + warp * 3 * ST;
+  const float2 kMinusTwo = make_float2(-2.f, -2.f);
+  constexpr float kSign = NEWTON ? -1.f : 1.f;
+
+  for (;;) {
+    if (threadIdx.x == 0) sItem = atomicAdd(counter, 1);
+    __syncthreads();
+    const int it = sItem;
+    __syncthreads();
+    if (it >= nitems) return;
+    const WorkItem w = items[it];
+    const SolveDev& S = solves[w.solve];
+    const int n = S.nslots, ns = S.ns;
+    const int tgt0 = w.tile * kSymTile;                 // first source index of leaf tile I
+    const int tcount = min(kSymTile, ns - tgt0);
+    const int slot0 = S.leaf0 + tgt0;
+    TileTargets<K> tt;
+    loadTileTargets<NTH, K, false>(S.tx, n, slot0, tcount, slot0 + tcount / 2, S.self, S.eps2, &sCentre, tt);
+    // the targets' own source weights W_i (zero for dead lanes: they then add nothing reversed)
+    float2 Wt[P];
+#pragma unroll
+    for (int m = 0; m < P; ++m) {
+      const int a = threadIdx.x + 2 * m * NTH, b = a + NTH;
+      Wt[m] = make_float2(a < tcount ? S.sp0[tgt0 + a].w : 0.f, b < tcount ? S.sp0[tgt0 + b].w : 0.f);
+    }
+    float hx[K], hy[K], hz[K], cx[K], cy[K], cz[K], hp[K], cp[K], hw[K], cw[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+      hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
+      hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
+    }
+    for (int J = w.s0; J < w.s1; ++J) {
+      const int src0 = J * kSymTile;
+      const int send = min(ns, src0 + kSymTile);
+      for (int b0 = src0; b0 < send; b0 += ST) {
+        for (int j = threadIdx.x; j < ST; j += NTH) {
+          const int src = b0 + j;
+          const bool live = src < send;
+          stageSource<K, false>(j, live, live ? S.sp0[src] : float4{}, live ? S.sp1[src] : float4{}, tt, sXY, sZW, sD,
+                                nullptr, nullptr);
+        }
+        __syncthreads();
+        if (J == w.tile) {  // diagonal: forward only, the self pair (source index == own) dropped
+          int self[K];
+#pragma unroll
+          for (int k = 0; k < K; ++k) self[k] = tgt0 + threadIdx.x + k * NTH;
+          fp32cTile<K, false, true, false, NEWTON>(T, ST, b0, nullptr, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
+                                                  tt.C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+        } else {
+#pragma unroll 1
+          for (int j0 = 0; j0 < ST; j0 += kSymRed) {
+            float2 vx[P], vy[P], vz[P];
+#pragma unroll
+            for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = make_float2(0.f, 0.f);
+#pragma unroll 2
+            for (int jj = 0; jj < kSymRed; ++jj) {
+              const int j = j0 + jj;
+              const float4 xy = sXY[j];
+              const float4 zw = sZW[j];
+              const float2 dj = sD[j];
+              const float2 X = make_float2(xy.x, xy.y), Y = make_float2(xy.z, xy.w), Z = make_float2(zw.x, zw.y);
+              const float2 W = make_float2(zw.z, zw.w);
+              float2 rx = make_float2(0.f, 0.f), ry = rx, rz = rx;
+#pragma unroll
+              for (int m = 0; m < P; ++m) {
+                const float2 dx = add2(X, tt.nx[m]), dy = add2(Y, tt.ny[m]), dz = add2(Z, tt.nz[m]);
+                float2 q = add2(dj, tt.C[m]);
+                q = fma2(dx, dx, q);
+                q = fma2(dy, dy, q);
+                q = fma2(dz, dz, q);
+                float2 r = make_float2(rcpApprox(q.x), rcpApprox(q.y));
+                if (NEWTON) r = mul2(r, fma2(q, r, kMinusTwo));  // -(Newton reciprocal)
+                const float2 sf = mul2(W, r);
+                vx[m] = fma2(sf, dx, vx[m]);
+                vy[m] = fma2(sf, dy, vy[m]);
+                vz[m] = fma2(sf, dz, vz[m]);
+                const float2 sr = mul2(Wt[m], r);
+                rx = fma2(sr, dx, rx);
+                ry = fma2(sr, dy, ry);
+                rz = fma2(sr, dz, rz);
+              }
+              // this lane's reverse terms of source jj: row (component, jj), column = lane
+              myBuf[(0 * kSymRed + jj) * kSymPitch + lane] = rx.x + rx.y;
+              myBuf[(1 * kSymRed + jj) * kSymPitch + lane] = ry.x + ry.y;
+              myBuf[(2 * kSymRed + jj) * kSymPitch + lane] = rz.x + rz.y;
+            }
+#pragma unroll
+            for (int m = 0; m < P; ++m) {
+              kahanAdd(hx[2 * m], cx[2 * m], kSign * vx[m].x);
+              kahanAdd(hx[2 * m + 1], cx[2 * m + 1], kSign * vx[m].y);
+              kahanAdd(hy[2 * m], cy[2 * m], kSign * vy[m].x);
+              kahanAdd(hy[2 * m + 1], cy[2 * m + 1], kSign * vy[m].y);
+              kahanAdd(hz[2 * m], cz[2 * m], kSign * vz[m].x);
+              kahanAdd(hz[2 * m + 1], cz[2 * m + 1], kSign * vz[m].y);
+            }
+            __syncwarp();
+            // lane l: source j0 + l, each component summed over the warp's 32 lanes in lane order
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+              const float* row = myBuf + (c * kSymRed + lane) * kSymPitch;
+              float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+              for (int k = 0; k < 32; k += 2) {
+                a0 += row[k];
+                a1 += row[k + 1];
+              }
+              myCross[c * ST + j0 + lane] = a0 + a1;
+            }
+            __syncwarp();  // the buffer is rewritten by the next 32 sources
+          }
+          __syncthreads();
+          // the four warps' sums of each (component, source), added in warp order; the reverse
+          // term is +sum s_r d (d_ji = -d_ij and rn = -(reciprocal) cancel)
+          for (int o = threadIdx.x; o < 3 * ST; o += NTH) {
+            const int comp = o / ST, jl = o % ST;
+            const int src = b0 + jl;
+            if (src >= send) continue;
+            const float acc = ((sCross[0 * 3 * ST + o] + sCross[1 * 3 * ST + o]) + sCross[2 * 3 * ST + o]) +
+                              sCross[3 * 3 * ST + o];
+            const double v = (double)(NEWTON ? acc : -acc);
+            if (fabs(v) < kSymLimit) {
+              atomicAdd(S.rev + (size_t)comp * ns + src, (unsigned long long)__double2ll_rn(v * kSymScale));
+            } else {
+              atomicExch(S.revBad + src, 1);  // inf/NaN or out of range: the source's result becomes NaN
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    writePartials<NTH, K, false>(S.partial + (size_t)w.chunk * 3 * n, n, slot0, tcount, hx, hy, hz, cx, cy, cz, hp,
+                                 cp, hw, cw);
+  }
+}
+
 constexpr int kFP64Threads = 128;
 constexpr int kFP64Tile = 128;
 constexpr double kFourPi = 4 * kPi;
@@ -564,8 +744,8 @@ __global__ void __launch_bounds__(kFP64Threads) pairFP64(const SolveDev* __restr
     const WorkItem w = items[it];
     const SolveDev& S = solves[w.solve];
     const int n = S.nslots;
-    const int slot = w.tile * kFP64Threads + threadIdx.x;
-    const bool live = slot < n;
+    const int slot = w.tbeg + threadIdx.x;
+    const bool live = slot < w.tend;
     double tx = 0.0, ty = 0.0, tz = 0.0;
     int self = -1;
     if (live) { tx = S.tx[slot]; ty = S.tx[n + slot]; tz = S.tx[2 * n + slot]; self = S.self[slot]; }
@@ -701,6 +881,28 @@ int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, fn, threads, 0) != cudaSuccess) return 0;
   return nb;
+}
+
+int pairSymBlocksPerSM() {
+  static const int nb = [] {
+    for (void* f : {(void*)pairFP32CSym<true>, (void*)pairFP32CSym<false>})
+      if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem) != cudaSuccess) return 0;
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)pairFP32CSym<true>, kSymThreads, kSymSmem) !=
+        cudaSuccess)
+      return 0;
+    return b;
+  }();
+  return nb;
+}
+
+cudaError_t launchPairSym(bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems, int* counter,
+                          int grid, cudaStream_t s) {
+  if (nitems <= 0 || grid <= 0) return cudaSuccess;
+  if (pairSymBlocksPerSM() <= 0) return cudaErrorInvalidConfiguration;
+  void* fn = rcpApprox ? (void*)pairFP32CSym<false> : (void*)pairFP32CSym<true>;
+  void* args[] = {(void*)&solves, (void*)&items, (void*)&nitems, (void*)&counter};
+  return cudaLaunchKernel(fn, dim3(grid), dim3(kSymThreads), args, kSymSmem, s);
 }
 
 cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,

@@ -29,7 +29,7 @@ __device__ __forceinline__ double stageCoef(int stage) { return stage == 3 ? 1.0
 __global__ void __launch_bounds__(kBlock) prepKernel(const SolveStage* __restrict__ stages,
                                                      const int4* __restrict__ map, int stage, int fp32c,
                                                      int* __restrict__ counter) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *counter = 0;
+  if (blockIdx.x == 0 && threadIdx.x == 0) counter[0] = counter[1] = 0;
   const int4 m = map[blockIdx.x];
   const SolveStage& S = stages[m.x];
   const int i = m.y + threadIdx.x;
@@ -72,6 +72,10 @@ __global__ void __launch_bounds__(kBlock) prepKernel(const SolveStage* __restric
       z = z + a * S.kz[stage - 1][t];
     }
     const double circ = -z * io.barea[f];
+    if (S.rev) {  // the symmetric leaf kernel adds into these
+      for (int c = 0; c < 3; ++c) S.rev[(size_t)c * S.ns + i] = 0ull;
+      S.revBad[i] = 0;
+    }
     if (fp32c) {
       float hi[3], lo[3];
       for (int c = 0; c < 3; ++c) { hi[c] = __double2float_rn(x[c]); lo[c] = __double2float_rn(x[c] - (double)hi[c]); }
@@ -87,7 +91,7 @@ __global__ void __launch_bounds__(kBlock) prepKernel(const SolveStage* __restric
 
 __global__ void __launch_bounds__(kBlock) epilogueKernel(const SolveStage* __restrict__ stages,
                                                          const int4* __restrict__ map, int fp32c, int psi,
-                                                         int velocity, int stageOut) {
+                                                         int velocity, int stageOut, int useRev) {
   const int4 m = map[blockIdx.x];
   const SolveStage& S = stages[m.x];
   const int i = m.y + threadIdx.x;
@@ -98,6 +102,14 @@ __global__ void __launch_bounds__(kBlock) epilogueKernel(const SolveStage* __res
   for (int c = 0; c < S.nchunks; ++c) {                 // fixed order: deterministic per target
     const double* P = S.partial + (size_t)c * ncomp * n;
     for (int k = 0; k < ncomp; ++k) v[k] += P[(size_t)k * n + i];
+  }
+  if (useRev && S.rev && S.leaf0 >= 0 && i >= S.leaf0) {   // reverse sums of the symmetric leaf kernel
+    const int k = i - S.leaf0;
+    if (S.revBad[k]) {
+      v[0] = v[1] = v[2] = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+    } else {
+      for (int c = 0; c < 3; ++c) v[c] += (double)(long long)S.rev[(size_t)c * S.ns + k] * (1.0 / kSymScale);
+    }
   }
   double u[3];
   if (fp32c) {                                          // u = x_i x V
@@ -170,10 +182,10 @@ cudaError_t launchPrep(const SolveStage* st, const int4* map, int nblocks, int s
 }
 
 cudaError_t launchEpilogue(const SolveStage* st, const int4* map, int nblocks, Precision prec, bool psi,
-                           bool velocity, int stageOut, cudaStream_t s) {
+                           bool velocity, int stageOut, cudaStream_t s, bool useRev) {
   if (nblocks <= 0) return cudaSuccess;
   epilogueKernel<<<nblocks, kBlock, 0, s>>>(st, map, prec == Precision::FP32C ? 1 : 0, psi ? 1 : 0,
-                                            velocity ? 1 : 0, stageOut);
+                                            velocity ? 1 : 0, stageOut, useRev ? 1 : 0);
   return cudaGetLastError();
 }
 
