@@ -328,26 +328,31 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   for (size_t i = 0; i < items.size(); ++i)
     B.itemPairs[i] = (double)(items[i].tend - items[i].tbeg) * (items[i].s1 - items[i].s0);
 
-  // Symmetric leaf x leaf evaluation of a single solve: the direct kernel keeps the non-leaf
-  // target tiles (vertices, masked parents; slots [0, leaf0)), the symmetric kernel takes the
-  // upper triangle of leaf tiles.  Row I (leaf tile I against tiles I..NT-1) is cut into the
+  // Symmetric leaf x leaf evaluation: the direct kernel keeps each solve's non-leaf target
+  // tiles (vertices, masked parents; slots [0, leaf0)), the symmetric kernel takes the upper
+  // triangle of its leaf tiles.  Row I (leaf tile I against tiles I..NT-1) is cut into the
   // solve's nchunks segments; segment c writes partial chunk c of tile I's slots (an empty
-  // segment writes zeros), so the epilogue's fixed-order chunk sum covers every leaf slot.
+  // segment writes zeros), so the epilogue's fixed-order chunk sum covers every leaf slot.  The
+  // cut depends on the solve alone, and the reverse sums are exact integer adds, so a solve's
+  // result is the same alone, in an ensemble or in the server.
   std::vector<WorkItem> symDirect, symItems;
   if (B.sym) {
-    const SolvePlan& P = *B.solves[0];
     for (const WorkItem& w : items)
-      if (w.tbeg < P.leaf0) symDirect.push_back(w);
-    const int nt = (P.ns + kSymTile - 1) / kSymTile;
-    for (int I = 0; I < nt; ++I) {
-      const int len = nt - I;
-      for (int c = 0; c < P.nchunks; ++c) {
-        WorkItem w{};
-        w.tile = I;
-        w.s0 = I + (int)((int64_t)len * c / P.nchunks);
-        w.s1 = I + (int)((int64_t)len * (c + 1) / P.nchunks);
-        w.chunk = c;
-        symItems.push_back(w);
+      if (w.tbeg < B.solves[w.solve]->leaf0) symDirect.push_back(w);
+    for (size_t m = 0; m < B.solves.size(); ++m) {
+      const SolvePlan& P = *B.solves[m];
+      const int nt = (P.ns + kSymTile - 1) / kSymTile;
+      for (int I = 0; I < nt; ++I) {
+        const int len = nt - I;
+        for (int c = 0; c < P.nchunks; ++c) {
+          WorkItem w{};
+          w.solve = (int)m;
+          w.tile = I;
+          w.s0 = I + (int)((int64_t)len * c / P.nchunks);
+          w.s1 = I + (int)((int64_t)len * (c + 1) / P.nchunks);
+          w.chunk = c;
+          symItems.push_back(w);
+        }
       }
     }
     std::stable_sort(symItems.begin(), symItems.end(),
@@ -1166,6 +1171,7 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
     B.rcpApprox = flags & LPM_BVE_RCP_APPROX;
     const bool sort = !(flags & LPM_BVE_NO_SORT);
     const bool skip = flags & LPM_BVE_SKIP_MASKED_TARGETS;
+    const bool sym = wantSymmetric(Mode::RK4, B.prec, sort, tree, flags);
     auto ioOf = [](const lpm_bve_state* st) {
       ParticleIO io;
       io.na = st->nverts;
@@ -1208,9 +1214,11 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
       io.barea = st->farea;
       B.owned.emplace_back(new SolvePlan());
       B.solves.push_back(B.owned.back().get());
-      const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s);
+      const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s, sym);
       buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), H, s);
     }
+    B.sym = sym;
+    for (const SolvePlan* p : B.solves) B.sym = B.sym && p->leaf0 >= 0;
     finalizeBatch(B, ctx->dev, s);
     if (ctx->verbose)
       std::fprintf(stderr, "[lpm_bve] ensemble: %d solves, %d items, grid %d\n", nsolves, B.nitems, B.grid);

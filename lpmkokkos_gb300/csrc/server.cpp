@@ -239,7 +239,7 @@ size_t estimateBytes(Precision prec, const PairShape& shape, bool skip, int64_t 
   const int chunk = chunkLength((int)ns, shape.srcTile);
   const size_t nchunks = ns > 0 ? (ns + chunk - 1) / chunk : 1;
   const size_t ncomp = (size_t)pairNumComponents(prec, true);
-  size_t plan = 8 * nslots + 12 * ntiles + 8 * ns + 24 * nslots + (prec == Precision::FP32C ? 64 : 32) * ns +
+  size_t plan = 8 * nslots + 12 * ntiles + 8 * ns + 24 * nslots + (prec == Precision::FP32C ? 64 + 28 : 32) * ns +
                 4 * 32 * nslots + 8 * nchunks * ncomp * nslots;
   const size_t bs = (size_t)stageBlockSize();
   size_t tables = 2 * (ntiles * nchunks * sizeof(WorkItem) + (2 * nslots / bs + ns / bs + 4) * sizeof(int4) +
@@ -293,7 +293,11 @@ std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) 
   M->fmask.resize((size_t)M->nf);
   if (lpm_mesh_build(seed, level, M->vx.data(), M->fx.data(), M->farea.data(), M->fmask.data()) != LPM_OK)
     fail(LPM_ERR_INVALID_ARGUMENT, "mesh seed %d level %d", seed, level);
-  M->plan = prepareHostFromHost(Mode::RK4, M->nv, M->nf, M->vx.data(), M->fx.data(), M->fmask.data(), S->skip, true);
+  // FP32C solves take the symmetric layout (leaf x leaf pairs once) unless the server was created
+  // with LPM_BVE_NO_SYMMETRIC
+  const bool sym = S->prec == Precision::FP32C && !(S->flags & LPM_BVE_NO_SYMMETRIC);
+  M->plan = prepareHostFromHost(Mode::RK4, M->nv, M->nf, M->vx.data(), M->fx.data(), M->fmask.data(), S->skip, true,
+                                sym);
   S->meshes[key] = M;
   S->meshOrder.push_back(key);
   if (S->meshOrder.size() > kMeshCache) {
@@ -465,6 +469,8 @@ std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs,
   B->rcpApprox = S->rcp;
   B->mem.streamOrdered(S->up, lane, S->pool);
   for (Req* r : rs) B->solves.push_back(r->plan.get());
+  B->sym = S->prec == Precision::FP32C;
+  for (const SolvePlan* p : B->solves) B->sym = B->sym && p->leaf0 >= 0;
   finalizeBatch(*B, S->dev, S->up);
   return B;
 }
@@ -821,6 +827,10 @@ void gpuLoop(lpm_bve_server* S) {
         SizeClass& C = classes[kg.first];
         if (C.batch->grid != kg.second) {
           C.batch->grid = kg.second;
+          // the symmetric evaluation's two launches run one after the other on the class's lane,
+          // each within the same share
+          C.batch->symDirectGrid = std::min(C.batch->nSymDirectItems, kg.second);
+          C.batch->symGrid = std::min(C.batch->nSymItems, kg.second);
           installStep(S, *C.batch, execs[kg.first]);
         }
       }

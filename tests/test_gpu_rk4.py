@@ -167,21 +167,21 @@ def test_solid_body_rotation(ctx):
     assert err < 0.05  # cubed sphere level 3: discretisation error only
 
 
-@pytest.mark.parametrize("prec", [P.FP64, P.FP32C])
-def test_ensemble_equals_single(ctx, prec):
-    from lpmkokkos_gb300 import bve
-    specs = [(0, 2, 1), (1, 3, 2), (0, 3, 3), (1, 2, 4)]
+@pytest.mark.parametrize("prec,extra", [(P.FP64, 0), (P.FP32C, 0), (P.FP32C, P.NO_SYMMETRIC)])
+def test_ensemble_equals_single(ctx, prec, extra):
+    """Each ensemble member equals its single solve bit for bit, with the symmetric leaf kernel
+    (FP32C default) and with the plain one."""
+    specs = [(0, 2, 1), (1, 3, 2), (0, 3, 3), (1, 2, 4), (0, 4, 5)]
     singles = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
     ens = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
-    dts = [0.01, 0.02, 0.005, 0.01]
+    dts = [0.01, 0.02, 0.005, 0.01, 0.005]
     for s, dt in zip(singles, dts):
-        # ensembles sum every leaf pair in both directions: compare with the same kernel
-        ctx.rk4_step(s.state(), dt, OMEGA, 2, flags=prec | P.NO_SYMMETRIC)
-    e = ctx.ensemble([s.state() for s in ens], flags=prec)
-    e.step(dts, [OMEGA] * 4, 2)
+        ctx.rk4_step(s.state(), dt, OMEGA, 2, flags=prec | extra)
+    e = ctx.ensemble([s.state() for s in ens], flags=prec | extra)
+    e.step(dts, [OMEGA] * len(specs), 2)
     torch.cuda.synchronize()
     info = e.info()
-    assert info["nsolves"] == 4 and info["nitems"] > 0
+    assert info["nsolves"] == len(specs) and info["nitems"] > 0
     for s, t in zip(singles, ens):
         assert _same(s.physFaces, t.physFaces)
         assert _same(s.velocityVerts, t.velocityVerts)
