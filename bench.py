@@ -121,8 +121,8 @@ def parse(argv=None):
     ap.add_argument("--no-parity", action="store_true", help="skip the sampled-target oracle comparison")
     ap.add_argument("--no-secondary", action="store_true", help="c5: skip the level-7 secondary leg")
     ap.add_argument("--no-symmetric", action="store_true",
-                    help="c2/c5: steps with the plain pair kernel (LPM_BVE_NO_SYMMETRIC: every leaf pair in both "
-                         "directions) instead of the symmetric leaf kernel")
+                    help="steps with the plain pair kernel (LPM_BVE_NO_SYMMETRIC: every leaf pair in both "
+                         "directions) instead of the symmetric leaf kernel (c2, c5; c3 ensembles; c4 server)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU-baseline sample budget")
     ap.add_argument("--config", choices=["c2", "c3", "c4", "c5"], default="c5",
                     help="c5: icos L8, eps 0.01, 8 vortices, RK4 steps then the stream function at all targets "
@@ -741,7 +741,8 @@ def run_ensemble(args, rank, world, local_rank):
     dts = [courant_dt(sk, lv) for sk, lv in picks]
     oms = [2 * math.pi] * len(picks)
     initial = [clone_sphere(bve, s) for s in spheres] if not args.no_tree else None
-    ens = ctx.ensemble([s.state() for s in spheres], flags=P.FP32C)
+    eflags = P.FP32C | (P.NO_SYMMETRIC if args.no_symmetric else 0)
+    ens = ctx.ensemble([s.state() for s in spheres], flags=eflags)
     info = ens.info()
     ens.step(dts, oms, max(1, args.warmup))
     torch.cuda.synchronize()
@@ -766,7 +767,7 @@ def run_ensemble(args, rank, world, local_rank):
                                f"(seed {SEED_BASE + 3}), dt at the level-4 Courant number, FP32C",
                    "levels": {f"{'icos' if k[0] == 0 else 'cube'}{k[1]}": picks.count(k) for k in menu},
                    "work_items": info["nitems"], "grid": info["grid"], "device_bytes": info["device_bytes"],
-                   "autotune": bool(args.autotune)},
+                   "autotune": bool(args.autotune), "symmetric_leaf_kernel": not args.no_symmetric},
         "pair_interactions_per_s": world * 4 * alg * args.steps / (el * 1e-3),
         "computed_pairs_per_s": world * 4 * info["pairs_per_eval"] * args.steps / (el * 1e-3),
         "gpu_launches": 13 * args.steps, "init_s": t_init, "all_vertex_velocities_finite": finite,
@@ -895,7 +896,7 @@ def run_server(args, rank, world, local_rank):
     arrivals = np.cumsum(gaps) - gaps[0]
     specs = [dict(seed=int(k), level=int(lv), dt=courant_dt(int(k), int(lv)), nsteps=args.req_steps,
                   ic_seed=SEED_BASE + 4 + i) for i, (k, lv) in enumerate(zip(kinds, lvls))]
-    sflags = P.FP32C | (P.TREECODE if args.tree else 0)
+    sflags = P.FP32C | (P.TREECODE if args.tree else 0) | (P.NO_SYMMETRIC if args.no_symmetric else 0)
     srv = bve.Server(local_rank, flags=sflags)
     # warm-up: one zero-step request per mesh (fills the host mesh/plan cache, loads kernels)
     meshes = sorted({(s["seed"], s["level"]) for s in specs})
