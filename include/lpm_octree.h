@@ -28,8 +28,19 @@ extern "C" {
 typedef struct lpm_octree lpm_octree;
 
 /* Build the tree of n DEVICE points (point i, component c at x[i*x_si + c*x_sc]; 1 <= n < 2^31)
- * with leaves at max_depth (1..10, MAX_OCTREE_DEPTH); neighbors != 0 also fills the
- * neighbour lists.  Queued on `stream`, which is synchronised (the level sizes are read back). */
+ * with leaves at max_depth (1..10, MAX_OCTREE_DEPTH).  `neighbors` is a bit set:
+ *   LPM_OCTREE_NEIGHBORS    also fill the neighbour lists;
+ *   LPM_OCTREE_FIXED_LEVELS the sync-free build the tree code uses: nothing is read back and the
+ *                           stream is not synchronised; level l sits at a fixed base with room for
+ *                           min(8^l, 8 n) nodes (base_address and nnodes_total from
+ *                           lpm_octree_info describe that layout), its first nnodes_per_level[l]
+ *                           nodes hold the same values as the concatenated build's level l, and
+ *                           the rest have an empty point range (count 0).  No neighbour lists;
+ *                           n < 2^28.  lpm_octree_info then synchronises the device to read the
+ *                           level counts and the box.
+ * Without LPM_OCTREE_FIXED_LEVELS the build synchronises `stream` (the level sizes are read back). */
+#define LPM_OCTREE_NEIGHBORS    1
+#define LPM_OCTREE_FIXED_LEVELS 2
 int lpm_octree_build(const double* x, int64_t x_si, int64_t x_sc, int64_t n, int max_depth, int neighbors,
                      lpm_octree** out, lpm_stream_t stream);
 

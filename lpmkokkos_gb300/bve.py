@@ -139,12 +139,16 @@ class _DeviceView:
 
 class Octree:
     """The Morton octree of src/LpmOctree.cpp built on the device (include/lpm_octree.h) over
-    float64 (n, 3) device points; `arrays()` copies its device arrays into torch tensors."""
+    float64 (n, 3) device points; `arrays()` copies its device arrays into torch tensors.
+    fixed_levels: the sync-free build (LPM_OCTREE_FIXED_LEVELS): level l at base_address[l] with
+    room for min(8^l, 8 n) nodes, its first nnodes_per_level[l] nodes filled."""
 
-    def __init__(self, x: torch.Tensor, max_depth: int, neighbors: bool = True, stream=None):
+    def __init__(self, x: torch.Tensor, max_depth: int, neighbors: bool = True, stream=None,
+                 fixed_levels: bool = False):
         assert x.dtype == torch.float64 and x.is_cuda and x.dim() == 2 and x.shape[1] == 3
         h = ctypes.c_void_p()
-        L.check(L.lib().lpm_octree_build(_vp(x), x.stride(0), x.stride(1), x.shape[0], max_depth, int(neighbors),
+        bits = (1 if neighbors else 0) | (2 if fixed_levels else 0)
+        L.check(L.lib().lpm_octree_build(_vp(x), x.stride(0), x.stride(1), x.shape[0], max_depth, bits,
                                          ctypes.byref(h), _stream(stream)))
         self._h = h
         d, nn, n = ctypes.c_int(), ctypes.c_int64(), ctypes.c_int64()

@@ -168,16 +168,29 @@ __global__ void uniqueKernel(const uint64_t* __restrict__ codes, const int* __re
   }
 }
 
-__global__ void uniqueCountKernel(const int* __restrict__ ustart, int nu, int64_t n, int* __restrict__ ucount) {
+// A count that is either known on the host (d == nullptr) or lives in device memory (the
+// sync-free build, whose grids cover an upper bound and whose threads past the count return).
+__device__ __forceinline__ int countOf(const int* d, int h) { return d ? *d : h; }
+
+__global__ void uniqueCountKernel(const int* __restrict__ ustart, int nuHost, const int* __restrict__ nuDev, int64_t n,
+                                  int* __restrict__ ucount) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nu = countOf(nuDev, nuHost);
   if (u >= nu) return;
   ucount[u] = (u + 1 < nu ? ustart[u + 1] : (int)n) - ustart[u];
 }
 
 // NodeSiblingCounter's flags (:186-231): 8 where the parent at level lev-1 changes.
-__global__ void siblingMark(const uint32_t* __restrict__ keys, int m, int lev, int maxDepth, int* __restrict__ flag) {
+// (sync-free build: the grid covers `bound` entries and writes 0 past the count, so that the scan
+// over the bound gives the same prefix sums)
+__global__ void siblingMark(const uint32_t* __restrict__ keys, int mHost, const int* __restrict__ mDev, int div,
+                            int bound, int lev, int maxDepth, int* __restrict__ flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+  const int m = mDev ? *mDev / div : mHost;
+  if (i >= m) {
+    if (mDev && i < bound) flag[i] = 0;
+    return;
+  }
   flag[i] = (i == 0 || parentKey(keys[i], lev, maxDepth) != parentKey(keys[i - 1], lev, maxDepth)) ? 8 : 0;
 }
 
@@ -185,10 +198,11 @@ __global__ void siblingMark(const uint32_t* __restrict__ keys, int m, int lev, i
 // parent follow each other in ascending order, so the 8 candidate keys are matched by a merge
 // walk (the reference binary-searches each; same result).
 __global__ void leafNodes(const uint32_t* __restrict__ ukeys, const int* __restrict__ ustart,
-                          const int* __restrict__ ucount, const int* __restrict__ sib, int nu, int depth,
-                          uint32_t* __restrict__ keys, int2* __restrict__ pt, int* __restrict__ parents,
-                          int* __restrict__ kids, int* __restrict__ nodeOf) {
+                          const int* __restrict__ ucount, const int* __restrict__ sib, int nuHost,
+                          const int* __restrict__ nuDev, int depth, uint32_t* __restrict__ keys, int2* __restrict__ pt,
+                          int* __restrict__ parents, int* __restrict__ kids, int* __restrict__ nodeOf) {
   const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nu = countOf(nuDev, nuHost);
   if (u >= nu) return;
   if (u > 0 && sib[u] == sib[u - 1]) return;
   const int kid0 = sib[u] - 8;
@@ -217,9 +231,12 @@ __global__ void ptInLeafKernel(const int* __restrict__ uidx, const int* __restri
 }
 
 // ParentNodeFunctor (:285-323): one parent per complete sibling set of the lower level.
-__global__ void parentGroups(const uint32_t* __restrict__ lowKeys, const int2* __restrict__ lowPt, int np, int lev,
-                             int maxDepth, uint32_t* __restrict__ pkeys, int2* __restrict__ ppt) {
+// (sync-free build: npDev points at the lower level's node count, np = count / 8)
+__global__ void parentGroups(const uint32_t* __restrict__ lowKeys, const int2* __restrict__ lowPt, int npHost,
+                             const int* __restrict__ lowCountDev, int lev, int maxDepth, uint32_t* __restrict__ pkeys,
+                             int2* __restrict__ ppt) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = lowCountDev ? *lowCountDev / 8 : npHost;
   if (g >= np) return;
   pkeys[g] = parentKey(lowKeys[8 * g], lev + 1, maxDepth);
   int cnt = 0, start = -1;
@@ -234,10 +251,11 @@ __global__ void parentGroups(const uint32_t* __restrict__ lowKeys, const int2* _
 // NodeArrayInternalFunctor (:325-369): complete sibling sets at level lev, kids and the lower
 // level's parents.
 __global__ void internalNodes(const uint32_t* __restrict__ pkeys, const int2* __restrict__ ppt,
-                              const int* __restrict__ sib, int np, int lev, int maxDepth, uint32_t* __restrict__ keys,
-                              int2* __restrict__ pt, int* __restrict__ parents, int* __restrict__ kids,
-                              int* __restrict__ lowParents) {
+                              const int* __restrict__ sib, int npHost, const int* __restrict__ lowCountDev, int lev,
+                              int maxDepth, uint32_t* __restrict__ keys, int2* __restrict__ pt, int* __restrict__ parents,
+                              int* __restrict__ kids, int* __restrict__ lowParents) {
   const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int np = lowCountDev ? *lowCountDev / 8 : npHost;
   if (g >= np) return;
   if (g > 0 && sib[g] == sib[g - 1]) return;
   const int kid0 = sib[g] - 8;
@@ -261,6 +279,16 @@ __global__ void internalNodes(const uint32_t* __restrict__ pkeys, const int2* __
     }
   }
 }
+
+// out = scan[len - 1] (0 for len = 0), len from the device (lenDev) or the host; with div > 1
+// the length is *lenDev / div (the parents of a level's complete sibling sets).
+__global__ void countFromScan(const int* __restrict__ scan, int lenHost, const int* __restrict__ lenDev, int div,
+                              int* __restrict__ out) {
+  const int len = lenDev ? *lenDev / div : lenHost;
+  *out = len > 0 ? scan[len - 1] : 0;
+}
+
+__global__ void setInt(int* __restrict__ p, int v) { *p = v; }
 
 // The root (src/LpmNodeArrayInternal.cpp:13-52): key 0, all points, kids 0..7.
 __global__ void rootNode(const int2* __restrict__ lev1Pt, uint32_t* __restrict__ keys, int2* __restrict__ pt,
@@ -326,7 +354,7 @@ T* Octree::grow(Buf& b, size_t count, cudaStream_t s) {
   const size_t bytes = std::max<size_t>(1, count) * sizeof(T);
   if (!registered_) {
     for (Buf* p : {&bKeys, &bPt, &bPar, &bKids, &bNbrs, &bSorted, &bOrig, &bLeaf, &bBox, &bCodes, &bCodes2, &bFlag,
-                   &bScan, &bUKeys, &bUStart, &bUCount, &bNodeOf, &bSib, &bTemp, &bPart})
+                   &bScan, &bUKeys, &bUStart, &bUCount, &bNodeOf, &bSib, &bTemp, &bPart, &bCount})
       all_.push_back(p);
     for (int l = 0; l <= kOctreeMaxDepth; ++l)
       for (Buf* p : {&bLevKeys[l], &bLevPt[l], &bLevPar[l], &bLevKids[l], &bLevNbrs[l]}) all_.push_back(p);
@@ -408,12 +436,12 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
   int* ucount = grow<int>(bUCount, nu, s);
   int* nodeOf = grow<int>(bNodeOf, nu, s);
   uniqueKernel<<<nb, kBlock, 0, s>>>(codes2, scan, n, ukeys, ustart);
-  uniqueCountKernel<<<blocksFor(nu), kBlock, 0, s>>>(ustart, nu, n, ucount);
+  uniqueCountKernel<<<blocksFor(nu), kBlock, 0, s>>>(ustart, nu, nullptr, n, ucount);
 
   // 5-6. leaves with full sibling sets (the point flags are free again; the point scan is kept
   // for pt_in_leaf)
   int* sib = grow<int>(bSib, nu, s);
-  siblingMark<<<blocksFor(nu), kBlock, 0, s>>>(ukeys, nu, depth, depth, flag);
+  siblingMark<<<blocksFor(nu), kBlock, 0, s>>>(ukeys, nu, nullptr, 1, nu, depth, depth, flag);
   {
     size_t need = 0;
     check(cub::DeviceScan::InclusiveSum(nullptr, need, flag, sib, nu, s), "scan size");
@@ -429,7 +457,7 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
     int2* p = grow<int2>(bLevPt[depth], m, s);
     int* par = grow<int>(bLevPar[depth], m, s);
     int* kd = grow<int>(bLevKids[depth], 8 * (size_t)m, s);
-    leafNodes<<<blocksFor(nu), kBlock, 0, s>>>(ukeys, ustart, ucount, sib, nu, depth, k, p, par, kd, nodeOf);
+    leafNodes<<<blocksFor(nu), kBlock, 0, s>>>(ukeys, ustart, ucount, sib, nu, nullptr, depth, k, p, par, kd, nodeOf);
     ptInLeafKernel<<<nb, kBlock, 0, s>>>(scan, nodeOf, n, ptInLeaf);
   }
 
@@ -440,10 +468,11 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
     uint32_t* pk = grow<uint32_t>(bUKeys, np, s);
     int2* ppt = grow<int2>(bUStart, np, s);
     parentGroups<<<blocksFor(np), kBlock, 0, s>>>(static_cast<uint32_t*>(bLevKeys[lev + 1].p),
-                                                  static_cast<int2*>(bLevPt[lev + 1].p), np, lev, depth, pk, ppt);
+                                                  static_cast<int2*>(bLevPt[lev + 1].p), np, nullptr, lev, depth, pk,
+                                                  ppt);
     int* f = grow<int>(bFlag, np, s);
     int* sc2 = grow<int>(bSib, np, s);
-    siblingMark<<<blocksFor(np), kBlock, 0, s>>>(pk, np, lev, depth, f);
+    siblingMark<<<blocksFor(np), kBlock, 0, s>>>(pk, np, nullptr, 1, np, lev, depth, f);
     size_t need = 0;
     check(cub::DeviceScan::InclusiveSum(nullptr, need, f, sc2, np, s), "scan size");
     temp = grow<unsigned char>(bTemp, need, s);
@@ -455,7 +484,7 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
     int2* p = grow<int2>(bLevPt[lev], m, s);
     int* par = grow<int>(bLevPar[lev], m, s);
     int* kd = grow<int>(bLevKids[lev], 8 * (size_t)m, s);
-    internalNodes<<<blocksFor(np), kBlock, 0, s>>>(pk, ppt, sc2, np, lev, depth, k, p, par, kd,
+    internalNodes<<<blocksFor(np), kBlock, 0, s>>>(pk, ppt, sc2, np, nullptr, lev, depth, k, p, par, kd,
                                                    static_cast<int*>(bLevPar[lev + 1].p));
   }
   cnt[0] = 1;
@@ -504,11 +533,107 @@ void Octree::build(const double* x, int64_t si, int64_t sc, int64_t npts, int ma
   check(cudaGetLastError(), "launch");
 }
 
+void Octree::buildOnDevice(const double* x, int64_t si, int64_t sc, int64_t npts, int maxDepth, cudaStream_t s) {
+  if (maxDepth < 1 || maxDepth > kOctreeMaxDepth) fail(LPM_ERR_INVALID_ARGUMENT, "octree depth must be 1..%d", kOctreeMaxDepth);
+  if (npts <= 0 || npts > INT32_MAX / 8) fail(LPM_ERR_INVALID_ARGUMENT, "octree: 1..2^28-1 points");
+  depth = maxDepth;
+  n = npts;
+  const unsigned nb = blocksFor(n);
+  // capacities: a level holds complete sibling sets of at most 8^l nodes, and at most 8 per
+  // unique leaf key below it (<= n)
+  int64_t cap[kOctreeMaxDepth + 1];
+  int64_t total = 0;
+  for (int l = 0; l <= depth; ++l) {
+    int64_t c = 1;
+    for (int k = 0; k < l && c < 8 * n; ++k) c *= 8;
+    cap[l] = std::min<int64_t>(c, l == 0 ? 1 : 8 * n);
+    gbase[l] = (int)total;
+    base[l] = (int)total;
+    npl[l] = 0;  // counts live on the device (dcount)
+    total += cap[l];
+  }
+  if (total > INT32_MAX / 8) fail(LPM_ERR_NOT_SUPPORTED, "octree: %lld nodes of fixed-level capacity", (long long)total);
+  gbase[depth + 1] = (int)total;
+  nnodes = total;
+  keys = grow<uint32_t>(bKeys, total, s);
+  ptInds = grow<int2>(bPt, total, s);
+  parents = grow<int>(bPar, total, s);
+  kids = grow<int>(bKids, 8 * (size_t)total, s);
+  nbrs = nullptr;
+  dcount = grow<int>(bCount, depth + 2, s);  // [0..depth] node counts, [depth + 1] unique leaf keys
+  int* dNu = dcount + depth + 1;
+  check(cudaMemsetAsync(ptInds, 0, sizeof(int2) * (size_t)total, s), "clear");  // empty past the counts
+
+  // 1. bounding box
+  const int boxBlocks = (int)std::min<int64_t>(nb, 512);
+  double* part = grow<double>(bPart, 6 * (size_t)boxBlocks, s);
+  double* dbx = grow<double>(bBox, 6, s);
+  boxPartial<<<boxBlocks, kBlock, 0, s>>>(x, si, sc, n, part);
+  boxFinal<<<1, kBlock, 0, s>>>(part, boxBlocks, dbx);
+  dbox = dbx;
+
+  // 2-3. codes, sort, permute; unique leaf keys counted on the device
+  uint64_t* codes = grow<uint64_t>(bCodes, n, s);
+  uint64_t* codes2 = grow<uint64_t>(bCodes2, n, s);
+  codesKernel<<<nb, kBlock, 0, s>>>(x, si, sc, n, depth, dbx, codes);
+  int* flag = grow<int>(bFlag, n, s);
+  int* scan = grow<int>(bScan, n, s);
+  size_t tsort = 0, tscan = 0;
+  check(cub::DeviceRadixSort::SortKeys(nullptr, tsort, codes, codes2, (int)n, 0, 32 + 3 * depth, s), "sort size");
+  check(cub::DeviceScan::InclusiveSum(nullptr, tscan, flag, scan, (int)n, s), "scan size");  // the longest scan
+  void* temp = grow<unsigned char>(bTemp, std::max(tsort, tscan), s);
+  size_t tb = bTemp.bytes;
+  check(cub::DeviceRadixSort::SortKeys(temp, tb, codes, codes2, (int)n, 0, 32 + 3 * depth, s), "sort");
+  sorted = grow<double>(bSorted, 3 * (size_t)n, s);
+  origIds = grow<int>(bOrig, n, s);
+  ptInLeaf = grow<int>(bLeaf, n, s);
+  permuteKernel<<<nb, kBlock, 0, s>>>(codes2, x, si, sc, n, sorted, origIds, flag);
+  tb = bTemp.bytes;
+  check(cub::DeviceScan::InclusiveSum(temp, tb, flag, scan, (int)n, s), "scan");
+  countFromScan<<<1, 1, 0, s>>>(scan, (int)n, nullptr, 1, dNu);
+
+  // 4. unique keys (room for n of them) and the leaf level's complete sibling sets
+  uint32_t* ukeys = grow<uint32_t>(bUKeys, n, s);
+  int* ustart = grow<int>(bUStart, 2 * (size_t)n, s);  // later the parents' int2 point ranges
+  int* ucount = grow<int>(bUCount, n, s);
+  int* nodeOf = grow<int>(bNodeOf, n, s);
+  int* sib = grow<int>(bSib, n, s);
+  uniqueKernel<<<nb, kBlock, 0, s>>>(codes2, scan, n, ukeys, ustart);
+  uniqueCountKernel<<<nb, kBlock, 0, s>>>(ustart, 0, dNu, n, ucount);
+  siblingMark<<<nb, kBlock, 0, s>>>(ukeys, 0, dNu, 1, (int)n, depth, depth, flag);
+  tb = bTemp.bytes;
+  check(cub::DeviceScan::InclusiveSum(temp, tb, flag, sib, (int)n, s), "scan");
+  countFromScan<<<1, 1, 0, s>>>(sib, 0, dNu, 1, dcount + depth);
+  const int gd = gbase[depth];
+  leafNodes<<<nb, kBlock, 0, s>>>(ukeys, ustart, ucount, sib, 0, dNu, depth, keys + gd, ptInds + gd, parents + gd,
+                                  kids + 8 * (size_t)gd, nodeOf);
+  ptInLeafKernel<<<nb, kBlock, 0, s>>>(scan, nodeOf, n, ptInLeaf);
+
+  // 5. internal levels bottom-up, each at its fixed base (nothing to concatenate afterwards)
+  for (int lev = depth - 1; lev >= 1; --lev) {
+    const int npB = (int)(cap[lev + 1] / 8);  // bound on the parents of the lower level's sets
+    const int gl = gbase[lev], gu = gbase[lev + 1];
+    uint32_t* pk = ukeys;                          // (the leaf kernels that read ukeys ran before)
+    int2* ppt = reinterpret_cast<int2*>(ustart);
+    parentGroups<<<blocksFor(npB), kBlock, 0, s>>>(keys + gu, ptInds + gu, 0, dcount + lev + 1, lev, depth, pk, ppt);
+    siblingMark<<<blocksFor(npB), kBlock, 0, s>>>(pk, 0, dcount + lev + 1, 8, npB, lev, depth, flag);
+    tb = bTemp.bytes;
+    check(cub::DeviceScan::InclusiveSum(temp, tb, flag, sib, npB, s), "scan");
+    countFromScan<<<1, 1, 0, s>>>(sib, 0, dcount + lev + 1, 8, dcount + lev);
+    internalNodes<<<blocksFor(npB), kBlock, 0, s>>>(pk, ppt, sib, 0, dcount + lev + 1, lev, depth, keys + gl,
+                                                    ptInds + gl, parents + gl, kids + 8 * (size_t)gl, parents + gu);
+  }
+  rootNode<<<1, 32, 0, s>>>(ptInds + gbase[1], keys, ptInds, parents, kids, parents + gbase[1], nullptr);
+  setInt<<<1, 1, 0, s>>>(dcount, 1);
+  check(cudaGetLastError(), "launch");
+}
+
 }  // namespace lpm
 
 struct lpm_octree {
   lpm::Octree tree;
   int device = 0;
+  bool fixed = false;  // LPM_OCTREE_FIXED_LEVELS: counts and box still on the device
 };
 
 extern "C" {
@@ -519,11 +644,19 @@ int lpm_octree_build(const double* x, int64_t x_si, int64_t x_sc, int64_t n, int
   *out = nullptr;
   if (!x || n <= 0 || n > INT32_MAX || x_si < 0 || x_sc < 0 || max_depth < 1 || max_depth > lpm::kOctreeMaxDepth)
     return LPM_ERR_INVALID_ARGUMENT;
+  const bool fixed = neighbors & LPM_OCTREE_FIXED_LEVELS;
+  if ((neighbors & ~(LPM_OCTREE_NEIGHBORS | LPM_OCTREE_FIXED_LEVELS)) ||
+      (fixed && (neighbors & LPM_OCTREE_NEIGHBORS)) || (fixed && n > INT32_MAX / 8))
+    return LPM_ERR_INVALID_ARGUMENT;
   lpm_octree* t = new (std::nothrow) lpm_octree();
   if (!t) return LPM_ERR_OUT_OF_MEMORY;
   try {
     lpm::check(cudaGetDevice(&t->device), "device");
-    t->tree.build(x, x_si, x_sc, n, max_depth, neighbors != 0, (cudaStream_t)stream);
+    t->fixed = fixed;
+    if (fixed)
+      t->tree.buildOnDevice(x, x_si, x_sc, n, max_depth, (cudaStream_t)stream);
+    else
+      t->tree.build(x, x_si, x_sc, n, max_depth, neighbors & LPM_OCTREE_NEIGHBORS, (cudaStream_t)stream);
   } catch (const lpm::Error& e) {
     std::fprintf(stderr, "lpm_octree_build: %s\n", e.msg.c_str());
     delete t;
@@ -540,7 +673,15 @@ int lpm_octree_build(const double* x, int64_t x_si, int64_t x_sc, int64_t n, int
 int lpm_octree_info(const lpm_octree* t, int* max_depth, int64_t* nnodes_total, int64_t* npoints,
                     int32_t* nnodes_per_level, int32_t* base_address, double* box) {
   if (!t) return LPM_ERR_INVALID_ARGUMENT;
-  const lpm::Octree& T = t->tree;
+  lpm::Octree& T = const_cast<lpm_octree*>(t)->tree;
+  if (t->fixed) {  // the sync-free build left its level counts and box on the device
+    int cnt[lpm::kOctreeMaxDepth + 2] = {};
+    if (cudaSetDevice(t->device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(cnt, T.dcount, sizeof(int) * (T.depth + 1), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(T.box, T.dbox, sizeof(T.box), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return LPM_ERR_CUDA;
+    for (int l = 0; l <= T.depth; ++l) T.npl[l] = cnt[l];
+  }
   if (max_depth) *max_depth = T.depth;
   if (nnodes_total) *nnodes_total = T.nnodes;
   if (npoints) *npoints = T.n;

@@ -36,6 +36,16 @@ class Octree {
   void build(const double* x, int64_t si, int64_t sc, int64_t n, int depth, bool neighbors, cudaStream_t s,
              bool hostBox = true);
 
+  // Sync-free build for the tree code: the same tree, its levels stored at fixed capacities --
+  // level l at gbase[l] (= base[l]) with room for min(8^l, 8 n) nodes, nnodes = the total
+  // capacity -- and the node counts kept on the device (dcount[0..depth]); nodes past a level's
+  // count have an empty point range (ptInds.y = 0) and are never reached from the root.  Nothing
+  // is read back, and a rebuild with the same n and depth allocates nothing, so after a first
+  // build the call can be captured in a CUDA graph.  No neighbour lists.
+  void buildOnDevice(const double* x, int64_t si, int64_t sc, int64_t n, int depth, cudaStream_t s);
+  int gbase[kOctreeMaxDepth + 2] = {};
+  int* dcount = nullptr;              // device [depth + 2]: node counts per level, then the unique leaf keys
+
   int depth = 0;
   int64_t n = 0, nnodes = 0;
   int base[kOctreeMaxDepth + 1] = {};
@@ -62,7 +72,7 @@ class Octree {
   void releaseAll();
 
   Buf bKeys, bPt, bPar, bKids, bNbrs, bSorted, bOrig, bLeaf, bBox;
-  Buf bCodes, bCodes2, bFlag, bScan, bUKeys, bUStart, bUCount, bNodeOf, bSib, bTemp, bPart;
+  Buf bCodes, bCodes2, bFlag, bScan, bUKeys, bUStart, bUCount, bNodeOf, bSib, bTemp, bPart, bCount;
   Buf bLevKeys[kOctreeMaxDepth + 1], bLevPt[kOctreeMaxDepth + 1], bLevPar[kOctreeMaxDepth + 1],
       bLevKids[kOctreeMaxDepth + 1], bLevNbrs[kOctreeMaxDepth + 1];
   std::vector<Buf*> all_;

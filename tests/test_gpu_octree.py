@@ -94,3 +94,28 @@ def test_neighbour_tables_on_a_second_device(oracle):
         t1 = bve.Octree(torch.from_numpy(x).cuda(1), 3)
         _same(t1, oracle.octree(x, 3))
         t1.close()
+
+
+@pytest.mark.parametrize("seed,level,depth", [(1, 6, 4), (0, 7, 5), (0, 5, 1), (1, 4, 6)])
+def test_fixed_level_build_equals_concatenated(oracle, seed, level, depth):
+    """The sync-free build (LPM_OCTREE_FIXED_LEVELS, used by the tree code): every level's first
+    nnodes_per_level[l] nodes at its fixed base equal the oracle's level l (keys, point ranges,
+    parents, kids), the rest have empty point ranges; per-point arrays equal the oracle's."""
+    x = _source_coords(seed, level)
+    ref = oracle.octree(x, depth)
+    t = bve.Octree(torch.from_numpy(x).cuda(), depth, neighbors=False, fixed_levels=True)
+    T = t.arrays()
+    assert np.array_equal(t.nnodes_per_level, ref["nnodes_per_level"])
+    assert np.array_equal(t.box, ref["box"])
+    pt = T["pt_inds"].cpu().numpy()
+    for lev in range(depth + 1):
+        b, m, rb = t.base_address[lev], ref["nnodes_per_level"][lev], ref["base_address"][lev]
+        cap = (t.base_address[lev + 1] if lev < depth else t.nnodes) - b
+        assert cap >= m
+        assert np.array_equal(T["keys"][b:b + m], ref["keys"][rb:rb + m]), lev
+        for name in ("pt_inds", "parents", "kids"):
+            assert np.array_equal(T[name].cpu().numpy()[b:b + m], ref[name][rb:rb + m]), (lev, name)
+        assert (pt[b + m:b + cap, 1] == 0).all(), lev
+    for name in ("sorted_pts", "orig_ids", "pt_in_leaf"):
+        assert np.array_equal(T[name].cpu().numpy(), ref[name]), name
+    t.close()
