@@ -430,26 +430,19 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
   std::unique_ptr<NvtxRange> pairRange(names ? new NvtxRange(names->pair) : nullptr);
   if (B.treeMode) {  // tree code: per solve octree, lists and gathered pair kernel; one epilogue
     const size_t n = B.solves.size();
-    B.treeStageHost.resize(n);
     // solves below the size threshold: one persistent direct launch over their work items
     if (B.nDirectItems > 0)
       LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.directItems, B.nDirectItems,
                           B.counter, std::min(B.nDirectItems, B.slots), s));
     for (size_t m = 0; m < n; ++m) {
       TreeEval& T = *B.trees[m];
-      SolveStage st = B.solves[m]->stage;
-      if (B.treeDirect[m]) {
+      if (B.treeDirect[m])
         T.markDirect(*B.solves[m]);
-      } else {
+      else
         T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
-        st.partial = T.partial();
-        st.nchunks = T.nchunks();
-      }
-      B.treeStageHost[m] = st;
     }
     pairRange.reset();
-    // (the next evaluation's first octree build synchronises before this host table changes)
-    LPM_CUDA(cudaMemcpyAsync(B.treeStageDev, B.treeStageHost.data(), n * sizeof(SolveStage), cudaMemcpyHostToDevice, s));
+    treeStageTable(B, s);
     std::unique_ptr<NvtxRange> epi(names ? new NvtxRange(names->epilogue) : nullptr);
     LPM_CUDA(launchEpilogue(B.treeStageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s));
     return;
@@ -477,6 +470,25 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
   pairRange.reset();
   std::unique_ptr<NvtxRange> epi(names ? new NvtxRange(names->epilogue) : nullptr);
   LPM_CUDA(launchEpilogue(B.stageDev, B.slotMap, B.nSlotBlocks, B.prec, psi, velocity, stageOut, s, sym));
+}
+
+// The epilogue's stage table of a tree-code batch: each solve's stage with its tree partial sums.
+// Uploaded only when it changes, so that a captured step holds no upload from pageable memory.
+void treeStageTable(Batch& B, cudaStream_t s) {
+  const size_t n = B.solves.size();
+  std::vector<SolveStage> cur(n);
+  for (size_t m = 0; m < n; ++m) {
+    cur[m] = B.solves[m]->stage;
+    const TreeEval& T = *B.trees[m];
+    if (!B.treeDirect[m] && T.partial()) {
+      cur[m].partial = T.partial();
+      cur[m].nchunks = T.nchunks();
+    }
+  }
+  if (B.treeStageHost.size() != n || std::memcmp(cur.data(), B.treeStageHost.data(), n * sizeof(SolveStage)) != 0) {
+    B.treeStageHost = cur;
+    LPM_CUDA(cudaMemcpyAsync(B.treeStageDev, B.treeStageHost.data(), n * sizeof(SolveStage), cudaMemcpyHostToDevice, s));
+  }
 }
 
 // One RK4 step (src/LpmBVERK4_Impl.hpp:42-130) for every solve of the batch, its launches named
@@ -1033,12 +1045,27 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
     const bool rcp = flags & LPM_BVE_RCP_APPROX;
     B.rcpApprox = rcp;
     useTree(ctx, B, tree, s);
-    if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // the tree build reads sizes back: no capture
+    // The tree code reads nothing back once its evaluations are sized (the first one), so its steps
+    // are captured too; the graph is rebuilt when an evaluation's buffers or arguments change
+    // (after a list overflow, reported without a synchronisation).
+    bool treeReady = false;
+    int treeGen = 0;
+    if (tree) {
+      treeReady = !B.trees.empty();
+      for (auto& t : B.trees) {
+        t->poll();
+        treeReady = treeReady && t->ready();
+        treeGen += t->generation();
+      }
+      if (treeReady) treeStageTable(B, s);
+    }
+    if ((flags & LPM_BVE_NO_GRAPH) || ctx->timer || (tree && !treeReady)) {
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
       B.timer = nullptr;
     } else {
-      if (B.graph && (B.graphQuirk != quirk || B.graphRenorm != renorm || B.graphRcp != rcp)) {
+      if (B.graph && (B.graphQuirk != quirk || B.graphRenorm != renorm || B.graphRcp != rcp || B.graphTree != tree ||
+                      (tree && B.graphTreeGen != treeGen))) {
         cudaGraphExecDestroy(B.graph);
         B.graph = nullptr;
       }
@@ -1059,6 +1086,9 @@ int lpm_bve_rk4_step(lpm_bve_ctx* ctx, const lpm_bve_state* st, double dt, doubl
         B.graphQuirk = quirk;
         B.graphRenorm = renorm;
         B.graphRcp = rcp;
+        B.graphTree = tree;
+        B.graphTreeGen = 0;
+        for (auto& t : B.trees) B.graphTreeGen += tree ? t->generation() : 0;
       }
       for (int k = 0; k < nsteps; ++k) LPM_CUDA(cudaGraphLaunch(B.graph, s));
     }
@@ -1256,11 +1286,27 @@ int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* O
     const bool renorm = E->flags & LPM_BVE_RENORM;
     const bool tree = E->flags & LPM_BVE_TREECODE;
     useTree(ctx, B, tree, s);
-    if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer || tree) {  // tree steps read sizes back: no capture
+    // tree-code ensembles are captured once every solve's evaluation is sized (as in rk4_step)
+    bool treeReady = false;
+    int treeGen = 0;
+    if (tree) {
+      treeReady = !B.trees.empty();
+      for (auto& t : B.trees) {
+        t->poll();
+        treeReady = treeReady && t->ready();
+        treeGen += t->generation();
+      }
+      if (treeReady) treeStageTable(B, s);
+    }
+    if ((E->flags & LPM_BVE_NO_GRAPH) || ctx->timer || (tree && !treeReady)) {
       B.timer = ctx->timer.get();
       for (int k = 0; k < nsteps; ++k) enqueueStep(B, quirk, renorm, s);
       B.timer = nullptr;
     } else {
+      if (B.graph && tree && B.graphTreeGen != treeGen) {
+        cudaGraphExecDestroy(B.graph);
+        B.graph = nullptr;
+      }
       if (!B.graph) {
         cudaGraph_t g = nullptr;
         LPM_CUDA(cudaStreamBeginCapture(ctx->capture, cudaStreamCaptureModeThreadLocal));
@@ -1275,6 +1321,8 @@ int lpm_bve_ensemble_step(lpm_bve_ensemble* E, const double* dt, const double* O
         const cudaError_t ie = cudaGraphInstantiate(&B.graph, g, 0);
         cudaGraphDestroy(g);
         LPM_CUDA(ie);
+        B.graphTreeGen = 0;
+        for (auto& t : B.trees) B.graphTreeGen += tree ? t->generation() : 0;
       }
       for (int k = 0; k < nsteps; ++k) LPM_CUDA(cudaGraphLaunch(B.graph, s));
     }

@@ -228,7 +228,8 @@ struct Batch {
   int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)
   // captured RK4 step
   cudaGraphExec_t graph = nullptr;
-  bool graphQuirk = false, graphRenorm = false, graphRcp = false;
+  bool graphQuirk = false, graphRenorm = false, graphRcp = false, graphTree = false;
+  int graphTreeGen = 0;  // the tree evaluations' generation the graph was captured with
   ~Batch() {
     if (graph) cudaGraphExecDestroy(graph);
   }
@@ -268,6 +269,8 @@ struct EvalNames;
 void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s,
                  const EvalNames* names = nullptr);
 void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
+// Uploads a tree-code batch's epilogue stage table when it changed.
+void treeStageTable(Batch& B, cudaStream_t s);
 
 // Snapshot file of a state held in host row-major arrays (snapshot.cpp).
 void writeSnapshotHost(const char* path, int seed, int level, int vpf, int64_t nv, int64_t nf, double t, double dt,

@@ -11,7 +11,10 @@
 
 #include "tree_eval.hpp"
 
+#include <cub/cub.cuh>
+
 #include <algorithm>
+#include <cstring>
 #include <cfloat>
 #include <climits>
 #include <cmath>
@@ -308,11 +311,12 @@ __global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ t
                                                Levels lv, int depth, double theta, int P, int ns,
                                                int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
                                                const int64_t* __restrict__ listOff, int* __restrict__ list,
-                                               int* __restrict__ err) {
+                                               const int* __restrict__ overflow, int* __restrict__ err) {
   __shared__ int stack[kWarpStack];
   const int tile = blockIdx.x;
   const int lane = threadIdx.x;
   if (tile >= ntiles) return;
+  if (FILL && *overflow) return;  // the lists do not fit: the pair kernel sums every source instead
   const double4_32a tg = tileGeom[tile];
   if (lane == 0) stack[0] = 0;  // the root (level 0, global index 0)
   __syncwarp();
@@ -406,6 +410,70 @@ __global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ t
   }
 }
 
+// The list buffer's capacity check, before the fill: overflow = total > capacity.
+__global__ void capCheck(const int64_t* __restrict__ total, int64_t cap, int* __restrict__ overflow) {
+  *overflow = *total > cap ? 1 : 0;
+}
+
+// After the fill: the evaluation's report to the host, in mapped host memory (read without a
+// synchronisation before a later evaluation): overflow (sticky until the host grows the
+// buffer), the largest list total seen, a traversal stack overflow.
+__global__ void report(const int64_t* __restrict__ total, const int* __restrict__ overflow,
+                       const int* __restrict__ stackErr, TreeWatch* __restrict__ w) {
+  const long long t = *total;
+  if (t > w->maxTotal) w->maxTotal = t;
+  if (*overflow) w->overflow = 1;
+  if (*stackErr) w->stackErr = 1;
+}
+
+// Sort keys of the work order: tiles by descending list length, ties by tile index.
+__global__ void orderKeys(const int64_t* __restrict__ lens, int ntiles, uint64_t* __restrict__ keys) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  const uint64_t l = (uint64_t)min(lens[t], (int64_t)INT32_MAX);
+  keys[t] = ((uint64_t)INT32_MAX - l) << 32 | (uint32_t)t;
+}
+
+// Work items: each tile's list in nchunks parts, tiles in key order, a tile's parts in order.
+__global__ void expandOrder(const uint64_t* __restrict__ keys, int ntiles, int nchunks, int* __restrict__ order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ntiles * nchunks) return;
+  const int t = (int)(uint32_t)keys[i / nchunks];
+  order[i] = t * nchunks + i % nchunks;
+}
+
+// Statistics of the evaluation (fixed-order block sums): pairs, direct pairs, far (proxy) pairs,
+// far clusters and the octree's nodes.  With overflowing lists every tile took every source.
+__global__ void __launch_bounds__(kBlock) treeStats(const int2* __restrict__ tiles, const int64_t* __restrict__ lens,
+                                                    const int64_t* __restrict__ fars, int ntiles, int P, int ns,
+                                                    const int* __restrict__ overflow, const int* __restrict__ dcount,
+                                                    int depth, double* __restrict__ out) {
+  __shared__ double sh[kBlock / 32];
+  const bool dir = *overflow != 0;
+  double pairs = 0, far = 0, clusters = 0;
+  for (int t = threadIdx.x; t < ntiles; t += kBlock) {
+    const double tc = (double)tiles[t].y;
+    pairs += tc * (double)(dir ? ns : lens[t]);
+    if (!dir) {
+      far += tc * (double)fars[t];
+      clusters += (double)(fars[t] / max(1, P));
+    }
+  }
+  pairs = blockSum<kBlock>(pairs, sh);
+  far = blockSum<kBlock>(far, sh);
+  clusters = blockSum<kBlock>(clusters, sh);
+  if (threadIdx.x == 0) {
+    double nodes = 0;
+    if (dcount)
+      for (int l = 0; l <= depth; ++l) nodes += dcount[l];
+    out[0] = pairs;
+    out[1] = pairs - far;
+    out[2] = far;
+    out[3] = clusters;
+    out[4] = nodes;
+  }
+}
+
 inline unsigned blocks(int64_t n, int b = kBlock) { return (unsigned)((n + b - 1) / b); }
 
 void ck(cudaError_t e, const char* what) {
@@ -442,6 +510,48 @@ TreeEval::~TreeEval() {
   cudaDeviceSynchronize();
   for (Buf* b : all_)
     if (b->p) cudaFree(b->p);
+  if (watch_) cudaFreeHost(watch_);
+}
+
+void TreeEval::ensureWatch() {
+  if (watch_) return;
+  void* h = nullptr;
+  ck(cudaHostAlloc(&h, sizeof(TreeWatch), cudaHostAllocMapped), "host allocation");
+  watch_ = static_cast<TreeWatch*>(h);
+  std::memset(watch_, 0, sizeof(TreeWatch));
+  void* d = nullptr;
+  ck(cudaHostGetDevicePointer(&d, h, 0), "mapped pointer");
+  dWatch_ = static_cast<TreeWatch*>(d);
+}
+
+bool TreeEval::poll() {
+  if (!watch_) return false;
+  volatile TreeWatch* w = watch_;
+  if (w->stackErr) {
+    w->stackErr = 0;
+    fail(LPM_ERR_INTERNAL, "tree code: traversal stack overflow (octree depth %d)", tree_.depth);
+  }
+  if (!w->overflow) return false;
+  // an evaluation since the last poll did not fit its lists (it summed every source instead):
+  // room for the largest total seen, with headroom, from the next evaluation on
+  listCap_ = std::max<int64_t>(listCap_, (int64_t)(1.25 * (double)w->maxTotal) + 4096);
+  w->overflow = 0;
+  ++generation_;
+  return true;
+}
+
+const TreeStats& TreeEval::stats() {
+  if (statsOnDevice_) {
+    double v[5] = {};
+    ck(cudaDeviceSynchronize(), "synchronise");
+    ck(cudaMemcpy(v, bStats.p, sizeof(v), cudaMemcpyDeviceToHost), "read-back");
+    stats_.pairs = v[0];
+    stats_.directPairs = v[1];
+    stats_.farPairs = v[2];
+    stats_.farClusters = (int64_t)v[3];
+    stats_.nodes = (int64_t)v[4];
+  }
+  return stats_;
 }
 
 void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& shape, bool psi, bool precise,
@@ -451,8 +561,12 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   if (!treePairShapeSupported(shape)) fail(LPM_ERR_NOT_SUPPORTED, "tree code: plan built for another launch shape");
   const int ns = Pl.ns, nslots = Pl.nslots, ntiles = Pl.nTreeTiles;
   const int P = (tp.degree + 1) * (tp.degree + 1);
+  ensureWatch();
+  poll();  // reports of earlier evaluations (no synchronisation)
+  direct_ = false;
   stats_ = TreeStats{};
-  // phase timing (with the context's timer): events at the phase boundaries, read at the sync
+  statsOnDevice_ = true;
+  // phase timing (with the context's timer): events at the phase boundaries, read at the end
   cudaEvent_t ev[5] = {};
   if (timer)
     for (auto& e : ev) e = timer->get();
@@ -468,16 +582,17 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   float4* tsp1 = nullptr;
   double4_32a* geom = nullptr;
   int* approx = nullptr;
+  int depth = 0;
   if (ns > 0) {
-    // 1-3. octree over the stage positions, sources in key order
+    // 1-3. octree over the stage positions (fixed-level layout, counts on the device), sources in
+    // key order
     double* pos = grow<double>(bPos, 3 * (size_t)ns, s);
     srcPositions<<<blocks(ns), kBlock, 0, s>>>(Pl.stage.sp0, Pl.stage.sp1, ns, pos);
-    const int depth = treeDepthFor(ns, tp.leafPoints);
-    tree_.build(pos, 3, 1, ns, depth, false, s, /*hostBox=*/false);  // the next sync: the list lengths
+    depth = treeDepthFor(ns, tp.leafPoints);
+    tree_.buildOnDevice(pos, 3, 1, ns, depth, s);
     mark(1);
-    nnodes = (int)tree_.nnodes;
+    nnodes = (int)tree_.nnodes;  // capacity: nodes past a level's count are empty
     stats_.depth = depth;
-    stats_.nodes = nnodes;
     const size_t nrec = (size_t)ns + (size_t)nnodes * P;
     tsp0 = grow<float4>(bSp0, nrec, s);
     tsp1 = grow<float4>(bSp1, nrec, s);
@@ -488,7 +603,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     int* ss = grow<int>(bSelf, nslots, s);
     sortedSelf<<<blocks(nslots), kBlock, 0, s>>>(Pl.dev.self, inv, nslots, ss);
     selfSorted = ss;
-    // 4. upward pass
+    // 4. upward pass (empty nodes return at once)
     geom = grow<double4_32a>(bGeom, nnodes, s);
     approx = grow<int>(bApprox, nnodes, s);
     upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns,
@@ -507,72 +622,66 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   // 5. tiles
   double4_32a* tgeom = grow<double4_32a>(bTileGeom, ntiles, s);
   tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
-  // 6. interaction lists: lengths, offsets and launch order on the host, then the indices
+  // 6. interaction lists: lengths, offsets (a device scan), the work order (a device sort) and
+  // the indices -- nothing read back but the very first total, which sizes the list buffer
   int64_t* lens = grow<int64_t>(bLen, ntiles, s);
   int64_t* fars = grow<int64_t>(bFar, ntiles, s);
   Levels lv{};
   for (int l = 0; l <= tree_.depth; ++l) lv.base[l] = tree_.base[l];
   lv.base[tree_.depth + 1] = nnodes;
-  int* terr = grow<int>(bErr, 1, s);
-  ck(cudaMemsetAsync(terr, 0, sizeof(int), s), "memset");
+  int* terr = grow<int>(bErr, 2, s);  // [0] stack overflow, [1] list overflow
+  int* overflow = terr + 1;
+  ck(cudaMemsetAsync(terr, 0, 2 * sizeof(int), s), "memset");
   if (ns > 0) {
     traverse<false><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                          tp.theta, P, ns, lens, fars, nullptr, nullptr, terr);
+                                          tp.theta, P, ns, lens, fars, nullptr, nullptr, overflow, terr);
   } else {
     ck(cudaMemsetAsync(lens, 0, sizeof(int64_t) * ntiles, s), "memset");
     ck(cudaMemsetAsync(fars, 0, sizeof(int64_t) * ntiles, s), "memset");
   }
   mark(3);
-  hLen_.resize(ntiles);
-  hFar_.resize(ntiles);
-  // tile sizes, for the pair statistics (read every time: a rebuilt plan may reuse an old address)
-  hTiles_.resize(ntiles);
-  ck(cudaMemcpyAsync(hTiles_.data(), Pl.treeTiles, sizeof(int2) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
-  ck(cudaMemcpyAsync(hLen_.data(), lens, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
-  ck(cudaMemcpyAsync(hFar_.data(), fars, sizeof(int64_t) * ntiles, cudaMemcpyDeviceToHost, s), "read-back");
-  int herr = 0;
-  ck(cudaMemcpyAsync(&herr, terr, sizeof(int), cudaMemcpyDeviceToHost, s), "read-back");
-  ck(cudaStreamSynchronize(s), "synchronise");
-  if (herr) fail(LPM_ERR_INTERNAL, "tree code: traversal stack overflow (octree depth %d)", tree_.depth);
-  hOff_.assign((size_t)ntiles + 1, 0);
-  for (int t = 0; t < ntiles; ++t) {
-    hOff_[t + 1] = hOff_[t] + hLen_[t];
-    const double tc = (double)hTiles_[t].y;
-    stats_.pairs += tc * (double)hLen_[t];
-    stats_.farPairs += tc * (double)hFar_[t];
-    stats_.farClusters += hFar_[t] / std::max(1, P);
+  int64_t* off = grow<int64_t>(bOff, (size_t)ntiles + 1, s);
+  uint64_t* keys = grow<uint64_t>(bKey, ntiles, s);
+  uint64_t* keys2 = grow<uint64_t>(bKey2, ntiles, s);
+  size_t tscan = 0, tsort = 0;
+  ck(cub::DeviceScan::InclusiveSum(nullptr, tscan, lens, off + 1, ntiles, s), "scan size");
+  ck(cub::DeviceRadixSort::SortKeys(nullptr, tsort, keys, keys2, ntiles, 0, 64, s), "sort size");
+  void* temp = grow<unsigned char>(bTemp, std::max(tscan, tsort), s);
+  size_t tb = bTemp.bytes;
+  ck(cudaMemsetAsync(off, 0, sizeof(int64_t), s), "memset");
+  ck(cub::DeviceScan::InclusiveSum(temp, tb, lens, off + 1, ntiles, s), "scan");
+  if (listCap_ == 0) {  // the first evaluation sizes the list buffer (its one synchronisation)
+    int64_t total = 0;
+    ck(cudaMemcpyAsync(&total, off + ntiles, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read-back");
+    ck(cudaStreamSynchronize(s), "synchronise");
+    listCap_ = (int64_t)(1.25 * (double)total) + 4096;
+    ++generation_;
   }
-  stats_.directPairs = stats_.pairs - stats_.farPairs;
+  int* oldList = static_cast<int*>(bList.p);
+  int* list = grow<int>(bList, (size_t)listCap_, s);
+  if (list != oldList) ++generation_;
+  capCheck<<<1, 1, 0, s>>>(off + ntiles, listCap_, overflow);
   // Work items: each tile's list in `nchunks` parts (enough items for ~8 waves of CTAs), each
-  // part with its own partial chunk; tiles by descending list length (ties by tile index), a
-  // tile's parts in order.  One sort of packed 64-bit keys over the tiles: the host part of an
-  // evaluation is on its critical path.
+  // part with its own partial chunk; tiles by descending list length (ties by tile index).
   const int nchunks = std::max(1, std::min(16, (8 * std::max(1, slots) + ntiles - 1) / std::max(1, ntiles)));
   const int nitems = ntiles * nchunks;
-  hKey_.resize(ntiles);
-  for (int t = 0; t < ntiles; ++t) {
-    const uint64_t l = (uint64_t)std::min<int64_t>(hLen_[t], INT32_MAX);
-    hKey_[t] = ((uint64_t)INT32_MAX - l) << 32 | (uint32_t)t;
-  }
-  std::sort(hKey_.begin(), hKey_.end());
-  hOrder_.resize(nitems);
-  for (int i = 0; i < ntiles; ++i) {
-    const int t = (int)(uint32_t)hKey_[i];
-    for (int p = 0; p < nchunks; ++p) hOrder_[(size_t)i * nchunks + p] = t * nchunks + p;
-  }
-  int64_t* off = grow<int64_t>(bOff, (size_t)ntiles + 1, s);
   int* order = grow<int>(bOrder, nitems, s);
-  int* list = grow<int>(bList, (size_t)std::max<int64_t>(1, hOff_[ntiles]), s);
-  ck(cudaMemcpyAsync(off, hOff_.data(), sizeof(int64_t) * (ntiles + 1), cudaMemcpyHostToDevice, s), "upload");
-  ck(cudaMemcpyAsync(order, hOrder_.data(), sizeof(int) * nitems, cudaMemcpyHostToDevice, s), "upload");
+  orderKeys<<<blocks(ntiles), kBlock, 0, s>>>(lens, ntiles, keys);
+  tb = bTemp.bytes;
+  ck(cub::DeviceRadixSort::SortKeys(temp, tb, keys, keys2, ntiles, 0, 64, s), "sort");
+  expandOrder<<<blocks(nitems), kBlock, 0, s>>>(keys2, ntiles, nchunks, order);
   if (ns > 0)
     traverse<true><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                         tp.theta, P, ns, nullptr, nullptr, off, list, terr);
+                                         tp.theta, P, ns, nullptr, nullptr, off, list, overflow, terr);
+  report<<<1, 1, 0, s>>>(off + ntiles, overflow, terr, dWatch_);
+  double* dstats = grow<double>(bStats, 5, s);
+  treeStats<<<1, kBlock, 0, s>>>(Pl.treeTiles, lens, fars, ntiles, P, ns, overflow, ns > 0 ? tree_.dcount : nullptr,
+                                 depth, dstats);
   mark(4);
   // 7. the gathered pair kernel
   double* partial = grow<double>(bPartial, (size_t)nchunks * 5 * std::max(1, nslots), s);
-  TreeDev& hd = hDev_;
-  hd = TreeDev{};
+  TreeDev hd;
+  std::memset(&hd, 0, sizeof(hd));  // compared byte for byte with the last upload below
   hd.tx = Pl.stage.tx;
   hd.sp0 = tsp0;
   hd.sp1 = tsp1;
@@ -584,13 +693,19 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hd.list = list;
   hd.order = order;
   hd.partial = partial;
+  hd.overflow = overflow;
   hd.nslots = nslots;
   hd.ntiles = ntiles;
   hd.nchunks = nchunks;
   hd.ns = ns;
   hd.eps2 = Pl.eps2;
   TreeDev* dd = grow<TreeDev>(bDev, 1, s);
-  ck(cudaMemcpyAsync(dd, &hd, sizeof(hd), cudaMemcpyHostToDevice, s), "upload");
+  if (dd != devAt_ || std::memcmp(&hd, &hDev_, sizeof(hd)) != 0) {  // unchanged between evaluations of a plan
+    hDev_ = hd;
+    devAt_ = dd;
+    ck(cudaMemcpyAsync(dd, &hDev_, sizeof(hd), cudaMemcpyHostToDevice, s), "upload");
+    ++generation_;
+  }
   partial_ = partial;
   nchunks_ = nchunks;
   int* counter = grow<int>(bCounter, 1, s);
@@ -615,7 +730,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     ck(cudaEventElapsedTime(&d, ev[3], ev[4]), "event");
     stats_.buildMs = a;
     stats_.upwardMs = b;
-    stats_.listMs = c + d;  // tile geometry and count traversal, then the fill traversal
+    stats_.listMs = c + d;  // tile geometry and count traversal, then offsets, order and the fill
     for (auto& e : ev) timer->pool.push_back(e);
   }
 }

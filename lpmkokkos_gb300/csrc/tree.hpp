@@ -52,6 +52,7 @@ struct TreeDev {
   const int* list;         // flattened per-tile source indices into sp0/sp1
   const int* order;        // [ntiles * nchunks] work items (tile * nchunks + part), longest first
   double* partial;         // [nchunks][ncomp][nslots]: part c of every tile's list sums into chunk c
+  const int* overflow;     // nonzero: the lists did not fit their buffer; every tile sums every source
   int nslots, ntiles, nchunks, ns;
   double eps2;
 };

@@ -7,22 +7,46 @@
 
 namespace lpm {
 
+// What an evaluation reports back to the host without a synchronisation: device writes into
+// mapped host memory, read before a later evaluation or a graph replay.
+struct TreeWatch {
+  int overflow;        // a list total exceeded the buffer (that evaluation summed every source)
+  int stackErr;        // a traversal stack overflowed (cannot happen for depth <= 10)
+  long long maxTotal;  // largest list total seen
+};
+
 class TreeEval {
  public:
   // One evaluation for the solve P: builds the source octree over the stage positions the prep
   // kernel wrote, the proxies and the per-tile index lists, and runs the gathered pair kernel
   // into this object's partial buffer ([nchunks()][ncomp][slot]), which the epilogue then sums.
-  // Synchronises `s` (octree level sizes, list lengths).
+  // Nothing is read back except on the first evaluation (the list total that sizes the list
+  // buffer): sizes and counts stay on the device, the lists go to a buffer of fixed capacity,
+  // and an evaluation whose lists do not fit sums every source directly (exact) and reports the
+  // overflow, so the buffer grows before the next one.  After the first evaluation, and while
+  // generation() stays the same, a call queues the same launches with the same arguments: the
+  // calls can be captured in a CUDA graph and replayed.
   void evaluate(SolvePlan& P, const TreeParams& tp, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
                 int slots, PairTimer* timer, cudaStream_t s);
+  // Applies the reports of evaluations since the last call (no synchronisation): grows the list
+  // buffer after an overflow; true if that changed the launch arguments (a captured graph of
+  // the evaluation must then be rebuilt).  Throws on a traversal stack overflow.
+  bool poll();
+  // Ready to be captured: sized by a first evaluation and no growth pending.
+  bool ready() const { return (direct_ || listCap_ > 0) && !(watch_ && watch_->overflow); }
+  // Changes whenever buffers or launch arguments change (graphs capture them).
+  int generation() const { return generation_; }
   // Records that this solve's evaluation used the direct sum (smaller than TreeParams::minPairs).
   void markDirect(const SolvePlan& P) {
+    direct_ = true;
+    statsOnDevice_ = false;
     stats_ = TreeStats{};
     stats_.pairs = stats_.directPairs = (double)P.nslots * P.ns;
   }
   double* partial() const { return partial_; }
   int nchunks() const { return nchunks_; }
-  const TreeStats& stats() const { return stats_; }
+  // Statistics of the last evaluation (reads the device: synchronises).
+  const TreeStats& stats();
 
  private:
   struct Buf {
@@ -41,18 +65,22 @@ class TreeEval {
  private:
   Octree tree_;
   TreeStats stats_;
+  void ensureWatch();
   Buf bPos, bSp0, bSp1, bInv, bSelf, bGeom, bApprox, bTileGeom, bLen, bFar, bOff, bOrder, bList, bPartial,
-      bDev, bCounter, bErr, bSlot;
-  std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bLen,
-                         &bFar, &bOff, &bOrder, &bList, &bPartial, &bDev, &bCounter, &bErr, &bSlot};
+      bDev, bCounter, bErr, bSlot, bKey, bKey2, bTemp, bStats;
+  std::vector<Buf*> all_{&bPos, &bSp0, &bSp1, &bInv, &bSelf, &bGeom, &bApprox, &bTileGeom, &bLen, &bFar, &bOff,
+                         &bOrder, &bList, &bPartial, &bDev, &bCounter, &bErr, &bSlot, &bKey, &bKey2, &bTemp, &bStats};
   double* partial_ = nullptr;
   int nchunks_ = 1;
-  // host source of the last upload (an evaluation synchronises before it rewrites it)
+  int64_t listCap_ = 0;          // entries of the list buffer (0: not sized yet)
+  bool direct_ = false;          // the solve is below the size threshold (direct sum)
+  int generation_ = 0;
+  bool statsOnDevice_ = false;
+  TreeWatch* watch_ = nullptr;   // mapped host memory
+  TreeWatch* dWatch_ = nullptr;  // its device address
+  // the uploaded kernel description (re-uploaded only when it changes)
   TreeDev hDev_{};
-  std::vector<int64_t> hLen_, hFar_, hOff_;
-  std::vector<int2> hTiles_;
-  std::vector<int> hOrder_;
-  std::vector<uint64_t> hKey_;  // tiles by descending list length (then tile index), for the order
+  TreeDev* devAt_ = nullptr;
 };
 
 // Octree depth whose leaves hold about `leafPoints` of n points on the sphere: the nonempty
