@@ -207,6 +207,11 @@ int lpm_sphere_tangency(const double* x, int64_t x_si, int64_t x_sc, const doubl
  * source pairs keeps the direct sum (the tree's fixed costs exceed its savings below ~1e9 pairs; in
  * an ensemble the small solves share one direct launch).  Defaults 8, 0.6, 512, 1e9. */
 int lpm_bve_ctx_set_treecode(lpm_bve_ctx* ctx, int degree, double theta, int leaf_points, double min_pairs);
+/* Symmetric leaf kernel (FP32C collocated velocity, RK4 steps, ensembles): plans built afterwards
+ * compute each leaf-leaf pair once for solves with at least min_leaves leaf sources (default
+ * 65,536: below that its second launch per evaluation costs more than it saves; 0 = every solve).
+ * A solve's result does not depend on the batch it runs in; the server uses the default. */
+int lpm_bve_ctx_set_symmetric(lpm_bve_ctx* ctx, int64_t min_leaves);
 /* Statistics of the context's last tree-code evaluation: octree depth and node count, far-field
  * clusters taken over all tiles, target x source pairs evaluated (direct + proxy), and -- with
  * timing enabled (lpm_bve_ctx_set_timing) -- phase_ms[3] = milliseconds of the octree build, the

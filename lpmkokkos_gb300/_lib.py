@@ -136,6 +136,7 @@ def _declare(L):
                                                vp]
     L.lpm_sphere_tangency.argtypes = [vp, c_i64, c_i64, vp, c_i64, c_i64, c_i64, vp, vp]
     L.lpm_bve_ctx_set_treecode.argtypes = [vp, ctypes.c_int, ctypes.c_double, ctypes.c_int, ctypes.c_double]
+    L.lpm_bve_ctx_set_symmetric.argtypes = [vp, c_i64]
     L.lpm_bve_ctx_tree_stats.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(c_i64),
                                          ctypes.POINTER(c_i64), c_dp, c_dp, c_dp, c_dp]
     L.lpm_octree_build.argtypes = [vp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int, ctypes.POINTER(vp), vp]

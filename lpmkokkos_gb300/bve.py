@@ -331,6 +331,11 @@ class Context:
         fewer than min_pairs target x source pairs keep the direct sum."""
         L.check(self._lib.lpm_bve_ctx_set_treecode(self.handle, degree, theta, leaf_points, min_pairs), self.handle)
 
+    def set_symmetric(self, min_leaves: int = 65536):
+        """Solves with at least min_leaves leaf sources compute each leaf-leaf pair once (FP32C
+        collocated velocity and RK4 steps; plans built afterwards); 0 = every solve."""
+        L.check(self._lib.lpm_bve_ctx_set_symmetric(self.handle, int(min_leaves)), self.handle)
+
     def tree_stats(self) -> dict:
         """Octree depth and nodes, far clusters and pairs of the last tree-code evaluation."""
         d, nodes, far = ctypes.c_int(), L.c_i64(), L.c_i64()

@@ -51,7 +51,7 @@ void checkVec(const char* name, const void* p, int64_t n, int64_t si, int64_t sc
 }
 
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
-                     cudaStream_t s, bool symLayout) {
+                     cudaStream_t s, bool symLayout, int64_t symMinLeaves) {
   std::vector<uint8_t> hmask((size_t)io.nb, 0);
   if (mask && io.nb > 0) {
     LPM_CUDA(cudaMemcpyAsync(hmask.data(), mask, (size_t)io.nb, cudaMemcpyDeviceToHost, s));
@@ -63,11 +63,12 @@ HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool 
     hb = fetchPoints(io.bx.p, io.nb, io.bx.si, io.bx.sc, s);
   }
   return prepareHostFromHost(mode, io.na, io.nb, ha.empty() ? nullptr : ha.data(), hb.empty() ? nullptr : hb.data(),
-                             hmask.data(), skipMasked, sort, symLayout);
+                             hmask.data(), skipMasked, sort, symLayout, symMinLeaves);
 }
 
 HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
-                             const uint8_t* hmaskIn, bool skipMasked, bool sort, bool symLayout) {
+                             const uint8_t* hmaskIn, bool skipMasked, bool sort, bool symLayout,
+                             int64_t symMinLeaves) {
   HostPlan H;
   H.na = na;
   H.nb = nb;
@@ -77,7 +78,11 @@ HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha
 
   // Target slots: particle ids (a: id = i; face f: id = na + f).  With the symmetric layout the
   // leaves are left out here and appended in source order below.
-  const bool sym = symLayout && sort && mode != Mode::Distinct;
+  int64_t nleaves = 0;
+  for (int64_t f = 0; f < nb; ++f) nleaves += hmask[f] ? 0 : 1;
+  const bool sym = symLayout && sort && mode != Mode::Distinct && nleaves >= std::max<int64_t>(1, symMinLeaves);
+  H.symWanted = symLayout;
+  H.symMin = symMinLeaves;
   std::vector<int> ids;
   if (mode != Mode::Collocated)
     for (int64_t i = 0; i < na; ++i) ids.push_back((int)i);
@@ -149,6 +154,8 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   P.nslots = nslots;
   P.ns = ns;
   P.leaf0 = H.leaf0;
+  P.symWanted = H.symWanted;
+  P.symMin = H.symMin;
   // Target tiles of tileSize slots; with the symmetric layout a tile boundary falls at leaf0, so
   // no tile mixes the Morton-ordered non-leaf slots with the leaves (a mixed tile would join
   // distant parts of the sphere).
@@ -337,10 +344,11 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
   // result is the same alone, in an ensemble or in the server.
   std::vector<WorkItem> symDirect, symItems;
   if (B.sym) {
-    for (const WorkItem& w : items)
-      if (w.tbeg < B.solves[w.solve]->leaf0) symDirect.push_back(w);
+    for (const WorkItem& w : items)  // solves without the layout keep every tile here
+      if (B.solves[w.solve]->leaf0 < 0 || w.tbeg < B.solves[w.solve]->leaf0) symDirect.push_back(w);
     for (size_t m = 0; m < B.solves.size(); ++m) {
       const SolvePlan& P = *B.solves[m];
+      if (P.leaf0 < 0) continue;
       const int nt = (P.ns + kSymTile - 1) / kSymTile;
       for (int I = 0; I < nt; ++I) {
         const int len = nt - I;
@@ -530,6 +538,7 @@ struct lpm_bve_ctx {
   // (collocated) evaluation on the same sources, so both stay cached instead of being rebuilt
   // call after call
   std::unique_ptr<lpm::Batch> velPlans[2];
+  int64_t symMinLeaves = lpm::kSymMinLeaves;  // lpm_bve_ctx_set_symmetric
   std::unique_ptr<lpm::Batch> rkBatch;
   std::unique_ptr<lpm::PairTimer> timer;  // set while timing is enabled
   lpm::PairShape forced{0, 0, 0, 0};       // FP32C launch shape chosen by the caller (threads 0 = none)
@@ -572,7 +581,7 @@ bool sameVec(const DVec& a, const DVec& b) { return a.p == b.p && a.si == b.si &
 bool sameGeometry(const lpm_bve_ctx* ctx, const Batch* B, Mode mode, Precision prec, const ParticleIO& io,
                   const uint8_t* mask, bool skipMasked, bool sort, double eps, bool tree, bool sym) {
   if (!B || B->solves.size() != 1) return false;
-  if ((B->solves[0]->leaf0 >= 0) != sym) return false;
+  if (B->solves[0]->symWanted != sym || (sym && B->solves[0]->symMin != ctx->symMinLeaves)) return false;
   if (!(shapeFor(ctx, prec, tree) == B->shape)) return false;
   const SolvePlan& P = *B->solves[0];
   return P.mode == mode && P.prec == prec && P.io.na == io.na && P.io.nb == io.nb && sameVec(P.io.ax, io.ax) &&
@@ -595,9 +604,9 @@ bool wantSymmetric(Mode mode, Precision prec, bool sort, bool tree, unsigned fla
 std::unique_ptr<Batch> makeSingle(lpm_bve_ctx* ctx, Mode mode, Precision prec, const ParticleIO& io,
                                   const uint8_t* mask, bool skipMasked, bool sort, double eps, bool precise,
                                   bool tree, cudaStream_t s, bool sym) {
-  const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s, sym);
+  const HostPlan H = prepareHost(mode, io, mask, skipMasked, sort, s, sym, ctx->symMinLeaves);
   auto B = std::make_unique<Batch>();
-  B->sym = H.leaf0 >= 0 && H.srcFace.size() > 0;
+  B->sym = H.leaf0 >= 0 && H.srcFace.size() > 0;  // (the layout needs enough leaves: prepareHost)
   B->prec = prec;
   B->shape = shapeFor(ctx, prec, tree);
   if (!tree && prec == Precision::FP32C && ctx->autotune && ctx->forced.threads == 0)
@@ -874,6 +883,12 @@ int lpm_bve_ctx_timing(lpm_bve_ctx* ctx, double* pair_ms, int64_t* pair_launches
   } catch (const std::exception& e) {
     return handle(ctx, fromStd(e));
   }
+  return LPM_OK;
+}
+
+int lpm_bve_ctx_set_symmetric(lpm_bve_ctx* ctx, int64_t min_leaves) {
+  if (!ctx || min_leaves < 0) return LPM_ERR_INVALID_ARGUMENT;
+  ctx->symMinLeaves = min_leaves;
   return LPM_OK;
 }
 
@@ -1244,11 +1259,11 @@ int lpm_bve_ensemble_create(lpm_bve_ctx* ctx, const lpm_bve_state* states, int n
       io.barea = st->farea;
       B.owned.emplace_back(new SolvePlan());
       B.solves.push_back(B.owned.back().get());
-      const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s, sym);
+      const HostPlan H = prepareHost(Mode::RK4, io, st->fmask, skip, sort, s, sym, ctx->symMinLeaves);
       buildSolve(*B.solves.back(), Mode::RK4, B.prec, io, st->fmask, skip, sort, eps, B.shape.tileSize(), H, s);
     }
-    B.sym = sym;
-    for (const SolvePlan* p : B.solves) B.sym = B.sym && p->leaf0 >= 0;
+    B.sym = false;
+    for (const SolvePlan* p : B.solves) B.sym = B.sym || (p->leaf0 >= 0 && p->ns > 0);
     finalizeBatch(B, ctx->dev, s);
     if (ctx->verbose)
       std::fprintf(stderr, "[lpm_bve] ensemble: %d solves, %d items, grid %d\n", nsolves, B.nitems, B.grid);

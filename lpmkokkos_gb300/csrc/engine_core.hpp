@@ -146,6 +146,8 @@ struct SolvePlan {
   std::vector<int2> tileSelfHost;
   std::vector<int> tileStart;  // [ntiles + 1] first slot of each target tile (tiles never straddle leaf0)
   int leaf0 = -1;  // symmetric layout: slots [leaf0, nslots) are the sources in source order
+  bool symWanted = false;      // the plan was built asking for the symmetric layout ...
+  int64_t symMin = 0;          // ... for solves of at least this many leaf sources
   // tree-code target tiles: runs of <= tileSize slots inside one level-3 Morton cell
   int nTreeTiles = 0;
   int2* treeTiles = nullptr;    // [nTreeTiles] {first slot, count}
@@ -248,16 +250,23 @@ struct HostPlan {
   std::vector<int> ids, srcFace, self, srcSlot;
   std::vector<uint32_t> slotKeys;  // Morton key of each slot (sorted plans only)
   int leaf0 = -1;                  // symmetric layout: first leaf slot (-1: plain layout)
+  bool symWanted = false;
+  int64_t symMin = 0;
 };
 
 // symLayout (collocated / RK4 plans, sorted): the non-leaf target slots (vertices, masked faces)
 // first in Morton order, then every leaf in source order, so that leaf slot leaf0 + k is source
 // k -- the layout of the symmetric leaf x leaf kernel.
+// The layout is taken only by solves with at least symMinLeaves leaf sources (below that the
+// second launch per evaluation costs more than the halved leaf pairs save).
 HostPlan prepareHost(Mode mode, const ParticleIO& io, const uint8_t* mask, bool skipMasked, bool sort,
-                     cudaStream_t s, bool symLayout = false);
+                     cudaStream_t s, bool symLayout = false, int64_t symMinLeaves = 0);
 // Same from host arrays: ha (na x 3) and hb (nb x 3) row-major positions, hmask (nb bytes).
 HostPlan prepareHostFromHost(Mode mode, int64_t na, int64_t nb, const double* ha, const double* hb,
-                             const uint8_t* hmask, bool skipMasked, bool sort, bool symLayout = false);
+                             const uint8_t* hmask, bool skipMasked, bool sort, bool symLayout = false,
+                             int64_t symMinLeaves = 0);
+// Default symMinLeaves: 64 leaf tiles (icosahedral level 6, cubed sphere level 7 and up).
+constexpr int64_t kSymMinLeaves = 65536;
 void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, const uint8_t* mask, bool skipMasked,
                 bool sort, double eps, int tileSize, const HostPlan& H, cudaStream_t s);
 int chunkLength(int ns, int srcTile);

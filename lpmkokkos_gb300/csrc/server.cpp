@@ -297,7 +297,7 @@ std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) 
   // with LPM_BVE_NO_SYMMETRIC
   const bool sym = S->prec == Precision::FP32C && !(S->flags & LPM_BVE_NO_SYMMETRIC);
   M->plan = prepareHostFromHost(Mode::RK4, M->nv, M->nf, M->vx.data(), M->fx.data(), M->fmask.data(), S->skip, true,
-                                sym);
+                                sym, kSymMinLeaves);
   S->meshes[key] = M;
   S->meshOrder.push_back(key);
   if (S->meshOrder.size() > kMeshCache) {
@@ -469,8 +469,8 @@ std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs,
   B->rcpApprox = S->rcp;
   B->mem.streamOrdered(S->up, lane, S->pool);
   for (Req* r : rs) B->solves.push_back(r->plan.get());
-  B->sym = S->prec == Precision::FP32C;
-  for (const SolvePlan* p : B->solves) B->sym = B->sym && p->leaf0 >= 0;
+  B->sym = false;  // solves below the layout's size threshold keep the plain kernel in the same batch
+  for (const SolvePlan* p : B->solves) B->sym = B->sym || (p->leaf0 >= 0 && p->ns > 0);
   finalizeBatch(*B, S->dev, S->up);
   return B;
 }

@@ -170,17 +170,24 @@ def test_solid_body_rotation(ctx):
 @pytest.mark.parametrize("prec,extra", [(P.FP64, 0), (P.FP32C, 0), (P.FP32C, P.NO_SYMMETRIC)])
 def test_ensemble_equals_single(ctx, prec, extra):
     """Each ensemble member equals its single solve bit for bit, with the symmetric leaf kernel
-    (FP32C default) and with the plain one."""
-    specs = [(0, 2, 1), (1, 3, 2), (0, 3, 3), (1, 2, 4), (0, 4, 5)]
-    singles = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
-    ens = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
-    dts = [0.01, 0.02, 0.005, 0.01, 0.005]
-    for s, dt in zip(singles, dts):
-        ctx.rk4_step(s.state(), dt, OMEGA, 2, flags=prec | extra)
-    e = ctx.ensemble([s.state() for s in ens], flags=prec | extra)
-    e.step(dts, [OMEGA] * len(specs), 2)
-    torch.cuda.synchronize()
-    info = e.info()
+    and with the plain one.  For FP32C the context's threshold is lowered to 1,000 leaf sources,
+    so that the icosahedral level-3 and level-4 solves take the symmetric layout and the others
+    (96 to 384 leaves) do not: a mixed batch."""
+    if prec == P.FP32C:
+        ctx.set_symmetric(1000)
+    try:
+        specs = [(0, 2, 1), (1, 3, 2), (0, 3, 3), (1, 2, 4), (0, 4, 5)]
+        singles = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
+        ens = [_sphere(ctx, sd, lv, prec, rseed=r) for sd, lv, r in specs]
+        dts = [0.01, 0.02, 0.005, 0.01, 0.005]
+        for s, dt in zip(singles, dts):
+            ctx.rk4_step(s.state(), dt, OMEGA, 2, flags=prec | extra)
+        e = ctx.ensemble([s.state() for s in ens], flags=prec | extra)
+        e.step(dts, [OMEGA] * len(specs), 2)
+        torch.cuda.synchronize()
+        info = e.info()
+    finally:
+        ctx.set_symmetric(65536)
     assert info["nsolves"] == len(specs) and info["nitems"] > 0
     for s, t in zip(singles, ens):
         assert _same(s.physFaces, t.physFaces)

@@ -23,6 +23,22 @@ TOL = 1e-6
 OMEGA = 2 * math.pi
 
 
+@pytest.fixture(scope="module")
+def sctx(native):
+    """A context that takes the symmetric kernel at every size (the default starts at 65,536
+    leaf sources), so that small, ragged and single-tile meshes exercise it."""
+    c = bve.Context(0)
+    c.set_symmetric(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(autouse=True)
+def _fresh(sctx):
+    yield
+    sctx.invalidate()
+
+
 def _l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
@@ -37,7 +53,8 @@ def _setup(seed, level, rseed=7, mask=True):
 
 
 @pytest.mark.parametrize("seed,level", [(0, 0), (1, 2), (0, 3), (1, 4), (0, 5), (1, 5), (0, 6)])
-def test_collocated_against_oracle_and_plain_kernel(ctx, oracle, seed, level):
+def test_collocated_against_oracle_and_plain_kernel(sctx, oracle, seed, level):
+    ctx = sctx
     m, fx, z, a, mk, zh = _setup(seed, level)
     leaf = m["fmask"] == 0
     u_sym, _ = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED)
@@ -49,13 +66,13 @@ def test_collocated_against_oracle_and_plain_kernel(ctx, oracle, seed, level):
     assert _l2(us, up) <= TOL, _l2(us, up)
 
 
-def test_no_mask_every_face_a_source(ctx, oracle):
+def test_no_mask_every_face_a_source(sctx, oracle):
     """No mask pointer: all 6,820 faces of icosahedral level 4 are sources and symmetric-kernel
     leaves (not a multiple of the tile), parents included.  Parents have zero area, so the true
     leaves' values are the well-conditioned ones compared here; a leaf with a zero-area parent
     exactly on it is NaN in the reference (0/0) and left out."""
     m, fx, z, a, _, zh = _setup(0, 4, mask=False)
-    u, _ = ctx.velocity(None, fx, z, a, None, flags=P.FP32C | P.COLLOCATED)
+    u, _ = sctx.velocity(None, fx, z, a, None, flags=P.FP32C | P.COLLOCATED)
     torch.cuda.synchronize()
     nomask = np.zeros(m["nfaces"], np.uint8)
     _, ref = oracle.velocity(m["vx"][:0], m["fx"], zh, m["farea"], nomask)
@@ -64,7 +81,8 @@ def test_no_mask_every_face_a_source(ctx, oracle):
     assert _l2(u.cpu().numpy()[leaf], ref[leaf]) <= TOL
 
 
-def test_repeatable_bitwise(ctx):
+def test_repeatable_bitwise(sctx):
+    ctx = sctx
     m, fx, z, a, mk, _ = _setup(0, 5)
     u1, _ = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED)
     u1 = u1.clone()
@@ -74,15 +92,15 @@ def test_repeatable_bitwise(ctx):
 
 
 @pytest.mark.parametrize("extra", [0, P.SKIP_MASKED_TARGETS, P.RCP_APPROX])
-def test_rk4_against_fp64_and_plain(ctx, extra):
+def test_rk4_against_fp64_and_plain(sctx, extra):
     """Three RK4 steps at icosahedral level 5 with the symmetric kernel, against the FP64 RK4
     (FP32C bar) and against the plain FP32C kernel."""
     runs = {}
     for name, flags in (("sym", P.FP32C | extra), ("plain", P.FP32C | P.NO_SYMMETRIC | extra),
                         ("fp64", P.FP64 | (extra & P.SKIP_MASKED_TARGETS))):
         s = bve.BVESphere(0, 5)
-        s.init_vorticity(bve.rh54_gaussians(11, 3), ctx, flags=P.FP64)
-        ctx.rk4_step(s.state(), 0.005, OMEGA, 3, flags=flags)
+        s.init_vorticity(bve.rh54_gaussians(11, 3), sctx, flags=P.FP64)
+        sctx.rk4_step(s.state(), 0.005, OMEGA, 3, flags=flags)
         torch.cuda.synchronize()
         runs[name] = s
     leaf = runs["fp64"].mesh["fmask"] == 0
@@ -96,7 +114,8 @@ def test_rk4_against_fp64_and_plain(ctx, extra):
         assert _l2(g, q) <= TOL, (attr, _l2(g, q))
 
 
-def test_eps_and_stream_function(ctx, oracle):
+def test_eps_and_stream_function(sctx, oracle):
+    ctx = sctx
     """eps = 0.01; with PSI the call takes the plain kernel (the symmetric one sums velocity
     only) and the result still meets the bar."""
     m, fx, z, a, mk, zh = _setup(1, 5)
@@ -108,3 +127,23 @@ def test_eps_and_stream_function(ctx, oracle):
     assert _l2(u.cpu().numpy()[leaf], ref[leaf]) <= TOL
     assert _l2(u2.cpu().numpy()[leaf], ref[leaf]) <= TOL
     assert _l2(p2.cpu().numpy()[leaf], rp[leaf]) <= TOL
+
+
+def test_size_threshold(ctx):
+    """The layout is a per-solve choice: below the threshold a solve's bits equal the plain
+    kernel's (LPM_BVE_NO_SYMMETRIC), at or above it the symmetric kernel runs (other rounding,
+    same bar).  The default threshold is 65,536 leaf sources."""
+    ctx.set_symmetric(6000)
+    try:
+        for seed, level, sym in ((0, 4, False), (1, 5, True)):   # 5,120 and 6,144 leaves
+            m, fx, z, a, mk, _ = _setup(seed, level)
+            leaf = torch.from_numpy(m["fmask"] == 0).cuda()
+            u, _ = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED)
+            u = u.clone()
+            q, _ = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED | P.NO_SYMMETRIC)
+            torch.cuda.synchronize()
+            same = torch.equal(u[leaf], q[leaf])
+            assert same != sym, (seed, level)
+            assert _l2(u[leaf].cpu().numpy(), q[leaf].cpu().numpy()) <= TOL
+    finally:
+        ctx.set_symmetric(65536)
