@@ -250,7 +250,7 @@ void buildSolve(SolvePlan& P, Mode mode, Precision prec, const ParticleIO& io, c
   S.ns = ns;
   S.leaf0 = H.leaf0;
   if (H.leaf0 >= 0 && prec == Precision::FP32C) {  // reverse sums of the symmetric leaf kernel
-    S.rev = M.alloc<unsigned long long>(3 * (size_t)std::max(1, ns));
+    S.rev = M.alloc<unsigned long long>(4 * (size_t)std::max(1, ns));
     S.revBad = M.alloc<int>(std::max(1, ns));
   }
 
@@ -368,7 +368,8 @@ void finalizeBatch(Batch& B, const DeviceInfo& dev, cudaStream_t s) {
     B.nSymDirectItems = (int)symDirect.size();
     B.nSymItems = (int)symItems.size();
     B.symDirectGrid = std::min(B.nSymDirectItems, slots);
-    B.symGrid = std::min(B.nSymItems, std::max(1, dev.sms * pairSymBlocksPerSM()));
+    B.symGrid = std::min(B.nSymItems, std::max(1, dev.sms * pairSymBlocksPerSM(false)));
+    B.symGridPsi = std::min(B.nSymItems, std::max(1, dev.sms * pairSymBlocksPerSM(true)));
   }
 
   const int bs = stageBlockSize();
@@ -447,7 +448,7 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
       if (B.treeDirect[m])
         T.markDirect(*B.solves[m]);
       else
-        T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.timer, s);
+        T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.treeGrid, B.timer, s);
     }
     pairRange.reset();
     treeStageTable(B, s);
@@ -461,12 +462,13 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
     e1 = B.timer->get();
     LPM_CUDA(cudaEventRecord(e0, s));
   }
-  // symmetric leaf x leaf evaluation: velocity only (the stream function keeps the plain path)
-  const bool sym = B.sym && !psi && !B.precise;
+  // symmetric leaf x leaf evaluation (velocity, and the stream function when asked)
+  const bool sym = B.sym && !B.precise;
   if (sym) {
-    LPM_CUDA(launchPair(B.prec, B.shape, false, false, B.rcpApprox, B.solveDev, B.symDirectItems, B.nSymDirectItems,
+    LPM_CUDA(launchPair(B.prec, B.shape, psi, false, B.rcpApprox, B.solveDev, B.symDirectItems, B.nSymDirectItems,
                         B.counter, B.symDirectGrid, s));
-    LPM_CUDA(launchPairSym(B.rcpApprox, B.solveDev, B.symItems, B.nSymItems, B.counter + 1, B.symGrid, s));
+    LPM_CUDA(launchPairSym(psi, B.rcpApprox, B.solveDev, B.symItems, B.nSymItems, B.counter + 1,
+                           psi ? B.symGridPsi : B.symGrid, s));
   } else {
     LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.items, B.nitems, B.counter,
                         B.grid, s));
@@ -747,6 +749,20 @@ void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree, cudaStream_t s) {
 }
 
 }  // namespace
+
+void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp) {
+  if (trees.size() != B.solves.size()) fail(LPM_ERR_INTERNAL, "tree code: one evaluator per solve");
+  B.treeMode = true;
+  B.trees = trees;
+  if (!B.treeStageDev) B.treeStageDev = B.mem.alloc<SolveStage>(B.solves.size());
+  B.treeStageHost.clear();
+  B.treeParams = tp;
+  B.treeDirectFor = tp.minPairs;
+  B.treeDirect.assign(B.solves.size(), 0);
+  B.directMem.release();
+  B.directItems = nullptr;
+  B.nDirectItems = 0;
+}
 }  // namespace lpm
 
 using namespace lpm;

@@ -75,7 +75,7 @@ struct SolveDev {
   // symmetric layout: slots [leaf0, nslots) are the leaf sources 0..ns-1 in source order
   // (leaf0 = -1: no such layout); reverse sums of the symmetric leaf kernel
   int leaf0;
-  unsigned long long* rev;   // [3][ns] fixed point
+  unsigned long long* rev;   // [4][ns] fixed point: velocity, stream function
   int* revBad;               // [ns]
 };
 
@@ -93,7 +93,7 @@ struct SolveStage {
   int nslots, ns, nchunks;
   double dt, omega;
   int leaf0;                 // symmetric layout: first leaf slot (-1: none)
-  unsigned long long* rev;   // [3][ns] fixed-point reverse sums (zeroed by prep), or null
+  unsigned long long* rev;   // [4][ns] fixed-point reverse sums (zeroed by prep), or null
   int* revBad;               // [ns]
 };
 
@@ -129,10 +129,11 @@ cudaError_t launchCombine(const SolveStage* st, const int4* map, int nblocks, bo
 cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
                        const SolveDev* solves, const WorkItem* items, int nitems, int* counter, int grid,
                        cudaStream_t s);
-// Symmetric leaf x leaf kernel over `items` (see WorkItem); grid = resident CTAs.
-cudaError_t launchPairSym(bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems, int* counter,
-                          int grid, cudaStream_t s);
-int pairSymBlocksPerSM();
+// Symmetric leaf x leaf kernel over `items` (see WorkItem), with or without the stream
+// function; grid = resident CTAs.
+cudaError_t launchPairSym(bool psi, bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems,
+                          int* counter, int grid, cudaStream_t s);
+int pairSymBlocksPerSM(bool psi);
 int pairShapeCount();              // FP32C launch shapes compiled in
 PairShape pairShapeAt(int i);
 int stageBlockSize();

@@ -206,7 +206,7 @@ struct Batch {
   bool sym = false;
   WorkItem* symDirectItems = nullptr;
   WorkItem* symItems = nullptr;
-  int nSymDirectItems = 0, nSymItems = 0, symDirectGrid = 0, symGrid = 0;
+  int nSymDirectItems = 0, nSymItems = 0, symDirectGrid = 0, symGrid = 0, symGridPsi = 0;
   std::vector<double> itemPairs;  // target-source pairs of each work item (host, launch order)
   DeviceArena mem;
   WorkItem* items = nullptr;
@@ -227,6 +227,7 @@ struct Batch {
   DeviceArena directMem;
   bool treeMode = false;
   TreeParams treeParams;
+  int treeGrid = 0;  // cap of the tree pair kernel's persistent grid (0: slots)
   int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)
   // captured RK4 step
   cudaGraphExec_t graph = nullptr;
@@ -280,6 +281,10 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
 void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
 // Uploads a tree-code batch's epilogue stage table when it changed.
 void treeStageTable(Batch& B, cudaStream_t s);
+// Puts a finalized batch in tree-code mode with evaluators the caller keeps (one per solve, in
+// solve order): buffers, list capacity and octree carry over from batch to batch.  Every solve
+// takes the tree code.
+void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp);
 
 // Snapshot file of a state held in host row-major arrays (snapshot.cpp).
 void writeSnapshotHost(const char* path, int seed, int level, int vpf, int64_t nv, int64_t nf, double t, double dt,

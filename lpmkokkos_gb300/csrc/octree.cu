@@ -379,7 +379,20 @@ void Octree::releaseAll() {
   }
 }
 
+void Octree::release(cudaStream_t s) {
+  for (Buf* b : all_) {
+    if (b->p) cudaFreeAsync(b->p, s);
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  dcount = nullptr;
+  nnodes = 0;
+}
+
 Octree::~Octree() {
+  bool held = false;
+  for (Buf* b : all_) held = held || b->p;
+  if (!held) return;  // released in stream order: nothing to wait for
   cudaDeviceSynchronize();
   releaseAll();
 }

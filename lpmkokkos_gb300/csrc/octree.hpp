@@ -43,6 +43,9 @@ class Octree {
   // is read back, and a rebuild with the same n and depth allocates nothing, so after a first
   // build the call can be captured in a CUDA graph.  No neighbour lists.
   void buildOnDevice(const double* x, int64_t si, int64_t sc, int64_t n, int depth, cudaStream_t s);
+  // Frees every buffer in stream order on `s` (after the work queued there); the object can be
+  // built again or destroyed without a device synchronisation.
+  void release(cudaStream_t s);
   int gbase[kOctreeMaxDepth + 2] = {};
   int* dcount = nullptr;              // device [depth + 2]: node counts per level, then the unique leaf keys
 

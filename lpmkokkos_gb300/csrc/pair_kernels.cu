@@ -31,6 +31,7 @@
 
 #include <climits>
 #include <cstdio>
+#include <type_traits>
 
 namespace lpm {
 namespace {
@@ -566,36 +567,49 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
 //     order-free, so the result does not depend on the schedule).
 //   * the diagonal tile J = I is summed in the forward direction only, with the self pair
 //     (source index = the target's own) dropped.
-// Per unordered pair: 17 paired FMA-pipe ops + 2 MUFU for two directed pairs (13 + 1 each in
-// pairFP32C), plus ~4 FP32 adds per source and thread for the transposed reduction.
+// Per paired step (two targets, one source: four directed pairs): 17 paired FMA-pipe ops and 2
+// MUFU (pairFP32C: 13 and 2 for two directed pairs), plus ~4 FP32 adds per source and thread for
+// the transposed reduction.
+// PSI: the stream function as well.  log2(2q) - 1 is formed once per unordered pair and serves
+// both directions (3 more paired ops and 2 MUFU per step, against 4 and 4 in pairFP32C's two
+// directed pairs): forward sums w_j (log2 2q - 1) Kahan-compensated in shared memory (the
+// registers are spent), a fourth reverse component, and the diagonal tile through the same
+// sweep with the self pair dropped.  The "- 1" folded into each term leaves the weight-sum
+// partial at zero.
 constexpr int kSymSt = 256;              // sources staged per step
 constexpr int kSymRed = 32;              // sources per warp transpose
 constexpr int kSymWarps = kSymThreads / 32;
 constexpr int kSymPitch = 33;            // floats per transpose row (32 lanes + 1 skew)
-constexpr size_t kSymSmem = sizeof(float4) * kSymSt * 2 + sizeof(float2) * kSymSt +
-                            sizeof(float) * kSymWarps * 3 * kSymRed * kSymPitch +
-                            sizeof(float) * kSymWarps * 3 * kSymSt;
+// reverse components: velocity (3) and, with the stream function, sum w (log2 2q - 1)
+__host__ __device__ constexpr int symComps(bool psi) { return psi ? 4 : 3; }
+constexpr size_t symSmem(bool psi) {
+  return sizeof(float4) * kSymSt * 2 + sizeof(float2) * kSymSt +
+         sizeof(float) * kSymWarps * symComps(psi) * kSymRed * kSymPitch +
+         sizeof(float) * kSymWarps * symComps(psi) * kSymSt + (psi ? sizeof(float) * 2 * kSymK * kSymThreads : 0);
+}
 
-template <bool NEWTON>
+template <bool NEWTON, bool PSI>
 __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* __restrict__ solves,
                                                              const WorkItem* __restrict__ items, int nitems,
                                                              int* __restrict__ counter) {
-  constexpr int NTH = kSymThreads, K = kSymK, P = K / 2, ST = kSymSt;
+  constexpr int NTH = kSymThreads, K = kSymK, P = K / 2, ST = kSymSt, NC = symComps(PSI);
   static_assert(NTH == 128, "the cross-warp combine assumes four warps");
-  extern __shared__ __align__(16) unsigned char symSmem[];
-  float4* sXY = reinterpret_cast<float4*>(symSmem);
+  extern __shared__ __align__(16) unsigned char symShared[];
+  float4* sXY = reinterpret_cast<float4*>(symShared);
   float4* sZW = sXY + ST;
   float2* sD = reinterpret_cast<float2*>(sZW + ST);
-  float* sWarp = reinterpret_cast<float*>(sD + ST);            // [warp][3 * 32 rows][33]
-  float* sCross = sWarp + kSymWarps * 3 * kSymRed * kSymPitch; // [warp][3][ST]
+  float* sWarp = reinterpret_cast<float*>(sD + ST);             // [warp][NC * 32 rows][33]
+  float* sCross = sWarp + kSymWarps * NC * kSymRed * kSymPitch; // [warp][NC][ST]
+  float* sPsi = sCross + kSymWarps * NC * ST;                   // PSI: [2K][NTH] forward psi sums, compensations
   __shared__ int sItem;
   __shared__ int sCentre;
   SourceTile<false> T;
   T.xy = sXY; T.zw = sZW; T.d = sD;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  float* myBuf = sWarp + warp * 3 * kSymRed * kSymPitch;
-  float* myCross = sCross + warp * 3 * ST;
+  float* myBuf = sWarp + warp * NC * kSymRed * kSymPitch;
+  float* myCross = sCross + warp * NC * ST;
   const float2 kMinusTwo = make_float2(-2.f, -2.f);
+  const float2 kMinusOne = make_float2(-1.f, -1.f);
   constexpr float kSign = NEWTON ? -1.f : 1.f;
 
   for (;;) {
@@ -625,6 +639,10 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
       hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
       hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
     }
+    if constexpr (PSI) {  // this thread's own slots: no barrier needed
+#pragma unroll
+      for (int k = 0; k < 2 * K; ++k) sPsi[k * NTH + threadIdx.x] = 0.f;
+    }
     for (int J = w.s0; J < w.s1; ++J) {
       const int src0 = J * kSymTile;
       const int send = min(ns, src0 + kSymTile);
@@ -636,18 +654,15 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
                                 nullptr, nullptr);
         }
         __syncthreads();
-        if (J == w.tile) {  // diagonal: forward only, the self pair (source index == own) dropped
-          int self[K];
-#pragma unroll
-          for (int k = 0; k < K; ++k) self[k] = tgt0 + threadIdx.x + k * NTH;
-          fp32cTile<K, false, true, false, NEWTON>(T, ST, b0, nullptr, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
-                                                  tt.C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
-        } else {
+        // One staged block.  DIAG (the tile against itself): forward terms only, the self pair
+        // (source index == the target's own) dropped.  Otherwise forward and reverse terms.
+        auto sweep = [&](auto diagTag) {
+          constexpr bool DIAG = decltype(diagTag)::value;
 #pragma unroll 1
           for (int j0 = 0; j0 < ST; j0 += kSymRed) {
-            float2 vx[P], vy[P], vz[P];
+            float2 vx[P], vy[P], vz[P], vp[P];
 #pragma unroll
-            for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = make_float2(0.f, 0.f);
+            for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = vp[m] = make_float2(0.f, 0.f);
 #pragma unroll 2
             for (int jj = 0; jj < kSymRed; ++jj) {
               const int j = j0 + jj;
@@ -656,7 +671,8 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
               const float2 dj = sD[j];
               const float2 X = make_float2(xy.x, xy.y), Y = make_float2(xy.z, xy.w), Z = make_float2(zw.x, zw.y);
               const float2 W = make_float2(zw.z, zw.w);
-              float2 rx = make_float2(0.f, 0.f), ry = rx, rz = rx;
+              float2 rx = make_float2(0.f, 0.f), ry = rx, rz = rx, rp = rx;
+              const int rel = b0 + j - tgt0 - (int)threadIdx.x;  // DIAG: k NTH for this thread's target k
 #pragma unroll
               for (int m = 0; m < P; ++m) {
                 const float2 dx = add2(X, tt.nx[m]), dy = add2(Y, tt.ny[m]), dz = add2(Z, tt.nz[m]);
@@ -666,19 +682,32 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
                 q = fma2(dz, dz, q);
                 float2 r = make_float2(rcpApprox(q.x), rcpApprox(q.y));
                 if (NEWTON) r = mul2(r, fma2(q, r, kMinusTwo));  // -(Newton reciprocal)
-                const float2 sf = mul2(W, r);
+                float2 sf = mul2(W, r);
+                float2 lgm;  // log2(2q) - 1, shared by both directions
+                if constexpr (PSI) lgm = add2(make_float2(lg2Approx(q.x), lg2Approx(q.y)), kMinusOne);
+                if constexpr (DIAG) {
+                  if (rel == 2 * m * NTH) { sf.x = 0.f; if (PSI) lgm.x = 0.f; }
+                  if (rel == (2 * m + 1) * NTH) { sf.y = 0.f; if (PSI) lgm.y = 0.f; }
+                }
                 vx[m] = fma2(sf, dx, vx[m]);
                 vy[m] = fma2(sf, dy, vy[m]);
                 vz[m] = fma2(sf, dz, vz[m]);
-                const float2 sr = mul2(Wt[m], r);
-                rx = fma2(sr, dx, rx);
-                ry = fma2(sr, dy, ry);
-                rz = fma2(sr, dz, rz);
+                if constexpr (PSI) vp[m] = fma2(W, lgm, vp[m]);
+                if constexpr (!DIAG) {
+                  const float2 sr = mul2(Wt[m], r);
+                  rx = fma2(sr, dx, rx);
+                  ry = fma2(sr, dy, ry);
+                  rz = fma2(sr, dz, rz);
+                  if constexpr (PSI) rp = fma2(Wt[m], lgm, rp);
+                }
               }
-              // this lane's reverse terms of source jj: row (component, jj), column = lane
-              myBuf[(0 * kSymRed + jj) * kSymPitch + lane] = rx.x + rx.y;
-              myBuf[(1 * kSymRed + jj) * kSymPitch + lane] = ry.x + ry.y;
-              myBuf[(2 * kSymRed + jj) * kSymPitch + lane] = rz.x + rz.y;
+              if constexpr (!DIAG) {
+                // this lane's reverse terms of source jj: row (component, jj), column = lane
+                myBuf[(0 * kSymRed + jj) * kSymPitch + lane] = rx.x + rx.y;
+                myBuf[(1 * kSymRed + jj) * kSymPitch + lane] = ry.x + ry.y;
+                myBuf[(2 * kSymRed + jj) * kSymPitch + lane] = rz.x + rz.y;
+                if constexpr (PSI) myBuf[(3 * kSymRed + jj) * kSymPitch + lane] = rp.x + rp.y;
+              }
             }
 #pragma unroll
             for (int m = 0; m < P; ++m) {
@@ -689,44 +718,96 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
               kahanAdd(hz[2 * m], cz[2 * m], kSign * vz[m].x);
               kahanAdd(hz[2 * m + 1], cz[2 * m + 1], kSign * vz[m].y);
             }
-            __syncwarp();
-            // lane l: source j0 + l, each component summed over the warp's 32 lanes in lane order
+            if constexpr (PSI) {
 #pragma unroll
-            for (int c = 0; c < 3; ++c) {
-              const float* row = myBuf + (c * kSymRed + lane) * kSymPitch;
-              float a0 = 0.f, a1 = 0.f;
+              for (int m = 0; m < P; ++m) {
 #pragma unroll
-              for (int k = 0; k < 32; k += 2) {
-                a0 += row[k];
-                a1 += row[k + 1];
+                for (int e = 0; e < 2; ++e) {
+                  const int k = 2 * m + e;
+                  float h = sPsi[k * NTH + threadIdx.x], c = sPsi[(K + k) * NTH + threadIdx.x];
+                  kahanAdd(h, c, e == 0 ? vp[m].x : vp[m].y);
+                  sPsi[k * NTH + threadIdx.x] = h;
+                  sPsi[(K + k) * NTH + threadIdx.x] = c;
+                }
               }
-              myCross[c * ST + j0 + lane] = a0 + a1;
             }
-            __syncwarp();  // the buffer is rewritten by the next 32 sources
-          }
-          __syncthreads();
-          // the four warps' sums of each (component, source), added in warp order; the reverse
-          // term is +sum s_r d (d_ji = -d_ij and rn = -(reciprocal) cancel)
-          for (int o = threadIdx.x; o < 3 * ST; o += NTH) {
-            const int comp = o / ST, jl = o % ST;
-            const int src = b0 + jl;
-            if (src >= send) continue;
-            const float acc = ((sCross[0 * 3 * ST + o] + sCross[1 * 3 * ST + o]) + sCross[2 * 3 * ST + o]) +
-                              sCross[3 * 3 * ST + o];
-            const double v = (double)(NEWTON ? acc : -acc);
-            if (fabs(v) < kSymLimit) {
-              atomicAdd(S.rev + (size_t)comp * ns + src, (unsigned long long)__double2ll_rn(v * kSymScale));
-            } else {
-              atomicExch(S.revBad + src, 1);  // inf/NaN or out of range: the source's result becomes NaN
+            if constexpr (!DIAG) {
+              __syncwarp();
+              // lane l: source j0 + l, each component summed over the warp's 32 lanes in lane order
+#pragma unroll
+              for (int c = 0; c < NC; ++c) {
+                const float* row = myBuf + (c * kSymRed + lane) * kSymPitch;
+                float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+                for (int k = 0; k < 32; k += 2) {
+                  a0 += row[k];
+                  a1 += row[k + 1];
+                }
+                myCross[c * ST + j0 + lane] = a0 + a1;
+              }
+              __syncwarp();  // the buffer is rewritten by the next 32 sources
             }
           }
+          if constexpr (!DIAG) {
+            __syncthreads();
+            // the four warps' sums of each (component, source), added in warp order; the reverse
+            // velocity is +sum s_r d (d_ji = -d_ij and rn = -(reciprocal) cancel), the reverse
+            // stream-function sum keeps its sign
+            for (int o = threadIdx.x; o < NC * ST; o += NTH) {
+              const int comp = o / ST, jl = o % ST;
+              const int src = b0 + jl;
+              if (src >= send) continue;
+              const float acc = ((sCross[0 * NC * ST + o] + sCross[1 * NC * ST + o]) + sCross[2 * NC * ST + o]) +
+                                sCross[3 * NC * ST + o];
+              const double v = (double)((NEWTON || comp == 3) ? acc : -acc);
+              if (fabs(v) < kSymLimit) {
+                atomicAdd(S.rev + (size_t)comp * ns + src, (unsigned long long)__double2ll_rn(v * kSymScale));
+              } else {
+                atomicExch(S.revBad + src, 1);  // inf/NaN or out of range: the source's result becomes NaN
+              }
+            }
+          }
+        };
+        if constexpr (PSI) {
+          if (J == w.tile)
+            sweep(std::true_type{});
+          else
+            sweep(std::false_type{});
+        } else if (J == w.tile) {  // diagonal: forward only, the self pair (source index == own) dropped
+          int self[K];
+#pragma unroll
+          for (int k = 0; k < K; ++k) self[k] = tgt0 + threadIdx.x + k * NTH;
+          fp32cTile<K, false, true, false, NEWTON>(T, ST, b0, nullptr, tt.nx, tt.ny, tt.nz, tt.nlx, tt.nly, tt.nlz,
+                                                  tt.C, self, hx, hy, hz, cx, cy, cz, hp, cp, hw, cw);
+        } else {
+          sweep(std::false_type{});
         }
         __syncthreads();
       }
     }
-    writePartials<NTH, K, false>(S.partial + (size_t)w.chunk * 3 * n, n, slot0, tcount, hx, hy, hz, cx, cy, cz, hp,
-                                 cp, hw, cw);
+    if constexpr (PSI) {  // the forward stream-function sums already hold the -1: no weight sum
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        hp[k] = sPsi[k * NTH + threadIdx.x];
+        cp[k] = sPsi[(K + k) * NTH + threadIdx.x];
+      }
+    }
+    writePartials<NTH, K, PSI>(S.partial + (size_t)w.chunk * (PSI ? 5 : 3) * n, n, slot0, tcount, hx, hy, hz, cx,
+                               cy, cz, hp, cp, hw, cw);
   }
+}
+
+// Resident CTAs per SM of the symmetric kernel (both Newton variants get the shared-memory limit).
+template <bool PSI>
+int symResidency() {
+  for (void* f : {(void*)pairFP32CSym<true, PSI>, (void*)pairFP32CSym<false, PSI>})
+    if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)symSmem(PSI)) != cudaSuccess)
+      return 0;
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)pairFP32CSym<true, PSI>, kSymThreads, symSmem(PSI)) !=
+      cudaSuccess)
+    return 0;
+  return b;
 }
 
 constexpr int kFP64Threads = 128;
@@ -887,26 +968,19 @@ int pairBlocksPerSM(Precision prec, const PairShape& shape, bool psi) {
   return nb;
 }
 
-int pairSymBlocksPerSM() {
-  static const int nb = [] {
-    for (void* f : {(void*)pairFP32CSym<true>, (void*)pairFP32CSym<false>})
-      if (cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSymSmem) != cudaSuccess) return 0;
-    int b = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, (void*)pairFP32CSym<true>, kSymThreads, kSymSmem) !=
-        cudaSuccess)
-      return 0;
-    return b;
-  }();
-  return nb;
+int pairSymBlocksPerSM(bool psi) {
+  static const int nb[2] = {[] { return symResidency<false>(); }(), [] { return symResidency<true>(); }()};
+  return nb[psi ? 1 : 0];
 }
 
-cudaError_t launchPairSym(bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems, int* counter,
-                          int grid, cudaStream_t s) {
+cudaError_t launchPairSym(bool psi, bool rcpApprox, const SolveDev* solves, const WorkItem* items, int nitems,
+                          int* counter, int grid, cudaStream_t s) {
   if (nitems <= 0 || grid <= 0) return cudaSuccess;
-  if (pairSymBlocksPerSM() <= 0) return cudaErrorInvalidConfiguration;
-  void* fn = rcpApprox ? (void*)pairFP32CSym<false> : (void*)pairFP32CSym<true>;
+  if (pairSymBlocksPerSM(psi) <= 0) return cudaErrorInvalidConfiguration;
+  void* fn = psi ? (rcpApprox ? (void*)pairFP32CSym<false, true> : (void*)pairFP32CSym<true, true>)
+                 : (rcpApprox ? (void*)pairFP32CSym<false, false> : (void*)pairFP32CSym<true, false>);
   void* args[] = {(void*)&solves, (void*)&items, (void*)&nitems, (void*)&counter};
-  return cudaLaunchKernel(fn, dim3(grid), dim3(kSymThreads), args, kSymSmem, s);
+  return cudaLaunchKernel(fn, dim3(grid), dim3(kSymThreads), args, symSmem(psi), s);
 }
 
 cudaError_t launchPair(Precision prec, const PairShape& shape, bool psi, bool precise, bool rcpApprox,

@@ -20,14 +20,20 @@
 // A host function queued on a request's lane behind its copy-back marks it done, returns its
 // budget reservation and wakes waiters and the admission loop.
 // With LPM_BVE_TREECODE two more threads, tree, take the requests of at least 1e9 pairs per
-// evaluation from the gpu thread and run them (one each at a time) through the library's
-// single-solve tree-code path on their own contexts and streams (the tree code reads sizes back between kernels,
-// so it cannot live in the classes' captured steps).
+// evaluation from the gpu thread, upload them and compute their initial velocity with the tree
+// code on their own streams -- the first evaluation of a solve sizes its interaction lists, the
+// tree code's one read-back -- and hand them back.  The gpu thread then steps them in size
+// classes of their own (tree classes: batches in tree-code mode whose steps are captured graphs,
+// like the direct classes').  A solve's tree evaluator (octree, lists, buffers) stays with the
+// request across batch rebuilds and is freed in stream order when it finishes.  A list that
+// outgrows its buffer is summed directly for that evaluation (exact) and flagged; the class then
+// runs one step uncaptured, which grows the buffer, and captures its step again.
 // A solve's result is bit-identical alone or in any mix: its plan, work items, chunking and
 // summation order depend on nothing but its own mesh and the launch shape, fixed per server.
 
 #include "lpm_bve_server.h"
 #include "engine_core.hpp"
+#include "tree_eval.hpp"
 
 #include <algorithm>
 #include <chrono>
@@ -164,6 +170,7 @@ struct Req {
   int cls = 0;                     // size class: log4 of pairs per evaluation
   cudaStream_t lane = nullptr;     // compute stream of its size class
   std::unique_ptr<SolvePlan> plan;
+  std::shared_ptr<TreeEval> tree;  // tree-code requests: the solve's evaluator, kept across batches
   DeviceArena mem;
   char* dev = nullptr;
   int stepsDone = 0;
@@ -212,11 +219,14 @@ struct lpm_bve_server {
   std::vector<double> latencies;
   std::map<std::tuple<int, int, int>, std::shared_ptr<const MeshHost>> meshes;  // prep thread only
   std::deque<std::tuple<int, int, int>> meshOrder;
-  // tree code (LPM_BVE_TREECODE): requests of at least minPairs pairs per evaluation go to the
-  // tree thread, which runs them one at a time through the single-solve path on its own stream
+  // tree code (LPM_BVE_TREECODE): requests of at least treeMinPairs pairs per evaluation go to a
+  // tree thread for their setup and initial velocity, then back to the gpu thread (treeReady)
   bool tree = false;
   double treeMinPairs = 1e9;
+  TreeParams treeParams;       // degree 8, theta 0.6, 512 sources per leaf
+  int treeSlots = 1;           // resident CTAs of the tree pair kernel on the whole GPU
   std::deque<Req*> treeQueue;  // under mu
+  std::deque<Req*> treeReady;  // under mu
   std::condition_variable cvTree;
   std::thread prepT, gpuT;
   std::vector<std::thread> treeT;
@@ -280,6 +290,11 @@ void failLocked(lpm_bve_server* S, Req* r, const std::string& msg) {
   S->cvPrep.notify_all();
 }
 
+// Requests this large take the tree code (LPM_BVE_TREECODE servers).
+bool treeSized(const lpm_bve_server* S, int64_t nv, int64_t nf, int64_t nl) {
+  return S->tree && (double)(nv + (S->skip ? nl : nf)) * (double)nl >= S->treeMinPairs;
+}
+
 std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) {
   const auto key = std::make_tuple(seed, level, S->skip ? 1 : 0);
   auto it = S->meshes.find(key);
@@ -294,8 +309,9 @@ std::shared_ptr<const MeshHost> meshFor(lpm_bve_server* S, int seed, int level) 
   if (lpm_mesh_build(seed, level, M->vx.data(), M->fx.data(), M->farea.data(), M->fmask.data()) != LPM_OK)
     fail(LPM_ERR_INVALID_ARGUMENT, "mesh seed %d level %d", seed, level);
   // FP32C solves take the symmetric layout (leaf x leaf pairs once) unless the server was created
-  // with LPM_BVE_NO_SYMMETRIC
-  const bool sym = S->prec == Precision::FP32C && !(S->flags & LPM_BVE_NO_SYMMETRIC);
+  // with LPM_BVE_NO_SYMMETRIC or the tree code takes the solve (its tiles follow the Morton order)
+  const bool sym = S->prec == Precision::FP32C && !(S->flags & LPM_BVE_NO_SYMMETRIC) &&
+                   !treeSized(S, M->nv, M->nf, M->nl);
   M->plan = prepareHostFromHost(Mode::RK4, M->nv, M->nf, M->vx.data(), M->fx.data(), M->fmask.data(), S->skip, true,
                                 sym, kSymMinLeaves);
   S->meshes[key] = M;
@@ -418,25 +434,23 @@ cudaStream_t laneOf(lpm_bve_server* S, int cls) {
   return l;
 }
 
-// Uploads a prepared request and builds its plan (upload stream; stream-ordered allocation,
-// freed in order on the request's lane).
-void setupSolve(lpm_bve_server* S, Req* r) {
+// Uploads a prepared request and builds its plan on stream `s` (stream-ordered allocation, freed
+// in order on `freeS`), with target tiles of `tileSize` slots.
+void uploadAndPlan(lpm_bve_server* S, Req* r, cudaStream_t s, cudaStream_t freeS, int tileSize) {
   const MeshHost& M = *r->mesh;
   r->nv = M.nv;
   r->nf = M.nf;
-  r->cls = costClass((double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl);
-  r->lane = laneOf(S, r->cls);
   const Layout L(M.nv, M.nf);
-  r->mem.streamOrdered(S->up, r->lane, S->pool);
+  r->mem.streamOrdered(s, freeS, S->pool);
   r->dev = r->mem.alloc<char>(L.bytes);
-  LPM_CUDA(cudaMemcpyAsync(r->dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, S->up));
+  LPM_CUDA(cudaMemcpyAsync(r->dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, s));
   double* d = reinterpret_cast<double*>(r->dev);
   if (!S->hostIc) {
     const int ng = r->r.n_gaussians;
     for (const auto& part : {std::make_pair(L.vx, L.vzeta), std::make_pair(L.fx, L.fzeta)}) {
       const int64_t n = part.first == L.vx ? M.nv : M.nf;
       const int rc = lpm_ic_rh54_gaussians_device(d + part.first, n, 3, 1, r->gc.data(), r->ga.data(), ng,
-                                                  r->r.gauss_width, d + part.second, (lpm_stream_t)S->up);
+                                                  r->r.gauss_width, d + part.second, (lpm_stream_t)s);
       if (rc != LPM_OK) fail(rc, "initial vorticity on the device: %s", cudaGetErrorString(cudaGetLastError()));
     }
   }
@@ -452,27 +466,53 @@ void setupSolve(lpm_bve_server* S, Req* r) {
   io.barea = d + L.farea;
   const uint8_t* mask = reinterpret_cast<const uint8_t*>(r->dev + L.maskByte);
   r->plan.reset(new SolvePlan());
-  r->plan->mem.streamOrdered(S->up, r->lane, S->pool);
-  buildSolve(*r->plan, Mode::RK4, S->prec, io, mask, S->skip, true, S->eps, S->shape.tileSize(), M.plan, S->up);
+  r->plan->mem.streamOrdered(s, freeS, S->pool);
+  buildSolve(*r->plan, Mode::RK4, S->prec, io, mask, S->skip, true, S->eps, tileSize, M.plan, s);
   r->plan->stage.dt = r->r.dt;
   r->plan->stage.omega = r->r.omega;
   r->pairsPerEval = (double)r->plan->nslots * r->plan->ns;
 }
 
-// A batch over solves of one lane.  Its pair grid is set by shareSlots before its step is
-// captured (initial-velocity batches keep the persistent grid finalizeBatch chose).
-std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs, cudaStream_t lane) {
+// A direct-sum request: its size class and lane, then the upload (upload stream, freed in order
+// on the lane).
+void setupSolve(lpm_bve_server* S, Req* r) {
+  const MeshHost& M = *r->mesh;
+  r->cls = costClass((double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl);
+  r->lane = laneOf(S, r->cls);
+  uploadAndPlan(S, r, S->up, r->lane, S->shape.tileSize());
+}
+
+// A batch over solves of one lane, built on stream `s`.  Its pair grid is set by shareSlots before
+// its step is captured (initial-velocity batches keep the persistent grid finalizeBatch chose).
+// Tree-code requests (each with its evaluator) make a tree-code batch.
+std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs, cudaStream_t lane,
+                                 cudaStream_t s) {
+  const bool tree = rs.front()->tree != nullptr;
   auto B = std::make_unique<Batch>();
   B->prec = S->prec;
-  B->shape = S->shape;
+  B->shape = tree ? kTreeShape : S->shape;
   B->rk4 = true;
   B->rcpApprox = S->rcp;
-  B->mem.streamOrdered(S->up, lane, S->pool);
+  B->mem.streamOrdered(s, lane, S->pool);
   for (Req* r : rs) B->solves.push_back(r->plan.get());
   B->sym = false;  // solves below the layout's size threshold keep the plain kernel in the same batch
-  for (const SolvePlan* p : B->solves) B->sym = B->sym || (p->leaf0 >= 0 && p->ns > 0);
-  finalizeBatch(*B, S->dev, S->up);
+  if (!tree)
+    for (const SolvePlan* p : B->solves) B->sym = B->sym || (p->leaf0 >= 0 && p->ns > 0);
+  finalizeBatch(*B, S->dev, s);
+  if (tree) {
+    std::vector<std::shared_ptr<TreeEval>> trees;
+    for (Req* r : rs) trees.push_back(r->tree);
+    attachTrees(*B, trees, S->treeParams);
+    bool sized = true;
+    for (Req* r : rs) sized = sized && r->tree->ready();
+    if (sized) treeStageTable(*B, s);  // else the first (uncaptured) evaluation uploads it
+  }
   return B;
+}
+
+// Resident tree pair-kernel CTAs that take the place of `slots` CTAs of the direct kernel.
+int treeGridFor(const lpm_bve_server* S, int slots) {
+  return std::max(1, (int)((int64_t)slots * S->treeSlots / std::max(1, S->slots)));
 }
 
 // Captures one RK4 step of B and installs it in `exec`: updated in place when exec exists (the
@@ -526,6 +566,10 @@ void CUDART_CB requestDone(void* p) {
 void finish(lpm_bve_server* S, Req* r) {
   const Layout L(r->nv, r->nf);
   LPM_CUDA(cudaMemcpyAsync(r->host, r->dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, r->lane));
+  if (r->tree) {  // the tree evaluator's buffers, in stream order (a batch may still hold it)
+    r->tree->release(r->lane);
+    r->tree.reset();
+  }
   r->plan.reset();
   r->mem.release();
   r->dev = nullptr;
@@ -553,6 +597,7 @@ void finish(lpm_bve_server* S, Req* r) {
 // slots stays out of every share for newcomers.  A host function queued
 // behind each burst wakes this thread when it completes.
 constexpr int kMaxInflight = 2;
+constexpr int kTreeClass = 64;    // tree classes: kTreeClass + log4 of the direct-sum pairs
 constexpr int kReserveFrac = 38;  // 1/38 of the slots: 8 of the 304 of the default shape
 constexpr double kLongStepMs = 50.0;
 constexpr double kBurstMs = 10.0;
@@ -568,6 +613,9 @@ struct SizeClass {
   std::unique_ptr<Batch> batch;
   cudaStream_t lane = nullptr;
   bool changed = false;
+  bool tree = false;   // a tree class (tree-code batch)
+  bool stale = false;  // tree class: the captured step predates the batch or its grid
+  int treeGen = -1;    // tree class: the evaluators' generations the step was captured with
   double msPerStep = -1.0;  // moving average of measured step time (-1: not measured yet)
   double pairsPerStep = 0.0;
   std::deque<Burst> inflight;
@@ -598,85 +646,41 @@ std::map<int, int> shareSlots(const std::map<int, SizeClass>& classes, int slots
   return grid;
 }
 
-// The tree thread: each request it is handed runs alone through the library's single-solve path
-// (lpm_bve_velocity / lpm_bve_rk4_step with LPM_BVE_TREECODE) on this thread's context and
-// stream -- device initial vorticity as on the gpu thread, the initial velocity, the steps, the
-// copy back -- so its result depends on nothing but the request.  Its kernels share the GPU
-// with the size classes' persistent grids (they take the slots the classes leave).
-void treeRequest(lpm_bve_server* S, lpm_bve_ctx* ctx, cudaStream_t ts, Req* r) {
-  const MeshHost& M = *r->mesh;
-  r->nv = M.nv;
-  r->nf = M.nf;
-  const Layout L(M.nv, M.nf);
-  DeviceArena mem;
-  mem.streamOrdered(ts, ts, S->pool);
-  char* dev = mem.alloc<char>(L.bytes);
-  LPM_CUDA(cudaMemcpyAsync(dev, r->host, L.maskByte + (size_t)M.nf, cudaMemcpyHostToDevice, ts));
-  double* d = reinterpret_cast<double*>(dev);
-  auto check = [&](int rc) {
-    if (rc != LPM_OK) fail(rc, "%s", lpm_bve_last_error(ctx));
-  };
-  if (!S->hostIc)
-    for (const auto& part : {std::make_pair(L.vx, L.vzeta), std::make_pair(L.fx, L.fzeta)}) {
-      const int64_t n = part.first == L.vx ? M.nv : M.nf;
-      check(lpm_ic_rh54_gaussians_device(d + part.first, n, 3, 1, r->gc.data(), r->ga.data(), r->r.n_gaussians,
-                                         r->r.gauss_width, d + part.second, (lpm_stream_t)ts));
-    }
-  const uint8_t* mask = reinterpret_cast<const uint8_t*>(dev + L.maskByte);
+// The tree thread: uploads a tree-code request and builds its plan on this thread's stream,
+// computes the initial velocity with a one-solve tree-code batch -- the solve's first evaluation,
+// which sizes its interaction lists (one read-back of this stream) -- and hands the request to
+// the gpu thread, whose tree classes step it.  Its result depends on nothing but the request.
+void treeSetup(lpm_bve_server* S, cudaStream_t ts, Req* r) {
   {
     std::lock_guard<std::mutex> lk(S->mu);
     r->state = LPM_REQ_RUNNING;
     r->tStart = Clock::now();
-    r->pairsPerEval = (double)(M.nv + (S->skip ? M.nl : M.nf)) * (double)M.nl;
-    S->st.tree_equiv_pairs += r->pairsPerEval;
   }
-  const unsigned fl = S->flags;  // FP32C | TREECODE and the RK4 options
-  lpm_points tv{d + L.vx, M.nv, 3, 1};
-  lpm_sources src{{d + L.fx, M.nf, 3, 1}, d + L.fzeta, d + L.farea, mask};
-  check(lpm_bve_velocity(ctx, &tv, &src, d + L.vvel, 3, 1, nullptr, LPM_BVE_FP32C | LPM_BVE_MESH_TARGETS | LPM_BVE_TREECODE,
-                         S->eps, (lpm_stream_t)ts));
-  check(lpm_bve_velocity(ctx, nullptr, &src, d + L.fvel, 3, 1, nullptr,
-                         LPM_BVE_FP32C | LPM_BVE_COLLOCATED | LPM_BVE_TREECODE | (fl & LPM_BVE_SKIP_MASKED_TARGETS),
-                         S->eps, (lpm_stream_t)ts));
-  lpm_bve_state st{};
-  st.nverts = M.nv;
-  st.nfaces = M.nf;
-  st.vx = d + L.vx; st.vx_stride_i = 3; st.vx_stride_c = 1;
-  st.vzeta = d + L.vzeta;
-  st.vvel = d + L.vvel; st.vvel_stride_i = 3; st.vvel_stride_c = 1;
-  st.fx = d + L.fx; st.fx_stride_i = 3; st.fx_stride_c = 1;
-  st.fzeta = d + L.fzeta;
-  st.fvel = d + L.fvel; st.fvel_stride_i = 3; st.fvel_stride_c = 1;
-  st.farea = d + L.farea;
-  st.fmask = mask;
-  check(lpm_bve_rk4_step(ctx, &st, r->r.dt, r->r.omega, r->r.nsteps, fl, S->eps, (lpm_stream_t)ts));
-  check(lpm_bve_plan_invalidate(ctx));  // the next request's arrays reuse this memory
-  LPM_CUDA(cudaMemcpyAsync(r->host, dev, L.ndoubles * sizeof(double), cudaMemcpyDeviceToHost, ts));
-  mem.release();
+  uploadAndPlan(S, r, ts, ts, kTreeShape.tileSize());
+  r->tree = std::make_shared<TreeEval>();
+  {
+    std::unique_ptr<Batch> B = makeBatch(S, {r}, ts, ts);
+    enqueueEval(*B, 0, 0, false, true, ts);
+  }
   LPM_CUDA(cudaStreamSynchronize(ts));
   std::lock_guard<std::mutex> lk(S->mu);
-  if (r->state != LPM_REQ_RUNNING) return;
-  r->state = LPM_REQ_DONE;
-  r->tDone = Clock::now();
-  S->reserved -= r->est;
-  S->inflight -= 1;
-  S->st.completed += 1;
-  S->st.solve_steps += r->r.nsteps;
-  S->st.tree_equiv_pairs += 4.0 * r->r.nsteps * r->pairsPerEval;  // the direct-sum pairs the steps replace
-  S->latencies.push_back(seconds(r->tSubmit, r->tDone));
-  S->cvDone.notify_all();
-  S->cvPrep.notify_all();
+  S->st.tree_equiv_pairs += r->pairsPerEval;
+  if (S->stop) {  // the gpu thread has gone: nobody steps it
+    r->tree->release(ts);
+    r->tree.reset();
+    r->plan.reset();
+    r->mem.release();
+    failLocked(S, r, "server destroyed before the request ran");
+    return;
+  }
+  S->treeReady.push_back(r);
 }
 
 void treeLoop(lpm_bve_server* S) {
   cudaSetDevice(S->dev.device);
-  lpm_bve_ctx* ctx = nullptr;
   cudaStream_t ts = nullptr;
   std::string setupErr;
-  lpm_bve_opts o{S->dev.device, 0, 0};
-  if (lpm_bve_ctx_create(&ctx, &o) != LPM_OK || lpm_bve_ctx_set_treecode(ctx, 8, 0.6, 512, 0.0) != LPM_OK ||
-      cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking) != cudaSuccess)
-    setupErr = "tree thread: no context or stream";
+  if (cudaStreamCreateWithFlags(&ts, cudaStreamNonBlocking) != cudaSuccess) setupErr = "tree thread: no stream";
   for (;;) {
     Req* r = nullptr;
     {
@@ -690,27 +694,30 @@ void treeLoop(lpm_bve_server* S) {
       r = S->treeQueue.front();
       S->treeQueue.pop_front();
     }
+    std::string err;
     try {
       if (!setupErr.empty()) fail(LPM_ERR_INTERNAL, "%s", setupErr.c_str());
-      treeRequest(S, ctx, ts, r);
+      treeSetup(S, ts, r);
     } catch (const Error& e) {
-      if (ts) cudaStreamSynchronize(ts);
-      if (ctx) lpm_bve_plan_invalidate(ctx);  // plans of the failed request's (reused) arrays
-      std::lock_guard<std::mutex> lk(S->mu);
-      failLocked(S, r, "tree code: " + e.msg);
+      err = e.msg;
     } catch (const std::exception& e) {
-      if (ts) cudaStreamSynchronize(ts);
-      if (ctx) lpm_bve_plan_invalidate(ctx);
-      std::lock_guard<std::mutex> lk(S->mu);
-      failLocked(S, r, "tree code: " + fromStd(e).msg);
+      err = fromStd(e).msg;
     }
     r->mesh.reset();
+    if (!err.empty()) {
+      if (ts) cudaStreamSynchronize(ts);
+      r->tree.reset();
+      r->plan.reset();
+      r->mem.release();
+      std::lock_guard<std::mutex> lk(S->mu);
+      failLocked(S, r, "tree code: " + err);
+    }
+    wakeGpu(S);
   }
   if (ts) {
     cudaStreamSynchronize(ts);
     cudaStreamDestroy(ts);
   }
-  if (ctx) lpm_bve_ctx_destroy(ctx);
 }
 
 void gpuLoop(lpm_bve_server* S) {
@@ -741,12 +748,14 @@ void gpuLoop(lpm_bve_server* S) {
   try {
     LPM_CUDA(cudaEventCreateWithFlags(&upEv, cudaEventDisableTiming));
     for (;;) {
-      std::vector<Req*> joiners;
+      std::vector<Req*> joiners, treeJoin;
       {
         std::lock_guard<std::mutex> lk(S->mu);
         if (S->stop) break;
         joiners.assign(S->prepared.begin(), S->prepared.end());
         S->prepared.clear();
+        treeJoin.assign(S->treeReady.begin(), S->treeReady.end());
+        S->treeReady.clear();
         const Clock::time_point now = Clock::now();
         if (nActive > 0) S->st.busy_s += seconds(tick, now);
         tick = now;
@@ -761,9 +770,8 @@ void gpuLoop(lpm_bve_server* S) {
         failLocked(S, r, msg);
       };
       for (Req* r : joiners) {
-        if (S->tree && (double)(r->mesh->nv + (S->skip ? r->mesh->nl : r->mesh->nf)) * (double)r->mesh->nl >=
-                           S->treeMinPairs) {
-          std::lock_guard<std::mutex> lk(S->mu);  // large enough for the tree code: the tree thread
+        if (treeSized(S, r->mesh->nv, r->mesh->nf, r->mesh->nl)) {
+          std::lock_guard<std::mutex> lk(S->mu);  // large enough for the tree code: a tree thread
           S->treeQueue.push_back(r);
           S->cvTree.notify_one();
           continue;
@@ -783,9 +791,26 @@ void gpuLoop(lpm_bve_server* S) {
       for (Req* r : ok) byClass[r->cls].push_back(r);
       std::vector<std::pair<cudaStream_t, std::unique_ptr<Batch>>> inits;  // initial velocity per class
       std::vector<Req*> noSteps;
+      // tree-code requests arrive set up, with their initial velocity: straight into a tree class
+      for (Req* r : treeJoin) {
+        r->cls = kTreeClass + costClass(r->pairsPerEval);
+        r->lane = laneOf(S, r->cls);
+        r->mem.streamOrdered(S->up, r->lane, S->pool);  // freed in order on the lane from now on
+        r->plan->mem.streamOrdered(S->up, r->lane, S->pool);
+        if (r->r.nsteps > 0) {
+          SizeClass& C = classes[r->cls];
+          C.lane = r->lane;
+          C.tree = true;
+          C.solves.push_back(r);
+          C.changed = true;
+          ++nActive;
+        } else {
+          noSteps.push_back(r);
+        }
+      }
       for (auto& kv : byClass) {
         const cudaStream_t lane = kv.second.front()->lane;
-        inits.emplace_back(lane, makeBatch(S, kv.second, lane));
+        inits.emplace_back(lane, makeBatch(S, kv.second, lane, S->up));
         for (Req* r : kv.second) {
           if (r->r.nsteps > 0) {
             SizeClass& C = classes[kv.first];
@@ -807,8 +832,9 @@ void gpuLoop(lpm_bve_server* S) {
           C.pairsPerStep = 0.0;
           for (Req* r : C.solves) C.pairsPerStep += 4.0 * r->pairsPerEval;
           if (!C.solves.empty()) {
-            C.batch = makeBatch(S, C.solves, C.lane);
+            C.batch = makeBatch(S, C.solves, C.lane, S->up);
             C.batch->grid = 0;  // installed below with its share of the slots
+            C.stale = true;
             waiting.push_back(C.lane);
           }
           C.changed = false;
@@ -831,7 +857,12 @@ void gpuLoop(lpm_bve_server* S) {
           // each within the same share
           C.batch->symDirectGrid = std::min(C.batch->nSymDirectItems, kg.second);
           C.batch->symGrid = std::min(C.batch->nSymItems, kg.second);
-          installStep(S, *C.batch, execs[kg.first]);
+          C.batch->symGridPsi = std::min(C.batch->nSymItems, kg.second);
+          C.batch->treeGrid = treeGridFor(S, kg.second);
+          if (C.tree)
+            C.stale = true;  // captured before its next burst, once every list is sized
+          else
+            installStep(S, *C.batch, execs[kg.first]);
         }
       }
       for (auto& in : inits) waiting.push_back(in.first);
@@ -845,7 +876,7 @@ void gpuLoop(lpm_bve_server* S) {
         enqueueEval(*in.second, 0, 0, false, true, in.first);
         in.second.reset();
       }
-      if (!ok.empty()) {
+      if (!ok.empty() || !treeJoin.empty()) {
         std::lock_guard<std::mutex> lk(S->mu);
         const Clock::time_point now = Clock::now();
         for (Req* r : ok) {
@@ -875,7 +906,7 @@ void gpuLoop(lpm_bve_server* S) {
       }
       // 4. launch bursts on every lane that has room
       bool launched = false;
-      double pairs = 0.0;
+      double pairs = 0.0, treePairs = 0.0;
       int64_t solveSteps = 0, classSteps = 0;
       for (auto& kv : classes) {
         SizeClass& C = kv.second;
@@ -887,11 +918,36 @@ void gpuLoop(lpm_bve_server* S) {
           if ((int)C.inflight.size() >= maxInflight) break;
           int left = INT_MAX;
           for (Req* r : C.solves) left = std::min(left, r->r.nsteps - r->stepsDone);
-          const int k = std::max(1, std::min({(int)(kBurstMs / est), left, kMaxStepsPerBurst}));
+          // a tree class whose lists outgrew their buffers since the last burst runs one step
+          // uncaptured (its evaluations grow them); otherwise its step is captured again when
+          // the batch, its grid or an evaluator's buffers changed
+          bool uncaptured = false;
+          if (C.tree) {
+            bool ready = true;
+            int gen = 0;
+            for (Req* r : C.solves) {
+              r->tree->poll();
+              ready = ready && r->tree->ready();
+              gen += r->tree->generation();
+            }
+            if (!ready) {
+              uncaptured = true;
+            } else if (C.stale || gen != C.treeGen || !execs[kv.first]) {
+              treeStageTable(*C.batch, C.lane);
+              installStep(S, *C.batch, execs[kv.first]);
+              C.stale = false;
+              C.treeGen = gen;
+            }
+          }
+          const int k = uncaptured ? 1 : std::max(1, std::min({(int)(kBurstMs / est), left, kMaxStepsPerBurst}));
           Burst b{getEvent(), getEvent(), k};
           LPM_CUDA(cudaEventRecord(b.e0, C.lane));
-          const cudaGraphExec_t exec = execs[kv.first];
-          for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(exec, C.lane));
+          if (uncaptured) {
+            enqueueStep(*C.batch, S->quirk, S->renorm, C.lane);
+          } else {
+            const cudaGraphExec_t exec = execs[kv.first];
+            for (int j = 0; j < k; ++j) LPM_CUDA(cudaGraphLaunch(exec, C.lane));
+          }
           LPM_CUDA(cudaEventRecord(b.e1, C.lane));
           LPM_CUDA(cudaLaunchHostFunc(C.lane, burstDone, S));
           C.inflight.push_back(b);
@@ -900,7 +956,7 @@ void gpuLoop(lpm_bve_server* S) {
           std::vector<Req*> still;
           for (Req* r : C.solves) {
             r->stepsDone += k;
-            pairs += 4.0 * k * r->pairsPerEval;
+            (C.tree ? treePairs : pairs) += 4.0 * k * r->pairsPerEval;  // tree: direct-sum equivalent
             solveSteps += k;
             if (r->stepsDone >= r->r.nsteps) {
               finish(S, r);
@@ -922,10 +978,11 @@ void gpuLoop(lpm_bve_server* S) {
         S->st.steps_run += classSteps;
         S->st.solve_steps += solveSteps;
         S->st.pairs += pairs;
+        S->st.tree_equiv_pairs += treePairs;
       }
       bool rebuild = false;
       for (auto& kv : classes) rebuild |= kv.second.changed;
-      if (launched || rebuild || !ok.empty()) continue;
+      if (launched || rebuild || !ok.empty() || !treeJoin.empty()) continue;
       // 5. nothing to launch: sleep until a burst completes or work arrives (bounded wait)
       {
         std::unique_lock<std::mutex> lk(S->wmu);
@@ -955,11 +1012,17 @@ void gpuLoop(lpm_bve_server* S) {
     S->finishing.clear();
     S->cvDone.notify_all();
   }
-  const std::vector<Req*> active = allActive();
+  std::vector<Req*> active = allActive();
+  {
+    std::lock_guard<std::mutex> lk(S->mu);  // set up by a tree thread, not yet in a class
+    active.insert(active.end(), S->treeReady.begin(), S->treeReady.end());
+    S->treeReady.clear();
+  }
   for (auto& kv : classes) kv.second.batch.reset();
   for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);
   for (Req* r : active) {  // abandoned at shutdown
+    r->tree.reset();
     r->plan.reset();
     r->mem.release();
   }
@@ -1042,6 +1105,8 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
     S->prioLeast = leastP;
     S->prioGreatest = greatestP;
     S->slots = std::max(1, pairBlocksPerSM(S->prec, S->shape, false) * S->dev.sms);
+    S->treeParams.minPairs = 0.0;  // the server routes by treeMinPairs; a tree class takes the tree code
+    S->treeSlots = kTreeShape.minBlocks * S->dev.sms;
     LPM_CUDA(cudaStreamCreateWithFlags(&S->cap, cudaStreamNonBlocking));
     cudaMemPoolProps props{};
     props.allocType = cudaMemAllocationTypePinned;
@@ -1059,8 +1124,8 @@ int lpm_bve_server_create(const lpm_bve_server_opts* opts, lpm_bve_server** out)
   try {
     raw->prepT = std::thread(prepLoop, raw);
     raw->gpuT = std::thread(gpuLoop, raw);
-    // two tree threads: a large request need not wait for another's whole run, only share its
-    // kernels (each thread has its own context and stream)
+    // two tree threads: a large request's setup need not wait for another's (each thread has
+    // its own stream)
     if (raw->tree)
       for (int k = 0; k < 2; ++k) raw->treeT.emplace_back(treeLoop, raw);
   } catch (const std::exception& e) {  // no thread: stop and join the one that started
@@ -1317,6 +1382,7 @@ int lpm_bve_server_destroy(lpm_bve_server* S) {
   for (auto& ln : S->lanes) cudaStreamSynchronize(ln.second);
   cudaStreamSynchronize(S->up);
   for (auto& kv : S->reqs) {
+    kv.second->tree.reset();
     kv.second->plan.reset();
     kv.second->mem.release();
   }

@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(kBlock) prepKernel(const SolveStage* __restric
     }
     const double circ = -z * io.barea[f];
     if (S.rev) {  // the symmetric leaf kernel adds into these
-      for (int c = 0; c < 3; ++c) S.rev[(size_t)c * S.ns + i] = 0ull;
+      for (int c = 0; c < 4; ++c) S.rev[(size_t)c * S.ns + i] = 0ull;
       S.revBad[i] = 0;
     }
     if (fp32c) {
@@ -106,9 +106,10 @@ __global__ void __launch_bounds__(kBlock) epilogueKernel(const SolveStage* __res
   if (useRev && S.rev && S.leaf0 >= 0 && i >= S.leaf0) {   // reverse sums of the symmetric leaf kernel
     const int k = i - S.leaf0;
     if (S.revBad[k]) {
-      v[0] = v[1] = v[2] = __longlong_as_double(0x7ff8000000000000ll);  // NaN
-    } else {
-      for (int c = 0; c < 3; ++c) v[c] += (double)(long long)S.rev[(size_t)c * S.ns + k] * (1.0 / kSymScale);
+      v[0] = v[1] = v[2] = v[3] = __longlong_as_double(0x7ff8000000000000ll);  // NaN
+    } else {  // component 3: sum w (log2 2q - 1), the weight sum folded in
+      const int nc = (fp32c && psi) ? 4 : 3;
+      for (int c = 0; c < nc; ++c) v[c] += (double)(long long)S.rev[(size_t)c * S.ns + k] * (1.0 / kSymScale);
     }
   }
   double u[3];

@@ -18,7 +18,10 @@
 #include <cfloat>
 #include <climits>
 #include <cmath>
+#include <mutex>
 #include <numeric>
+#include <utility>
+#include <vector>
 
 namespace lpm {
 namespace {
@@ -506,22 +509,91 @@ T* TreeEval::grow(Buf& b, size_t count, cudaStream_t s) {
   return static_cast<T*>(b.p);
 }
 
+// Report slots in mapped host memory, allocated in blocks and recycled: freeing mapped memory
+// would synchronise the device, and a slot may still be written by kernels in flight when its
+// evaluator goes away.  A slot returns to the pool only once the work queued before its release
+// has completed (a host function on that stream) or after a device synchronisation.
+class WatchPool {
+ public:
+  static WatchPool& get() {
+    static WatchPool* p = new WatchPool();  // lives as long as the process (host functions may run late)
+    return *p;
+  }
+  void take(TreeWatch** host, TreeWatch** dev) {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (free_.empty()) {
+      constexpr int kBlock = 64;
+      void* h = nullptr;
+      ck(cudaHostAlloc(&h, sizeof(TreeWatch) * kBlock, cudaHostAllocMapped | cudaHostAllocPortable),
+         "host allocation");
+      void* d = nullptr;
+      ck(cudaHostGetDevicePointer(&d, h, 0), "mapped pointer");
+      for (int i = kBlock - 1; i >= 0; --i)
+        free_.emplace_back(static_cast<TreeWatch*>(h) + i, static_cast<TreeWatch*>(d) + i);
+    }
+    *host = free_.back().first;
+    *dev = free_.back().second;
+    free_.pop_back();
+    std::memset(*host, 0, sizeof(TreeWatch));
+  }
+  void give(TreeWatch* host, TreeWatch* dev) {
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.emplace_back(host, dev);
+  }
+  struct Pending {
+    TreeWatch* host;
+    TreeWatch* dev;
+  };
+  static void CUDART_CB giveLater(void* p) {  // host function: no CUDA calls
+    Pending* q = static_cast<Pending*>(p);
+    get().give(q->host, q->dev);
+    delete q;
+  }
+
+ private:
+  std::mutex mu_;
+  std::vector<std::pair<TreeWatch*, TreeWatch*>> free_;
+};
+
 TreeEval::~TreeEval() {
-  cudaDeviceSynchronize();
-  for (Buf* b : all_)
-    if (b->p) cudaFree(b->p);
-  if (watch_) cudaFreeHost(watch_);
+  bool held = false;
+  for (Buf* b : all_) held = held || b->p;
+  if (held) {  // not released in stream order: wait for the device, then free
+    cudaDeviceSynchronize();
+    for (Buf* b : all_)
+      if (b->p) cudaFree(b->p);
+  }
+  if (watch_) WatchPool::get().give(watch_, dWatch_);
+}
+
+void TreeEval::release(cudaStream_t s) {
+  for (Buf* b : all_) {
+    if (b->p) ck(cudaFreeAsync(b->p, s), "free");
+    b->p = nullptr;
+    b->bytes = 0;
+  }
+  tree_.release(s);
+  if (watch_) {
+    auto* q = new WatchPool::Pending{watch_, dWatch_};
+    const cudaError_t e = cudaLaunchHostFunc(s, WatchPool::giveLater, q);
+    if (e != cudaSuccess) {
+      delete q;  // the slot is dropped, not reused
+      ck(e, "host function");
+    }
+    watch_ = nullptr;
+    dWatch_ = nullptr;
+  }
+  partial_ = nullptr;
+  listCap_ = 0;
+  devAt_ = nullptr;
+  hDev_ = TreeDev{};
+  statsOnDevice_ = false;
+  ++generation_;
 }
 
 void TreeEval::ensureWatch() {
   if (watch_) return;
-  void* h = nullptr;
-  ck(cudaHostAlloc(&h, sizeof(TreeWatch), cudaHostAllocMapped), "host allocation");
-  watch_ = static_cast<TreeWatch*>(h);
-  std::memset(watch_, 0, sizeof(TreeWatch));
-  void* d = nullptr;
-  ck(cudaHostGetDevicePointer(&d, h, 0), "mapped pointer");
-  dWatch_ = static_cast<TreeWatch*>(d);
+  WatchPool::get().take(&watch_, &dWatch_);
 }
 
 bool TreeEval::poll() {
@@ -555,14 +627,18 @@ const TreeStats& TreeEval::stats() {
 }
 
 void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& shape, bool psi, bool precise,
-                        bool rcpApprox, int slots, PairTimer* timer, cudaStream_t s) {
+                        bool rcpApprox, int slots, int grid, PairTimer* timer, cudaStream_t s) {
   if (tp.degree < 2 || tp.degree > kMaxDegree) fail(LPM_ERR_INVALID_ARGUMENT, "tree code: degree must be 2..%d", kMaxDegree);
   if (!(tp.theta > 0.0 && tp.theta < 1.0)) fail(LPM_ERR_INVALID_ARGUMENT, "tree code: theta must be in (0, 1)");
   if (!treePairShapeSupported(shape)) fail(LPM_ERR_NOT_SUPPORTED, "tree code: plan built for another launch shape");
   const int ns = Pl.ns, nslots = Pl.nslots, ntiles = Pl.nTreeTiles;
   const int P = (tp.degree + 1) * (tp.degree + 1);
   ensureWatch();
-  poll();  // reports of earlier evaluations (no synchronisation)
+  // reports of earlier evaluations (no synchronisation); never while the stream is captured, where
+  // a report arriving now would make the capture grow a buffer (callers poll before capturing)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  ck(cudaStreamIsCapturing(s, &cap), "capture status");
+  if (cap == cudaStreamCaptureStatusNone) poll();
   direct_ = false;
   stats_ = TreeStats{};
   statsOnDevice_ = true;
@@ -716,7 +792,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     e1 = timer->get();
     ck(cudaEventRecord(e0, s), "event");
   }
-  ck(launchTreePair(shape, psi, precise, rcpApprox, dd, nitems, counter, std::min(nitems, std::max(1, slots)), s),
+  ck(launchTreePair(shape, psi, precise, rcpApprox, dd, nitems, counter,
+                    std::min(nitems, std::max(1, grid > 0 ? grid : slots)), s),
      "pair launch");
   if (timer) {
     ck(cudaEventRecord(e1, s), "event");

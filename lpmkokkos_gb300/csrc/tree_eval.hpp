@@ -25,15 +25,20 @@ class TreeEval {
   // and an evaluation whose lists do not fit sums every source directly (exact) and reports the
   // overflow, so the buffer grows before the next one.  After the first evaluation, and while
   // generation() stays the same, a call queues the same launches with the same arguments: the
-  // calls can be captured in a CUDA graph and replayed.
+  // calls can be captured in a CUDA graph and replayed.  `slots` (resident CTAs of the whole
+  // GPU) sets how each tile's list is cut into work items, and so the summation order; `grid`
+  // caps the pair kernel's persistent grid (0: slots), which changes no result.
   void evaluate(SolvePlan& P, const TreeParams& tp, const PairShape& shape, bool psi, bool precise, bool rcpApprox,
-                int slots, PairTimer* timer, cudaStream_t s);
+                int slots, int grid, PairTimer* timer, cudaStream_t s);
   // Applies the reports of evaluations since the last call (no synchronisation): grows the list
   // buffer after an overflow; true if that changed the launch arguments (a captured graph of
   // the evaluation must then be rebuilt).  Throws on a traversal stack overflow.
   bool poll();
-  // Ready to be captured: sized by a first evaluation and no growth pending.
-  bool ready() const { return (direct_ || listCap_ > 0) && !(watch_ && watch_->overflow); }
+  // Ready to be captured: sized by a first evaluation, no overflow reported since the last poll,
+  // and the list buffer already grown to the capacity a poll set (an evaluation grows it).
+  bool ready() const {
+    return direct_ || (listCap_ > 0 && bList.bytes >= sizeof(int) * (size_t)listCap_ && !(watch_ && watch_->overflow));
+  }
   // Changes whenever buffers or launch arguments change (graphs capture them).
   int generation() const { return generation_; }
   // Records that this solve's evaluation used the direct sum (smaller than TreeParams::minPairs).
@@ -47,6 +52,10 @@ class TreeEval {
   int nchunks() const { return nchunks_; }
   // Statistics of the last evaluation (reads the device: synchronises).
   const TreeStats& stats();
+  // Frees every device buffer in stream order on `s` and hands the report slot back to its pool
+  // from a host function queued there, so that neither this call nor the destructor waits for
+  // the device.  A later evaluation starts over (sizing pass included).
+  void release(cudaStream_t s);
 
  private:
   struct Buf {

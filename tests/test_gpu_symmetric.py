@@ -115,18 +115,45 @@ def test_rk4_against_fp64_and_plain(sctx, extra):
 
 
 def test_eps_and_stream_function(sctx, oracle):
+    """eps = 0.01 with the stream function: the symmetric kernel forms log2(2q) - 1 once per
+    unordered pair for both directions; velocity and stream function meet the bar against the
+    oracle, and the plain kernel's stream function (LPM_BVE_NO_SYMMETRIC) agrees to the same bar."""
     ctx = sctx
-    """eps = 0.01; with PSI the call takes the plain kernel (the symmetric one sums velocity
-    only) and the result still meets the bar."""
     m, fx, z, a, mk, zh = _setup(1, 5)
     leaf = m["fmask"] == 0
     u, _ = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED, eps=0.01)
+    u = u.clone()
     u2, p2 = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED | P.PSI, eps=0.01)
+    u2, p2 = u2.clone(), p2.clone()
+    u3, p3 = ctx.velocity(None, fx, z, a, mk, flags=P.FP32C | P.COLLOCATED | P.PSI | P.NO_SYMMETRIC, eps=0.01)
     torch.cuda.synchronize()
     _, ref, _, rp = oracle.velocity(m["vx"][:0], m["fx"], zh, m["farea"], m["fmask"], eps=0.01, psi=True)
     assert _l2(u.cpu().numpy()[leaf], ref[leaf]) <= TOL
     assert _l2(u2.cpu().numpy()[leaf], ref[leaf]) <= TOL
+    assert torch.equal(u[torch.from_numpy(leaf).cuda()], u2[torch.from_numpy(leaf).cuda()])
     assert _l2(p2.cpu().numpy()[leaf], rp[leaf]) <= TOL
+    assert _l2(p3.cpu().numpy()[leaf], rp[leaf]) <= TOL
+    assert not torch.equal(p2, p3)   # the symmetric kernel ran
+
+
+@pytest.mark.parametrize("seed,level,eps", [(0, 4, 0.0), (1, 4, 0.0), (0, 5, 0.05)])
+def test_stream_function_vertices_and_faces(sctx, oracle, seed, level, eps):
+    """BVESphere.solve with the stream function: vertices (plain kernel over all sources) and
+    leaf faces (symmetric kernel), eps 0 included (the logs of the smallest separations),
+    against the oracle."""
+    from lpmkokkos_gb300 import bve
+    s = bve.BVESphere(seed, level, layout="left")
+    s.init_vorticity(bve.rh54_gaussians(31 + level, 3), sctx, flags=P.FP64)
+    s.solve(sctx, flags=P.FP32C, eps=eps, psi=True)
+    torch.cuda.synchronize()
+    m = s.mesh
+    leaf = m["fmask"] == 0
+    uv, uf, pv, pf = oracle.velocity(m["vx"], m["fx"], s.relVortFaces.cpu().numpy(), m["farea"], m["fmask"],
+                                     eps=eps, psi=True)
+    assert _l2(s.velocityVerts.cpu().numpy(), uv) <= TOL
+    assert _l2(s.velocityFaces.cpu().numpy()[leaf], uf[leaf]) <= TOL
+    assert _l2(s.streamFnVerts.cpu().numpy(), pv) <= TOL
+    assert _l2(s.streamFnFaces.cpu().numpy()[leaf], pf[leaf]) <= TOL
 
 
 def test_size_threshold(ctx):
