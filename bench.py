@@ -141,8 +141,8 @@ def parse(argv=None):
     ap.add_argument("--no-tree", action="store_true",
                     help="c2/c3/c5: skip the tree-code leg (LPM_BVE_TREECODE, reported beside the direct sum)")
     ap.add_argument("--tree", action="store_true",
-                    help="c4: a server with LPM_BVE_TREECODE (requests of >= 1e9 pairs per evaluation run on "
-                         "its tree-code thread)")
+                    help="c4: a server with LPM_BVE_TREECODE (requests of >= 1e9 pairs per evaluation are set up "
+                         "by its tree threads and stepped in tree classes)")
     ap.add_argument("--tree-only", action="store_true",
                     help="c2/c5: time the tree-code leg alone (no direct steps; for profiling the tree path)")
     return ap.parse_args(argv)

@@ -11,6 +11,10 @@
  * leaves as soon as its own steps are done.  A solve's result does not depend on which other solves shared
  * its launches (per-solve summation order is fixed): bit-identical alone or in any mix.  Host
  * preparation (mesh, initial data, plan) runs on a separate thread.
+ * With LPM_BVE_TREECODE in flags, requests of at least 1e9 target x source pairs per evaluation
+ * take the tree code: two threads upload them and compute their initial velocity (which sizes
+ * their interaction lists), then they step in tree classes whose steps are captured graphs,
+ * side by side with the direct classes.
  */
 #ifndef LPM_BVE_SERVER_H
 #define LPM_BVE_SERVER_H

@@ -130,7 +130,7 @@ def test_eps_and_stream_function(sctx, oracle):
     _, ref, _, rp = oracle.velocity(m["vx"][:0], m["fx"], zh, m["farea"], m["fmask"], eps=0.01, psi=True)
     assert _l2(u.cpu().numpy()[leaf], ref[leaf]) <= TOL
     assert _l2(u2.cpu().numpy()[leaf], ref[leaf]) <= TOL
-    assert torch.equal(u[torch.from_numpy(leaf).cuda()], u2[torch.from_numpy(leaf).cuda()])
+    # (not bit-equal to u: with PSI the diagonal tile takes the symmetric sweep, not the plain tile)
     assert _l2(p2.cpu().numpy()[leaf], rp[leaf]) <= TOL
     assert _l2(p3.cpu().numpy()[leaf], rp[leaf]) <= TOL
     assert not torch.equal(p2, p3)   # the symmetric kernel ran
