@@ -843,7 +843,7 @@ def tree_leg(P, bve, torch, ctx, s0, dt, eps, steps, flush, lane_ops, check_step
         "octree": {"depth": ts["depth"], "nodes": ts["nodes"], "far_clusters": ts["far_clusters"]},
         "phase_ms_per_evaluation": {"octree_build": ts["build_ms"], "upward_pass": ts["upward_ms"],
                                     "interaction_lists": ts["list_ms"], "pair_kernel": pair_ms / pair_n},
-        "pair_kernel": {"kernel": "treeFP32C<32,8,256,8>", "pairs_per_evaluation": ts["pairs"],
+        "pair_kernel": {"kernel": "treeFP32C<32,4,128,12>", "pairs_per_evaluation": ts["pairs"],
                         "direct_pairs": ts["direct_pairs"], "proxy_pairs": ts["far_pairs"],
                         "computed_pairs_per_s": rate, "frac_of_fma_peak": rate / peak},
     }

@@ -878,7 +878,8 @@ struct ShapeFn {
 // Register use of the RK4 velocity kernel (ptxas, sm_103a, paired arithmetic) sets the
 // resident CTAs per SM: 128x4 unbounded 154 regs -> 3/SM, min-blocks 4: 124 -> 4/SM;
 // 128x6 min-blocks 3: 163 -> 3/SM; 128x8 233 -> 2/SM; 64x8 min-blocks 4: 233 -> 4/SM; 32x8 min-blocks 8
-// (the tree code's shape) -> 8/SM;
+// -> 8/SM; 32x4 with 128-source tiles, min-blocks 12 (the tree code's shape, for the direct solves of
+// a tree batch) -> 12/SM;
 // 256x4 min-blocks 2: 125 -> 2/SM.  None of these spills.
 const ShapeFn kShapes[] = {
   LPM_SHAPE(128, 4, 256, 1),
@@ -888,6 +889,7 @@ const ShapeFn kShapes[] = {
   LPM_SHAPE(64, 8, 256, 4),
   LPM_SHAPE(256, 4, 256, 2),
   LPM_SHAPE(32, 8, 256, 8),
+  LPM_SHAPE(32, 4, 128, 12),
 };
 #undef LPM_SHAPE
 

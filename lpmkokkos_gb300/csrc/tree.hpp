@@ -68,8 +68,11 @@ struct TreeStats {
 
 cudaError_t launchTreePair(const PairShape& shape, bool psi, bool precise, bool rcpApprox, const TreeDev* dev,
                            int nitems, int* counter, int grid, cudaStream_t s);
-// The tree kernel's launch shape: 32 threads x 8 targets (256-target tiles), 8 CTAs per SM.
-inline constexpr PairShape kTreeShape{32, 8, 256, 8};
+// The tree kernel's launch shape: 32 threads x 4 targets (128-target tiles), 128-record source
+// blocks, 12 CTAs per SM (160-168 registers, 10.8 KB of shared memory).  Smaller tiles take fewer
+// pairs (a tile's near field shrinks with its radius): 16.5 % fewer than 256-target tiles at
+// icosahedral level 8, 13.5 % at level 7.
+inline constexpr PairShape kTreeShape{32, 4, 128, 12};
 bool treePairShapeSupported(const PairShape& shape);
 
 }  // namespace lpm
