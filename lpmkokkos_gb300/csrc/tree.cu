@@ -96,40 +96,58 @@ __global__ void sortedSelf(const int* __restrict__ self, const int* __restrict__
 // middle child's, its velocity is near-singular in the reference's formula, and after a step it
 // runs away (its bounding sphere would then admit no far field).  Parents are still evaluated with their tile's
 // list; a cubed-sphere parent sits on its children's shared corner, inside the tile.
+// One warp per tile (tiles hold at most a few hundred slots); the butterfly reductions leave the
+// same value in every lane.
+__device__ __forceinline__ double warpSumAll(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warpMaxAll(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+constexpr int kGeomTilesPerBlock = kBlock / 32;
+
 __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict__ tx, int n,
-                                                       const int2* __restrict__ tiles, const int* __restrict__ perm,
-                                                       int64_t na, const uint8_t* __restrict__ mask,
+                                                       const int2* __restrict__ tiles, int ntiles,
+                                                       const int* __restrict__ perm, int64_t na,
+                                                       const uint8_t* __restrict__ mask,
                                                        double4_32a* __restrict__ geom) {
-  __shared__ double sh[kBlock / 32];
-  const int2 tr = tiles[blockIdx.x];
+  const int lane = threadIdx.x & 31;
+  const int tile = blockIdx.x * kGeomTilesPerBlock + (threadIdx.x >> 5);
+  if (tile >= ntiles) return;  // the whole warp
+  const int2 tr = tiles[tile];
   const int t0 = tr.x, cnt = tr.y;
   auto shapes = [&](int slot, double x, double y, double z) {
     const int id = perm[slot];
     return sane(x, y, z) && !(mask && id >= na && mask[id - na]);
   };
   double sx = 0, sy = 0, sz = 0, sc = 0;
-  for (int q = threadIdx.x; q < cnt; q += kBlock) {
+  for (int q = lane; q < cnt; q += 32) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
     if (shapes(slot, x, y, z)) { sx += x; sy += y; sz += z; sc += 1.0; }
   }
-  sx = blockSum<kBlock>(sx, sh);
-  sy = blockSum<kBlock>(sy, sh);
-  sz = blockSum<kBlock>(sz, sh);
-  sc = blockSum<kBlock>(sc, sh);
+  sx = warpSumAll(sx);
+  sy = warpSumAll(sy);
+  sz = warpSumAll(sz);
+  sc = warpSumAll(sc);
   if (sc == 0.0) {
-    if (threadIdx.x == 0) geom[blockIdx.x] = make_double4_32a(0, 0, 0, INFINITY);
+    if (lane == 0) geom[tile] = make_double4_32a(0, 0, 0, INFINITY);
     return;
   }
   const double cx = sx / sc, cy = sy / sc, cz = sz / sc;
   double r2 = 0.0;
-  for (int q = threadIdx.x; q < cnt; q += kBlock) {
+  for (int q = lane; q < cnt; q += 32) {
     const int slot = t0 + q;
     const double x = tx[slot], y = tx[n + slot], z = tx[2 * n + slot];
     if (shapes(slot, x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
   }
-  r2 = blockMax<kBlock>(r2, sh);
-  if (threadIdx.x == 0) geom[blockIdx.x] = make_double4_32a(cx, cy, cz, sqrt(r2));
+  r2 = warpMaxAll(r2);
+  if (lane == 0) geom[tile] = make_double4_32a(cx, cy, cz, sqrt(r2));
 }
 
 // Chebyshev points of the second kind t_a = cos(pi a / n) and their barycentric weights.
@@ -697,7 +715,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   }
   // 5. tiles
   double4_32a* tgeom = grow<double4_32a>(bTileGeom, ntiles, s);
-  tileGeometry<<<ntiles, kBlock, 0, s>>>(Pl.stage.tx, nslots, Pl.treeTiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
+  tileGeometry<<<(ntiles + kGeomTilesPerBlock - 1) / kGeomTilesPerBlock, kBlock, 0, s>>>(
+      Pl.stage.tx, nslots, Pl.treeTiles, ntiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
   // 6. interaction lists: lengths, offsets (a device scan), the work order (a device sort) and
   // the indices -- nothing read back but the very first total, which sizes the list buffer
   int64_t* lens = grow<int64_t>(bLen, ntiles, s);
