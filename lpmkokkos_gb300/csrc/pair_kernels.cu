@@ -484,16 +484,15 @@ __global__ void __launch_bounds__(NTH, MINB) treeFP32C(const TreeDev* __restrict
       hx[k] = hy[k] = hz[k] = cx[k] = cy[k] = cz[k] = 0.f;
       hp[k] = cp[k] = hw[k] = cw[k] = 0.f;
     }
-    // part `part` of the tile's list: [l0, l1), cut at multiples of the sub-block.  When the
-    // evaluation's lists overflowed their buffer, every tile takes every sorted source instead
-    // (the exact direct sum; the host grows the buffer for the next evaluation).
-    const bool dir = *S.overflow != 0;
-    const int64_t tl = dir ? (int64_t)S.ns : S.listOff[tile + 1] - S.listOff[tile];
+    // part `part` of the tile's list: [l0, l1), cut at multiples of the sub-block.  (When the
+    // evaluation's lists overflowed their buffer, every tile's list is the identity list of all
+    // sorted sources: the exact direct sum.)
+    const int64_t tl = S.listLen[tile];
     const int64_t l0 = tl * part / S.nchunks / kSub * kSub;
     const int64_t l1 = part + 1 == S.nchunks ? tl : tl * (part + 1) / S.nchunks / kSub * kSub;
-    const int64_t off = dir ? l0 : S.listOff[tile] + l0;
+    const int64_t off = S.listOff[tile] + l0;
     const int64_t len = l1 - l0;
-    auto entry = [&](int64_t q) { return dir ? (int)(off + q) : S.list[off + q]; };
+    auto entry = [&](int64_t q) { return S.list[off + q]; };
     // Pipeline: the records of block b + 1 are copied (cp.async) and the list indices of block
     // b + 2 loaded into registers while block b computes; staging then reads shared memory only.
     int nextId[kPer];

@@ -431,6 +431,19 @@ __global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ t
   }
 }
 
+// Lists that overflowed their buffer (the fill wrote nothing): every tile's list becomes the
+// identity list of all sorted sources, the exact direct sum (the buffer holds at least ns).
+__global__ void directFallback(const int* __restrict__ overflow, int64_t* __restrict__ off,
+                               int64_t* __restrict__ lens, int ntiles, int* __restrict__ list, int ns) {
+  if (!*overflow) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < ntiles) {
+    off[i] = 0;
+    lens[i] = ns;
+  }
+  if (i < ns) list[i] = i;
+}
+
 // The list buffer's capacity check, before the fill: overflow = total > capacity.
 __global__ void capCheck(const int64_t* __restrict__ total, int64_t cap, int* __restrict__ overflow) {
   *overflow = *total > cap ? 1 : 0;
@@ -749,7 +762,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     int64_t total = 0;
     ck(cudaMemcpyAsync(&total, off + ntiles, sizeof(int64_t), cudaMemcpyDeviceToHost, s), "read-back");
     ck(cudaStreamSynchronize(s), "synchronise");
-    listCap_ = (int64_t)(1.25 * (double)total) + 4096;
+    listCap_ = std::max<int64_t>((int64_t)(1.25 * (double)total) + 4096, ns);  // >= ns: the fallback
     ++generation_;
   }
   int* oldList = static_cast<int*>(bList.p);
@@ -772,6 +785,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   double* dstats = grow<double>(bStats, 5, s);
   treeStats<<<1, kBlock, 0, s>>>(Pl.treeTiles, lens, fars, ntiles, P, ns, overflow, ns > 0 ? tree_.dcount : nullptr,
                                  depth, dstats);
+  directFallback<<<blocks(std::max(1, std::max(ntiles, ns))), kBlock, 0, s>>>(overflow, off, lens, ntiles, list, ns);
   mark(4);
   // 7. the gathered pair kernel
   double* partial = grow<double>(bPartial, (size_t)nchunks * 5 * std::max(1, nslots), s);
@@ -788,7 +802,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   hd.list = list;
   hd.order = order;
   hd.partial = partial;
-  hd.overflow = overflow;
+  hd.listLen = lens;
   hd.nslots = nslots;
   hd.ntiles = ntiles;
   hd.nchunks = nchunks;

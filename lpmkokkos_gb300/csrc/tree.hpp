@@ -48,11 +48,11 @@ struct TreeDev {
   const int* srcSlot;      // [ns] slot of the same particle as sorted source k, -1 if none
   const int2* tiles;       // [ntiles] {first slot, count} (runs inside one level-3 Morton cell)
   const int* tileCentre;   // [ntiles] centre slot of the tile (as in the direct kernel)
-  const int64_t* listOff;  // [ntiles + 1] offsets into list
+  const int64_t* listOff;  // [ntiles] offset of each tile's list in `list`
+  const int64_t* listLen;  // [ntiles] its length
   const int* list;         // flattened per-tile source indices into sp0/sp1
   const int* order;        // [ntiles * nchunks] work items (tile * nchunks + part), longest first
   double* partial;         // [nchunks][ncomp][nslots]: part c of every tile's list sums into chunk c
-  const int* overflow;     // nonzero: the lists did not fit their buffer; every tile sums every source
   int nslots, ntiles, nchunks, ns;
   double eps2;
 };

@@ -57,6 +57,37 @@ def test_velocity_and_psi_against_fp64(tctx, seed, level):
     assert st["far_clusters"] > 0 and st["far_pairs"] > 0
 
 
+def test_list_overflow_falls_back_to_direct_then_grows(tctx):
+    """The list buffer is sized by a solve's first evaluation.  Shuffling the face positions in
+    place (the cached plan keeps its tiles, which become spatially random, so almost nothing is
+    far field) makes the next evaluation's lists outgrow the buffer: that evaluation sums every
+    source for every tile (the exact direct sum) and reports it, and the one after runs with a
+    grown buffer.  Both meet the FP32C bar against the FP64 sum of the shuffled state."""
+    ctx = tctx
+    s, src, leaf = _sphere(ctx, 0, 5)
+    nf, nl = s.physFaces.shape[0], int(leaf.sum())
+    ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    torch.cuda.synchronize()
+    assert ctx.tree_stats()["far_pairs"] > 0
+    g = torch.Generator().manual_seed(5)
+    perm = torch.randperm(nf, generator=g).cuda()
+    s.physFaces.copy_(s.physFaces[perm].clone())
+    t2, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    t2 = t2.clone()
+    torch.cuda.synchronize()
+    st2 = ctx.tree_stats()
+    assert st2["far_pairs"] == 0 and st2["pairs"] == nf * nl, st2  # the direct fallback
+    t3, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
+    t3 = t3.clone()
+    torch.cuda.synchronize()
+    st3 = ctx.tree_stats()
+    assert st3["pairs"] <= nf * nl, st3
+    ref, _ = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED)
+    torch.cuda.synchronize()
+    e2, e3 = _rel(t2[leaf], ref[leaf]), _rel(t3[leaf], ref[leaf])
+    assert e2 <= TOL and e3 <= TOL, (e2, e3)
+
+
 def test_reproducible_and_work_reduction(tctx):
     ctx = tctx
     s, src, leaf = _sphere(ctx, 0, 6)
