@@ -429,6 +429,26 @@ void refreshTables(Batch& B, cudaStream_t s) {
   LPM_CUDA(cudaStreamSynchronize(s));
 }
 
+// Side streams of a batch's tree-code evaluations (created on first use, with the priority of
+// the stream the batch runs on) and the fork / join events.
+constexpr int kTreeLanes = 4;
+int ensureTreeLanes(Batch& B, cudaStream_t s, int want) {
+  if ((int)B.treeLanes.size() < want) {
+    int prio = 0;
+    LPM_CUDA(cudaStreamGetPriority(s, &prio));
+    if (!B.treeFork) LPM_CUDA(cudaEventCreateWithFlags(&B.treeFork, cudaEventDisableTiming));
+    while ((int)B.treeLanes.size() < want) {
+      cudaStream_t l = nullptr;
+      cudaEvent_t e = nullptr;
+      LPM_CUDA(cudaStreamCreateWithPriority(&l, cudaStreamNonBlocking, prio));
+      B.treeLanes.push_back(l);
+      LPM_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      B.treeJoin.push_back(e);
+    }
+  }
+  return want;
+}
+
 // One evaluation of the direct sums for every solve of the batch.
 void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity, cudaStream_t s,
                  const EvalNames* names) {
@@ -439,16 +459,29 @@ void enqueueEval(Batch& B, int prepStage, int stageOut, bool psi, bool velocity,
   std::unique_ptr<NvtxRange> pairRange(names ? new NvtxRange(names->pair) : nullptr);
   if (B.treeMode) {  // tree code: per solve octree, lists and gathered pair kernel; one epilogue
     const size_t n = B.solves.size();
+    int ntree = 0;
+    for (size_t m = 0; m < n; ++m) ntree += B.treeDirect[m] ? 0 : 1;
+    const int lanes = ntree > 1 ? ensureTreeLanes(B, s, std::min(ntree, kTreeLanes)) : 0;
+    if (lanes > 0) {  // fork before the direct launch, so that both run side by side
+      LPM_CUDA(cudaEventRecord(B.treeFork, s));
+      for (int k = 0; k < lanes; ++k) LPM_CUDA(cudaStreamWaitEvent(B.treeLanes[k], B.treeFork, 0));
+    }
     // solves below the size threshold: one persistent direct launch over their work items
     if (B.nDirectItems > 0)
       LPM_CUDA(launchPair(B.prec, B.shape, psi, B.precise, B.rcpApprox, B.solveDev, B.directItems, B.nDirectItems,
                           B.counter, std::min(B.nDirectItems, B.slots), s));
-    for (size_t m = 0; m < n; ++m) {
+    for (size_t m = 0, j = 0; m < n; ++m) {
       TreeEval& T = *B.trees[m];
-      if (B.treeDirect[m])
+      if (B.treeDirect[m]) {
         T.markDirect(*B.solves[m]);
-      else
-        T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.treeGrid, B.timer, s);
+        continue;
+      }
+      const cudaStream_t ts = lanes > 0 ? B.treeLanes[j++ % lanes] : s;
+      T.evaluate(*B.solves[m], B.treeParams, B.shape, psi, B.precise, B.rcpApprox, B.slots, B.treeGrid, B.timer, ts);
+    }
+    for (int k = 0; k < lanes; ++k) {
+      LPM_CUDA(cudaEventRecord(B.treeJoin[k], B.treeLanes[k]));
+      LPM_CUDA(cudaStreamWaitEvent(s, B.treeJoin[k], 0));
     }
     pairRange.reset();
     treeStageTable(B, s);
@@ -750,7 +783,8 @@ void useTree(lpm_bve_ctx* ctx, Batch& B, bool tree, cudaStream_t s) {
 
 }  // namespace
 
-void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp) {
+void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp,
+                 cudaStream_t s) {
   if (trees.size() != B.solves.size()) fail(LPM_ERR_INTERNAL, "tree code: one evaluator per solve");
   B.treeMode = true;
   B.trees = trees;
@@ -762,6 +796,7 @@ void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, 
   B.directMem.release();
   B.directItems = nullptr;
   B.nDirectItems = 0;
+  if (trees.size() > 1) ensureTreeLanes(B, s, std::min<int>((int)trees.size(), kTreeLanes));
 }
 }  // namespace lpm
 

@@ -228,6 +228,12 @@ struct Batch {
   bool treeMode = false;
   TreeParams treeParams;
   int treeGrid = 0;  // cap of the tree pair kernel's persistent grid (0: slots)
+  // several tree-code solves: their evaluations run on up to kTreeLanes side streams forked from
+  // the batch's stream after the prep kernel and joined before the epilogue (in a captured step,
+  // parallel branches), so that one solve's small octree and list kernels overlap another's
+  std::vector<cudaStream_t> treeLanes;
+  cudaEvent_t treeFork = nullptr;
+  std::vector<cudaEvent_t> treeJoin;
   int slots = 0;  // resident CTA slots of the pair kernels (SMs x CTAs per SM)
   // captured RK4 step
   cudaGraphExec_t graph = nullptr;
@@ -235,6 +241,9 @@ struct Batch {
   int graphTreeGen = 0;  // the tree evaluations' generation the graph was captured with
   ~Batch() {
     if (graph) cudaGraphExecDestroy(graph);
+    for (cudaEvent_t e : treeJoin) cudaEventDestroy(e);
+    if (treeFork) cudaEventDestroy(treeFork);
+    for (cudaStream_t l : treeLanes) cudaStreamDestroy(l);  // released once their work completes
   }
 };
 
@@ -283,8 +292,10 @@ void enqueueStep(Batch& B, bool quirk, bool renorm, cudaStream_t s);
 void treeStageTable(Batch& B, cudaStream_t s);
 // Puts a finalized batch in tree-code mode with evaluators the caller keeps (one per solve, in
 // solve order): buffers, list capacity and octree carry over from batch to batch.  Every solve
-// takes the tree code.
-void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp);
+// takes the tree code.  `s` is the stream the batch will run on (its side streams, created here
+// so that a first step can be captured, take its priority).
+void attachTrees(Batch& B, const std::vector<std::shared_ptr<TreeEval>>& trees, const TreeParams& tp,
+                 cudaStream_t s);
 
 // Snapshot file of a state held in host row-major arrays (snapshot.cpp).
 void writeSnapshotHost(const char* path, int seed, int level, int vpf, int64_t nv, int64_t nf, double t, double dt,

@@ -502,7 +502,7 @@ std::unique_ptr<Batch> makeBatch(lpm_bve_server* S, const std::vector<Req*>& rs,
   if (tree) {
     std::vector<std::shared_ptr<TreeEval>> trees;
     for (Req* r : rs) trees.push_back(r->tree);
-    attachTrees(*B, trees, S->treeParams);
+    attachTrees(*B, trees, S->treeParams, lane);
     bool sized = true;
     for (Req* r : rs) sized = sized && r->tree->ready();
     if (sized) treeStageTable(*B, s);  // else the first (uncaptured) evaluation uploads it

@@ -58,7 +58,7 @@ def test_velocity_and_psi_against_fp64(tctx, seed, level):
 
 
 def test_list_overflow_falls_back_to_direct_then_grows(tctx):
-    """The list buffer is sized by a solve's first evaluation.  Shuffling the face positions in
+    """The list buffer is sized by a solve's first evaluation.  Shuffling the leaf positions in
     place (the cached plan keeps its tiles, which become spatially random, so almost nothing is
     far field) makes the next evaluation's lists outgrow the buffer: that evaluation sums every
     source for every tile (the exact direct sum) and reports it, and the one after runs with a
@@ -69,9 +69,12 @@ def test_list_overflow_falls_back_to_direct_then_grows(tctx):
     ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
     torch.cuda.synchronize()
     assert ctx.tree_stats()["far_pairs"] > 0
+    # leaves among leaves only: a few masked parents sit exactly on a leaf, and as sources they
+    # would make exactly coincident pairs
     g = torch.Generator().manual_seed(5)
-    perm = torch.randperm(nf, generator=g).cuda()
-    s.physFaces.copy_(s.physFaces[perm].clone())
+    idx = torch.nonzero(leaf).flatten()
+    perm = idx[torch.randperm(idx.numel(), generator=g).cuda()]
+    s.physFaces[idx] = s.physFaces[perm].clone()
     t2, _ = ctx.velocity(None, *src, flags=P.FP32C | P.COLLOCATED | P.TREECODE)
     t2 = t2.clone()
     torch.cuda.synchronize()
