@@ -286,23 +286,18 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
       basisF(ueta, degree, sT, sBw, 1.f, &sL[t][n1]);
     }
     __syncthreads();
-    if (t < P) {  // Kahan-compensated FP32 over the chunk (the FP32 pipe; FP64 is 1/64 of it), even
-      // and odd sources in two independent sums: half the dependency chain of one
+    if (t < P) {  // Kahan-compensated FP32 over the chunk (the FP32 pipe; FP64 is 1/64 of it)
+      // (two interleaved sums over even and odd sources measured slower: 1.47 against 1.25 ms per
+      // level-8 pass)
       const int m = min(kUpThreads, k1 - c0);
-      float h0 = 0.f, e0 = 0.f, h1 = 0.f, e1 = 0.f;
-      auto add = [](float& h, float& c, float v) {
-        const float y = v - c;
+      float h = 0.f, c = 0.f;
+      for (int j = 0; j < m; ++j) {
+        const float y = sL[j][ia] * sL[j][n1 + ib] - c;
         const float tt = h + y;
         c = (tt - h) - y;
         h = tt;
-      };
-      int j = 0;
-      for (; j + 1 < m; j += 2) {
-        add(h0, e0, sL[j][ia] * sL[j][n1 + ib]);
-        add(h1, e1, sL[j + 1][ia] * sL[j + 1][n1 + ib]);
       }
-      if (j < m) add(h0, e0, sL[j][ia] * sL[j][n1 + ib]);
-      q += ((double)h0 - (double)e0) + ((double)h1 - (double)e1);
+      q += (double)h - (double)c;
     }
     __syncthreads();
   }
