@@ -520,7 +520,7 @@ def oracle_parity(ctx, P, torch, np, sphere, w, prec, solve=True):
     `solve`, else as init_vorticity or the stream-function pass left them) and the plain FP64
     path at the sampled targets, against the CPU oracle on 4,096 random vertices and 4,096 random
     leaf faces summed over all sources: relative L2 for FP32C, max |e| / max |ref| for FP64
-    (oracle/sampled_parity.py, the checker)."""
+    (oracle/sampled_parity.py, part of the oracle)."""
     from oracle import sampled_parity as SP
     t0 = time.time()
     eps = w["eps"]
@@ -606,7 +606,7 @@ def _fp64_sample_rate(ctx, P, torch, np, sphere, eps, ntargets=32768, seed=5):
 
 
 def fp64_denominators(ctx, P, bve, torch, np, sphere, w, pairs_done, ms_per_step, full_level=6):
-    """The plain FP64 GPU path (the GPU oracle of the north star's "FP32C vs FP64" target).
+    """The plain FP64 GPU path (the GPU oracle of the "FP32C vs FP64" target: at least 4x its RK4 steps/s).
     A full FP64 step at this level takes minutes (level 8: ~12 min), so its steps/s is
     extrapolated from the pair rate on 32,768 sampled vertex targets; the extrapolation is checked
     by one full FP64 RK4 step at level `full_level` (graph-replayed, after a warm-up step) timed

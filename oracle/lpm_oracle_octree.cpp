@@ -1,7 +1,7 @@
 // lpm_oracle_octree.cpp -- TEST INFRASTRUCTURE ONLY (the oracle).
 //
 // Serial CPU restatement of the data-parallel Morton octree of pbosler/lpmKokkos
-// (Zhou et al. 2011, listings 1 and 2), used as the checker for the GPU octree:
+// (Zhou et al. 2011, listings 1 and 2), the reference that the GPU octree is compared with:
 //
 //   bounding box            BoxFunctor / BBoxReducer     src/LpmBox3d.hpp:84-160
 //   cube from box           box2cube                     src/LpmBox3d.hpp:290-303

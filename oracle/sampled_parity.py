@@ -7,7 +7,7 @@ test's time, but each target of the reference's reductions is independent of the
 checks the GPU at full size.  The subset holds vertices (distinct targets) and leaf faces
 (collocated targets, the i == j pair excluded by index).
 
-Only tests/ and bench.py's parity field use this module; it is the checker, never the thing
+Only tests/ and bench.py's parity field use this module; it is the oracle, never the thing
 measured.
 """
 from __future__ import annotations

@@ -189,7 +189,7 @@ def test_invalid(ctx):
 
 
 def test_regularised_kernel(tctx):
-    """eps > 0 (the regularised kernel of the benchmark spec; absent from the reference)."""
+    """eps > 0 (the regularised kernel 1 / (1 - x.y + eps^2); absent from the reference)."""
     ctx = tctx
     s, src, leaf = _sphere(ctx, 0, 6)
     rf, pf = ctx.velocity(None, *src, flags=P.FP64 | P.COLLOCATED | P.PSI, eps=0.01)

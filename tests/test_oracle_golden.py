@@ -1,6 +1,6 @@
 """The CPU oracle against the reference's own known answers (no GPU).
 
-Pins the restatement before it is trusted as the checker:
+Pins the restatement before it is trusted as the oracle:
   * the recorded spherical-Poisson psi linf table, icosahedral and cubed sphere, levels 0-5
     (scripts/poissonOutput.py:6-30; the reference ran the same kernels on CPU and GPU and
     printed identical numbers) -- to the printed 6 significant digits;
