@@ -112,7 +112,7 @@ def parse(argv=None):
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--prec", choices=["fp32c", "fp64"], default="fp32c")
     ap.add_argument("--e2e-steps", type=int, default=0,
-                    help="RK4 steps of the end-to-end pass (0: half of --steps, at least 3)")
+                    help="RK4 steps of the end-to-end pass (0: as many as --steps, at least 3)")
     ap.add_argument("--err-steps", type=int, default=0,
                     help="c2/c5: also advance an FP64 trajectory beside an FP32C one for this many steps and report "
                          "the per-step velocity/vorticity errors (device norms; FP64 is ~150x slower)")
@@ -361,7 +361,7 @@ def run_ours(args, rank, world, local_rank):
     peak_nominal = sms * 128 * 2070e6 / OPS_PER_PAIR / 1e9
 
     # 3) end to end through the public API with host buffers
-    e2e_steps = args.e2e_steps if args.e2e_steps > 0 else max(3, args.steps // 2)
+    e2e_steps = args.e2e_steps if args.e2e_steps > 0 else max(3, args.steps)
     names = ("vx", "vzeta", "vvel", "fx", "fzeta", "fvel")
     host = {n: torch.empty(getattr(st, n).shape, dtype=torch.float64, pin_memory=True) for n in names}
     for n in names:
