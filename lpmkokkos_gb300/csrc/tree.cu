@@ -191,8 +191,7 @@ __device__ __forceinline__ void basisF(float u, int n, const float* t, const flo
 // more than (n+1)^2 sources all within ~37 degrees of the centre direction, the gnomonic chart,
 // the proxy charges Q_ab (one thread per proxy, sources in index order) and the proxy records
 // at sp0/sp1[ns + g (n+1)^2 + ab].
-__global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, const double* __restrict__ pos,
-                                                     int degree, const Cheb C, int ns, int firstNode,
+__global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, int degree, const Cheb C, int ns, int firstNode,
                                                      double4_32a* __restrict__ geom, int* __restrict__ approx,
                                                      float4* __restrict__ sp0, float4* __restrict__ sp1) {
   __shared__ double sh[kUpThreads / 32];
@@ -212,11 +211,19 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
     return;
   }
   const int k0 = pt.x, k1 = pt.x + pt.y;
-  double sx = 0, sy = 0, sz = 0;
-  for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) { sx += pos[3 * k]; sy += pos[3 * k + 1]; sz += pos[3 * k + 2]; }
-  sx = blockSum<kUpThreads>(sx, sh);
-  sy = blockSum<kUpThreads>(sy, sh);
-  sz = blockSum<kUpThreads>(sz, sh);
+  // Every per-source loop reads the sources' FP32 hi/lo records (sp0/sp1, key order), not their
+  // FP64 positions: FP64 runs at 1/64 of the FP32 rate on GB300, and with FP64 sums, differences
+  // and conversions per source this pass was FP64-pipe bound.  The centroid only has to lie near
+  // the cluster (the radius and chart extents are measured from it); each thread sums its hi
+  // parts in FP32, the block in FP64.
+  float fsx = 0.f, fsy = 0.f, fsz = 0.f;
+  for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) {
+    const float4 a = sp0[k];
+    fsx += a.x; fsy += a.y; fsz += a.z;
+  }
+  const double sx = blockSum<kUpThreads>((double)fsx, sh);
+  const double sy = blockSum<kUpThreads>((double)fsy, sh);
+  const double sz = blockSum<kUpThreads>((double)fsz, sh);
   const double cx = sx / pt.y, cy = sy / pt.y, cz = sz / pt.y;
   const double cn = sqrt(cx * cx + cy * cy + cz * cz);
   const bool cand = pt.y > P && cn > 1e-3;
@@ -239,7 +246,8 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   const float f1x = (float)e1x, f1y = (float)e1y, f1z = (float)e1z, f2x = (float)e2x, f2y = (float)e2y, f2z = (float)e2z;
   float r2 = 0.f, dmin = FLT_MAX, xmin = FLT_MAX, xmax = -FLT_MAX, ymin = FLT_MAX, ymax = -FLT_MAX;
   for (int k = k0 + threadIdx.x; k < k1; k += kUpThreads) {
-    const float x = (float)pos[3 * k], y = (float)pos[3 * k + 1], z = (float)pos[3 * k + 2];
+    const float4 a = sp0[k];
+    const float x = a.x, y = a.y, z = a.z;  // hi parts: within 6e-8 of the position
     r2 = fmaxf(r2, (x - fcx) * (x - fcx) + (y - fcy) * (y - fcy) + (z - fcz) * (z - fcz));
     if (cand) {
       const float d = x * fux + y * fuy + z * fuz;
@@ -269,20 +277,26 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   const double mx = 0.5 * (xlo + xhi), hx = 0.5 * (xhi - xlo);
   const double my = 0.5 * (ylo + yhi), hy = 0.5 * (yhi - ylo);
   const float fmx = (float)mx, fmy = (float)my, fihx = (float)(1.0 / hx), fihy = (float)(1.0 / hy);
+  // the chart centre c^ as FP32 hi/lo parts, for the offsets below
+  const float uhx = fux, uhy = fuy, uhz = fuz;
+  const float ulx = (float)(ux - (double)uhx), uly = (float)(uy - (double)uhy), ulz = (float)(uz - (double)uhz);
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
   double q = 0.0;  // FP64 total of the per-chunk compensated FP32 sums
   for (int c0 = k0; c0 < k1; c0 += kUpThreads) {
     const int k = c0 + t;
     if (k < k1) {
-      // chart coordinates from the offset d = x - c^ (FP64 difference, then FP32): x.c^ = 1 + d.c^
-      // and x.e = d.e for the tangent directions, so every FP32 product is of the offset's size
-      // and the coordinates carry ~1e-7 of it, not of |x|
-      const float dx = (float)(pos[3 * k] - ux), dy = (float)(pos[3 * k + 1] - uy), dz = (float)(pos[3 * k + 2] - uz);
+      // chart coordinates from the offset d = x - c^: x.c^ = 1 + d.c^ and x.e = d.e for the
+      // tangent directions, so every FP32 product is of the offset's size and the coordinates
+      // carry ~1e-7 of it, not of |x|.  d from hi/lo parts: the hi difference is exact when the
+      // coordinates are within a factor 2 (a cluster within ~37 degrees of c^), the lo parts
+      // add the rest.
+      const float4 a = sp0[k], b = sp1[k];
+      const float dx = (a.x - uhx) + (b.x - ulx), dy = (a.y - uhy) + (b.y - uly), dz = (a.z - uhz) + (b.z - ulz);
       const float rd = __frcp_rn(1.f + (dx * fux + dy * fuy + dz * fuz));
       const float uxi = ((dx * f1x + dy * f1y + dz * f1z) * rd - fmx) * fihx;
       const float ueta = ((dx * f2x + dy * f2y + dz * f2z) * rd - fmy) * fihy;
-      basisF(uxi, degree, sT, sBw, sp0[k].w, &sL[t][0]);  // w L_a(xi): one FMA per proxy below
+      basisF(uxi, degree, sT, sBw, a.w, &sL[t][0]);  // w L_a(xi): one FMA per proxy below
       basisF(ueta, degree, sT, sBw, 1.f, &sL[t][n1]);
     }
     __syncthreads();
@@ -715,7 +729,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     // 4. upward pass (empty nodes return at once)
     geom = grow<double4_32a>(bGeom, nnodes, s);
     approx = grow<int>(bApprox, nnodes, s);
-    upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tree_.sorted, tp.degree, chebFor(tp.degree), ns,
+    upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tp.degree, chebFor(tp.degree), ns,
                                          depth >= 2 ? tree_.base[2] : nnodes, geom, approx, tsp0, tsp1);
     mark(2);
   } else {
