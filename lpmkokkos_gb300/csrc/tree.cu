@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
                                                        const int2* __restrict__ tiles, int ntiles,
                                                        const int* __restrict__ perm, int64_t na,
                                                        const uint8_t* __restrict__ mask,
-                                                       double4_32a* __restrict__ geom) {
+                                                       float4* __restrict__ geom) {
   const int lane = threadIdx.x & 31;
   const int tile = blockIdx.x * kGeomTilesPerBlock + (threadIdx.x >> 5);
   if (tile >= ntiles) return;  // the whole warp
@@ -136,7 +136,7 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
   sz = warpSumAll(sz);
   sc = warpSumAll(sc);
   if (sc == 0.0) {
-    if (lane == 0) geom[tile] = make_double4_32a(0, 0, 0, INFINITY);
+    if (lane == 0) geom[tile] = make_float4(0.f, 0.f, 0.f, INFINITY);
     return;
   }
   const double cx = sx / sc, cy = sy / sc, cz = sz / sc;
@@ -147,7 +147,8 @@ __global__ void __launch_bounds__(kBlock) tileGeometry(const double* __restrict_
     if (shapes(slot, x, y, z)) r2 = fmax(r2, (x - cx) * (x - cx) + (y - cy) * (y - cy) + (z - cz) * (z - cz));
   }
   r2 = warpMaxAll(r2);
-  if (lane == 0) geom[tile] = make_double4_32a(cx, cy, cz, sqrt(r2));
+  // FP32 for the traversal's acceptance test; the 1e-6 margin covers the rounded centre
+  if (lane == 0) geom[tile] = make_float4((float)cx, (float)cy, (float)cz, (float)(sqrt(r2) + 1e-6));
 }
 
 // Chebyshev points of the second kind t_a = cos(pi a / n) and their barycentric weights.
@@ -192,7 +193,7 @@ __device__ __forceinline__ void basisF(float u, int n, const float* t, const flo
 // the proxy charges Q_ab (one thread per proxy, sources in index order) and the proxy records
 // at sp0/sp1[ns + g (n+1)^2 + ab].
 __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, int degree, const Cheb C, int ns, int firstNode,
-                                                     double4_32a* __restrict__ geom, int* __restrict__ approx,
+                                                     float4* __restrict__ geom, int* __restrict__ approx,
                                                      float4* __restrict__ sp0, float4* __restrict__ sp1) {
   __shared__ double sh[kUpThreads / 32];
   __shared__ float sL[kUpThreads][2 * kMaxNodes1D];
@@ -207,7 +208,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   if (pt.y == 0 || g < firstNode) {
     // empty; or the root and the octants, whose sources span more than any chart allows (their
     // geometry would only ever open them, so they are opened unconditionally: infinite radius)
-    if (threadIdx.x == 0) { geom[g] = make_double4_32a(0, 0, 0, pt.y == 0 ? -1.0 : INFINITY); approx[g] = 0; }
+    if (threadIdx.x == 0) { geom[g] = make_float4(0.f, 0.f, 0.f, pt.y == 0 ? -1.f : INFINITY); approx[g] = 0; }
     return;
   }
   const int k0 = pt.x, k1 = pt.x + pt.y;
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   double yhi = blockMax<kUpThreads>((double)ymax, sh);
   const bool valid = cand && dlo >= kMinChartCos && xhi > xlo && yhi > ylo;
   if (threadIdx.x == 0) {
-    geom[g] = make_double4_32a(cx, cy, cz, rad);
+    geom[g] = make_float4((float)cx, (float)cy, (float)cz, (float)rad);  // rad's 1e-6 margin covers the rounding
     approx[g] = valid ? 1 : 0;
   }
   if (!valid) return;
@@ -342,10 +343,10 @@ constexpr int kWarpStack = 4096;  // per-warp node stack: <= 256 entries per lev
 // list at listOff[tile], contiguous direct ranges merged.  A stack overflow (impossible for the
 // depths the tree code builds) sets *err instead of writing out of bounds.
 template <bool FILL>
-__global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ tileGeom, int ntiles,
-                                               const double4_32a* __restrict__ geom, const int* __restrict__ approx,
+__global__ void __launch_bounds__(32) traverse(const float4* __restrict__ tileGeom, int ntiles,
+                                               const float4* __restrict__ geom, const int* __restrict__ approx,
                                                const int2* __restrict__ ptInds, const int* __restrict__ kids,
-                                               Levels lv, int depth, double theta, int P, int ns,
+                                               Levels lv, int depth, float theta2, int P, int ns,
                                                int64_t* __restrict__ lens, int64_t* __restrict__ farLens,
                                                const int64_t* __restrict__ listOff, int* __restrict__ list,
                                                const int* __restrict__ overflow, int* __restrict__ err) {
@@ -354,7 +355,7 @@ __global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ t
   const int lane = threadIdx.x;
   if (tile >= ntiles) return;
   if (FILL && *overflow) return;  // the lists do not fit: the pair kernel sums every source instead
-  const double4_32a tg = tileGeom[tile];
+  const float4 tg = tileGeom[tile];
   if (lane == 0) stack[0] = 0;  // the root (level 0, global index 0)
   __syncwarp();
   int sp = 1;
@@ -373,9 +374,12 @@ __global__ void __launch_bounds__(32) traverse(const double4_32a* __restrict__ t
     if (g >= 0) {
       pt = ptInds[g];
       if (pt.y > 0) {
-        const double4_32a ng = geom[g];
-        const double dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
-        const bool mac = (tg.w + ng.w) < theta * sqrt(dx * dx + dy * dy + dz * dz);
+        // (r_tile + r_node) < theta |c_tile - c_node|, squared and in FP32 (FP64 runs at 1/64
+        // of the FP32 rate; the radii carry 1e-6 margins); an infinite radius never passes
+        const float4 ng = geom[g];
+        const float dx = tg.x - ng.x, dy = tg.y - ng.y, dz = tg.z - ng.z;
+        const float rr = tg.w + ng.w;
+        const bool mac = rr * rr < theta2 * (dx * dx + dy * dy + dz * dz);
         while (lev < depth && g >= lv.base[lev + 1]) ++lev;
         if (mac && approx[g]) kind = 1;
         else if (mac && pt.y <= P) kind = 2;      // well separated but smaller than its proxy set
@@ -703,7 +707,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   int nnodes = 0;
   float4* tsp0 = nullptr;
   float4* tsp1 = nullptr;
-  double4_32a* geom = nullptr;
+  float4* geom = nullptr;
   int* approx = nullptr;
   int depth = 0;
   if (ns > 0) {
@@ -727,7 +731,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     sortedSelf<<<blocks(nslots), kBlock, 0, s>>>(Pl.dev.self, inv, nslots, ss);
     selfSorted = ss;
     // 4. upward pass (empty nodes return at once)
-    geom = grow<double4_32a>(bGeom, nnodes, s);
+    geom = grow<float4>(bGeom, nnodes, s);
     approx = grow<int>(bApprox, nnodes, s);
     upward<<<nnodes, kUpThreads, 0, s>>>(tree_.ptInds, tp.degree, chebFor(tp.degree), ns,
                                          depth >= 2 ? tree_.base[2] : nnodes, geom, approx, tsp0, tsp1);
@@ -743,7 +747,8 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
     tslot = grow<int>(bSlot, 1, s);
   }
   // 5. tiles
-  double4_32a* tgeom = grow<double4_32a>(bTileGeom, ntiles, s);
+  float4* tgeom = grow<float4>(bTileGeom, ntiles, s);
+  const float theta2 = (float)(tp.theta * tp.theta);
   tileGeometry<<<(ntiles + kGeomTilesPerBlock - 1) / kGeomTilesPerBlock, kBlock, 0, s>>>(
       Pl.stage.tx, nslots, Pl.treeTiles, ntiles, Pl.stage.perm, Pl.io.na, Pl.mask, tgeom);
   // 6. interaction lists: lengths, offsets (a device scan), the work order (a device sort) and
@@ -758,7 +763,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   ck(cudaMemsetAsync(terr, 0, 2 * sizeof(int), s), "memset");
   if (ns > 0) {
     traverse<false><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                          tp.theta, P, ns, lens, fars, nullptr, nullptr, overflow, terr);
+                                          theta2, P, ns, lens, fars, nullptr, nullptr, overflow, terr);
   } else {
     ck(cudaMemsetAsync(lens, 0, sizeof(int64_t) * ntiles, s), "memset");
     ck(cudaMemsetAsync(fars, 0, sizeof(int64_t) * ntiles, s), "memset");
@@ -796,7 +801,7 @@ void TreeEval::evaluate(SolvePlan& Pl, const TreeParams& tp, const PairShape& sh
   expandOrder<<<blocks(nitems), kBlock, 0, s>>>(keys2, ntiles, nchunks, order);
   if (ns > 0)
     traverse<true><<<ntiles, 32, 0, s>>>(tgeom, ntiles, geom, approx, tree_.ptInds, tree_.kids, lv, tree_.depth,
-                                         tp.theta, P, ns, nullptr, nullptr, off, list, overflow, terr);
+                                         theta2, P, ns, nullptr, nullptr, off, list, overflow, terr);
   report<<<1, 1, 0, s>>>(off + ntiles, overflow, terr, dWatch_);
   double* dstats = grow<double>(bStats, 5, s);
   treeStats<<<1, kBlock, 0, s>>>(Pl.treeTiles, lens, fars, ntiles, P, ns, overflow, ns > 0 ? tree_.dcount : nullptr,
