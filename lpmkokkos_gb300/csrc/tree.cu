@@ -50,6 +50,34 @@ __device__ __forceinline__ double blockSum(double v, double* sh) {
   for (int w = 0; w < NT / 32; ++w) t += sh[w];
   return t;
 }
+// FP32 versions: FP64 runs at 1/64 of the FP32 rate on GB300, and in a kernel whose work per
+// block is short, FP64 reductions over every thread are a large share of the FP64 pipe.
+template <int NT>
+__device__ __forceinline__ float blockSumF(float v, float* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.f;
+  for (int w = 0; w < NT / 32; ++w) t += sh[w];
+  return t;
+}
+template <int NT>
+__device__ __forceinline__ float blockMaxF(float v, float* sh) {
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_down_sync(0xffffffffu, v, o));
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = -FLT_MAX;
+  for (int w = 0; w < NT / 32; ++w) t = fmaxf(t, sh[w]);
+  return t;
+}
+__device__ __forceinline__ void kahanAddF(float& h, float& c, float v) {
+  const float y = v - c;
+  const float t = h + y;
+  c = (t - h) - y;
+  h = t;
+}
 template <int NT>
 __device__ __forceinline__ double blockMax(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
@@ -195,7 +223,7 @@ __device__ __forceinline__ void basisF(float u, int n, const float* t, const flo
 __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ ptInds, int degree, const Cheb C, int ns, int firstNode,
                                                      float4* __restrict__ geom, int* __restrict__ approx,
                                                      float4* __restrict__ sp0, float4* __restrict__ sp1) {
-  __shared__ double sh[kUpThreads / 32];
+  __shared__ float shf[kUpThreads / 32];
   __shared__ float sL[kUpThreads][2 * kMaxNodes1D];
   __shared__ float sT[kMaxNodes1D], sBw[kMaxNodes1D];
   if (threadIdx.x <= degree) {
@@ -222,9 +250,9 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
     const float4 a = sp0[k];
     fsx += a.x; fsy += a.y; fsz += a.z;
   }
-  const double sx = blockSum<kUpThreads>((double)fsx, sh);
-  const double sy = blockSum<kUpThreads>((double)fsy, sh);
-  const double sz = blockSum<kUpThreads>((double)fsz, sh);
+  const double sx = blockSumF<kUpThreads>(fsx, shf);
+  const double sy = blockSumF<kUpThreads>(fsy, shf);
+  const double sz = blockSumF<kUpThreads>(fsz, shf);
   const double cx = sx / pt.y, cy = sy / pt.y, cz = sz / pt.y;
   const double cn = sqrt(cx * cx + cy * cy + cz * cz);
   const bool cand = pt.y > P && cn > 1e-3;
@@ -260,12 +288,12 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
       }
     }
   }
-  const double rad = sqrt(blockMax<kUpThreads>((double)r2, sh)) + 1e-6;  // covers the FP32 rounding
-  const double dlo = -blockMax<kUpThreads>(-(double)dmin, sh);
-  double xlo = -blockMax<kUpThreads>(-(double)xmin, sh);
-  double xhi = blockMax<kUpThreads>((double)xmax, sh);
-  double ylo = -blockMax<kUpThreads>(-(double)ymin, sh);
-  double yhi = blockMax<kUpThreads>((double)ymax, sh);
+  const double rad = sqrt((double)blockMaxF<kUpThreads>(r2, shf)) + 1e-6;  // covers the FP32 rounding
+  const double dlo = -(double)blockMaxF<kUpThreads>(-dmin, shf);
+  double xlo = -(double)blockMaxF<kUpThreads>(-xmin, shf);
+  double xhi = blockMaxF<kUpThreads>(xmax, shf);
+  double ylo = -(double)blockMaxF<kUpThreads>(-ymin, shf);
+  double yhi = blockMaxF<kUpThreads>(ymax, shf);
   const bool valid = cand && dlo >= kMinChartCos && xhi > xlo && yhi > ylo;
   if (threadIdx.x == 0) {
     geom[g] = make_float4((float)cx, (float)cy, (float)cz, (float)rad);  // rad's 1e-6 margin covers the rounding
@@ -283,7 +311,7 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
   const float ulx = (float)(ux - (double)uhx), uly = (float)(uy - (double)uhy), ulz = (float)(uz - (double)uhz);
   const int t = threadIdx.x;
   const int ia = t / n1, ib = t % n1;
-  double q = 0.0;  // FP64 total of the per-chunk compensated FP32 sums
+  float qh = 0.f, qc = 0.f;  // the per-chunk compensated sums, themselves added with compensation
   for (int c0 = k0; c0 < k1; c0 += kUpThreads) {
     const int k = c0 + t;
     if (k < k1) {
@@ -312,15 +340,16 @@ __global__ void __launch_bounds__(kUpThreads) upward(const int2* __restrict__ pt
         c = (tt - h) - y;
         h = tt;
       }
-      q += (double)h - (double)c;
+      kahanAddF(qh, qc, h - c);
     }
     __syncthreads();
   }
   if (t < P) {
+    const double q = (double)qh - (double)qc;
     const double xi = mx + hx * C.t[ia], eta = my + hy * C.t[ib];
     double px = ux + xi * e1x + eta * e2x, py = uy + xi * e1y + eta * e2y, pz = uz + xi * e1z + eta * e2z;
-    const double pn = sqrt(px * px + py * py + pz * pz);
-    px /= pn; py /= pn; pz /= pn;
+    const double ip = 1.0 / sqrt(px * px + py * py + pz * pz);
+    px *= ip; py *= ip; pz *= ip;
     const float hx0 = __double2float_rn(px), hy0 = __double2float_rn(py), hz0 = __double2float_rn(pz);
     const int slot = ns + g * P + t;
     sp0[slot] = make_float4(hx0, hy0, hz0, __double2float_rn(q));
