@@ -249,10 +249,11 @@ def test_ensemble_with_the_tree_code(tctx):
 def test_server_with_the_tree_code(ctx):
     """A server created with LPM_BVE_TREECODE: the two icosahedral level-6 requests (1.2e10 pairs
     per evaluation, above min_pairs) are set up by the tree threads and stepped together in one
-    tree class (a captured tree-code step), the small ones in the batched direct classes.  Every
-    result equals the same request's result alone, bit for bit, and a tree request is within the
-    bar of an FP64 single solve."""
-    big = [(0, 6, 901), (0, 6, 905)]
+    tree class (a captured tree-code step, their evaluations on side streams); the cubed-sphere
+    level-7 request (2.3e10 pairs) runs in a second tree class beside it, the small ones in the
+    batched direct classes.  Every result equals the same request's result alone, bit for bit,
+    and a tree request is within the bar of an FP64 single solve."""
+    big = [(0, 6, 901), (0, 6, 905), (1, 7, 906)]
     small = [(0, 3, 902), (1, 4, 903), (1, 3, 904)]
 
     counters = []
@@ -266,14 +267,14 @@ def test_server_with_the_tree_code(ctx):
             counters.append(srv.stats())
             return [srv.result(i) for i in ids]
 
-    mix = run([small[0], big[0], small[1], big[1], small[2]])
+    mix = run([small[0], big[0], small[1], big[1], big[2], small[2]])
     # the tree requests' direct-sum-equivalent pairs are kept apart from the pairs computed
-    nv, nf, nl = bve.mesh_counts(0, 6)
-    assert counters[0]["tree_equiv_pairs"] == 2 * (1 + 4 * 3) * (nv + nf) * nl
+    equiv = sum((1 + 4 * 3) * (lambda c: (c[0] + c[1]) * c[2])(bve.mesh_counts(sk, lv)) for sk, lv, _ in big)
+    assert counters[0]["tree_equiv_pairs"] == equiv
     direct = sum((1 + 4 * 3) * (lambda c: (c[0] + c[1]) * c[2])(bve.mesh_counts(sk, lv)) for sk, lv, _ in small)
     assert counters[0]["pairs"] == direct
-    alone = run([big[0]]) + run([big[1]]) + run(small)
-    for got, want in zip([mix[1], mix[3], mix[0], mix[2], mix[4]], alone):
+    alone = run([big[0]]) + run([big[1]]) + run([big[2]]) + run(small)
+    for got, want in zip([mix[1], mix[3], mix[4], mix[0], mix[2], mix[5]], alone):
         for k in ("vx", "vvel", "fx", "fvel", "vzeta", "fzeta"):
             assert np.array_equal(got[k], want[k], equal_nan=True), k
     s = bve.BVESphere(0, 6)
