@@ -736,13 +736,10 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
 #pragma unroll
               for (int c = 0; c < NC; ++c) {
                 const float* row = myBuf + (c * kSymRed + lane) * kSymPitch;
-                float a0 = 0.f, a1 = 0.f;
+                float2 a = make_float2(0.f, 0.f);
 #pragma unroll
-                for (int k = 0; k < 32; k += 2) {
-                  a0 += row[k];
-                  a1 += row[k + 1];
-                }
-                myCross[c * ST + j0 + lane] = a0 + a1;
+                for (int k = 0; k < 32; k += 2) a = add2(a, make_float2(row[k], row[k + 1]));
+                myCross[c * ST + j0 + lane] = a.x + a.y;
               }
               __syncwarp();  // the buffer is rewritten by the next 32 sources
             }
