@@ -593,6 +593,7 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
                                                              int* __restrict__ counter) {
   constexpr int NTH = kSymThreads, K = kSymK, P = K / 2, ST = kSymSt, NC = symComps(PSI);
   static_assert(NTH == 128, "the cross-warp combine assumes four warps");
+  static_assert(kSymSt % (2 * kSymRed) == 0, "compensated adds every two transpose rounds");
   extern __shared__ __align__(16) unsigned char symShared[];
   float4* sXY = reinterpret_cast<float4*>(symShared);
   float4* sZW = sXY + ST;
@@ -657,11 +658,16 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
         // (source index == the target's own) dropped.  Otherwise forward and reverse terms.
         auto sweep = [&](auto diagTag) {
           constexpr bool DIAG = decltype(diagTag)::value;
+          // FP32 sub-block sums over two transpose rounds (64 sources) between compensated adds;
+          // one round with the stream function (whose longer-lived sums would spill)
+          constexpr int kRounds = PSI ? 1 : 2;
+          float2 vx[P], vy[P], vz[P], vp[P];
 #pragma unroll 1
           for (int j0 = 0; j0 < ST; j0 += kSymRed) {
-            float2 vx[P], vy[P], vz[P], vp[P];
+            if ((j0 / kSymRed) % kRounds == 0) {
 #pragma unroll
-            for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = vp[m] = make_float2(0.f, 0.f);
+              for (int m = 0; m < P; ++m) vx[m] = vy[m] = vz[m] = vp[m] = make_float2(0.f, 0.f);
+            }
 #pragma unroll 2
             for (int jj = 0; jj < kSymRed; ++jj) {
               const int j = j0 + jj;
@@ -708,6 +714,7 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
                 if constexpr (PSI) myBuf[(3 * kSymRed + jj) * kSymPitch + lane] = rp.x + rp.y;
               }
             }
+            if ((j0 / kSymRed) % kRounds == kRounds - 1) {
 #pragma unroll
             for (int m = 0; m < P; ++m) {
               kahanAdd(hx[2 * m], cx[2 * m], kSign * vx[m].x);
@@ -729,6 +736,7 @@ __global__ void __launch_bounds__(kSymThreads, 2) pairFP32CSym(const SolveDev* _
                   sPsi[(K + k) * NTH + threadIdx.x] = c;
                 }
               }
+            }
             }
             if constexpr (!DIAG) {
               __syncwarp();
