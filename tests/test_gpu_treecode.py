@@ -8,6 +8,8 @@ Masked icosahedral parents lie within ~1e-6 of a leaf, so their velocities are d
 near-singular pair in every path (some inf/NaN).  Comparisons therefore take vertices and leaf
 faces."""
 import math
+import threading
+import time
 
 import numpy as np
 import pytest
@@ -283,6 +285,37 @@ def test_server_with_the_tree_code(ctx):
     torch.cuda.synchronize()
     ref = s.velocityVerts.cpu().numpy()
     assert np.linalg.norm(mix[1]["vvel"] - ref) <= TOL * np.linalg.norm(ref)
+
+
+def test_server_tree_request_without_steps_and_shutdown():
+    """Tree-code server edge cases.  A tree request with no steps returns its initial state (the
+    initial velocity from its tree-code evaluation), equal to the same request alone, beside one
+    with a step.  A server destroyed while a tree request is being set up or stepped returns (its
+    evaluator and plan are released) instead of hanging."""
+    keys = ("vx", "vvel", "fx", "fvel", "vzeta", "fzeta")
+    spec = dict(ic_seed=911, n_gaussians=3, gauss_width=0.1)
+    with bve.Server(0, flags=P.FP32C | P.TREECODE, host_ic=True) as srv:
+        a = srv.submit(0, 6, 0.0025, 0, **spec)
+        b = srv.submit(0, 6, 0.0025, 1, ic_seed=912, n_gaussians=3, gauss_width=0.1)
+        assert srv.wait(a, 300.0) and srv.wait(b, 300.0)
+        ra, rb = srv.result(a), srv.result(b)
+        st = srv.stats()
+    nv, nf, nl = bve.mesh_counts(0, 6)
+    assert st["tree_equiv_pairs"] == (1 + 1 + 4) * (nv + nf) * nl
+    assert np.isfinite(rb["vvel"]).all() and not np.array_equal(ra["fx"], rb["fx"])
+    with bve.Server(0, flags=P.FP32C | P.TREECODE, host_ic=True) as srv:
+        a2 = srv.submit(0, 6, 0.0025, 0, **spec)
+        assert srv.wait(a2, 300.0)
+        alone = srv.result(a2)
+    for k in keys:
+        assert np.array_equal(ra[k], alone[k], equal_nan=True), k
+    srv = bve.Server(0, flags=P.FP32C | P.TREECODE)
+    srv.submit(0, 7, 0.00125, 50, ic_seed=913, n_gaussians=3, gauss_width=0.1)
+    time.sleep(0.5)
+    t = threading.Thread(target=srv.close, daemon=True)
+    t.start()
+    t.join(120.0)
+    assert not t.is_alive(), "server destroy did not return"
 
 
 @pytest.mark.parametrize("seed,level", [(0, 0), (0, 1), (1, 0), (1, 2)])
